@@ -1,0 +1,242 @@
+"""ctypes loader for the CPU checkers — TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
+import this module.  The product (``liblsg.so`` and its Python binding) never
+does.
+
+Two libraries are wrapped:
+
+* ``_build/liblsg_oracle.so`` — the project's C restatement of the reference
+  solvers (``lsg_oracle.c``); builds anywhere with gcc.
+* ``_ref/libref_mpi_real.so`` — the UNMODIFIED reference sources
+  (YaphetS-jx/Linear-Solver ``MPI_REAL``) compiled here by ``make ref`` against
+  a one-rank MPI shim, driven through ``ref_harness.c``.  Present only where
+  the reference checkout exists; used to pin the restatement.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liblsg_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libref_mpi_real.so")
+MAXR = 16
+
+SOLVERS = {"aar": 0, "pgr": 1, "pl2r": 2, "cg": 3}
+A_REF = -1.0 / (4.0 * math.pi)  # operator scale the reference driver passes (MPI_REAL/main.c:68)
+
+
+class OpStruct(C.Structure):
+    _fields_ = [("n", C.c_int * 3), ("radius", C.c_int), ("coeff", C.c_double * (MAXR + 1)),
+                ("a", C.c_double), ("sigma", C.c_double)]
+
+
+class ResultStruct(C.Structure):
+    _fields_ = [("iters", C.c_int), ("relres", C.c_double), ("rhs_norm", C.c_double),
+                ("converged", C.c_int), ("status", C.c_int), ("seconds", C.c_double)]
+
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+def build(with_ref: bool | None = None) -> None:
+    """Compile the oracle (and, where the reference checkout exists, the reference)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    ref_dir = os.environ.get("LSG_REFERENCE_DIR", "/root/reference/MPI_REAL")
+    if with_ref is None:
+        with_ref = os.path.isdir(ref_dir)
+    if with_ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_dir}"], check=True)
+
+
+_lib = None
+_ref = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build(with_ref=False)
+        L = C.CDLL(ORACLE_SO)
+        L.lsgo_lap_coefficient.argtypes = [_dp, C.c_int]
+        L.lsgo_op_init.argtypes = [C.POINTER(OpStruct), C.c_int, C.c_int, C.c_int, C.c_int,
+                                   C.c_double, C.c_double]
+        L.lsgo_diag.argtypes = [C.POINTER(OpStruct)]
+        L.lsgo_diag.restype = C.c_double
+        L.lsgo_apply.argtypes = [C.POINTER(OpStruct), _dp, _dp]
+        L.lsgo_pinv_solve.argtypes = [_dp, _dp, _dp, C.c_int]
+        L.lsgo_pinv_solve.restype = C.c_int
+        L.lsgo_aar.argtypes = [C.POINTER(OpStruct), C.c_int, _dp, _dp, C.c_double, C.c_double,
+                               C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(ResultStruct)]
+        for name in ("lsgo_pgr", "lsgo_pl2r"):
+            getattr(L, name).argtypes = [C.POINTER(OpStruct), C.c_int, _dp, _dp, C.c_double,
+                                         C.c_int, C.c_int, C.c_int, C.c_double,
+                                         C.POINTER(ResultStruct)]
+        L.lsgo_cg.argtypes = [C.POINTER(OpStruct), C.c_int, _dp, _dp, C.c_int, C.c_double,
+                              C.POINTER(ResultStruct)]
+        L.lsgo_reference_rhs.argtypes = [C.c_int, C.c_int, C.c_int, _dp]
+        L.lsgo_set_threads.argtypes = [C.c_int]
+        L.lsgo_max_threads.restype = C.c_int
+        L.lsgo_set_threads(1)
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def ref() -> C.CDLL:
+    global _ref
+    if _ref is None:
+        L = C.CDLL(REF_SO)
+        L.refh_rhs.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp]
+        L.refh_coefficients.argtypes = [C.c_int, _dp]
+        L.refh_apply.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp]
+        L.refh_solve.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int,
+                                 _dp, _dp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                                 C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double)]
+        L.refh_solve.restype = C.c_int
+        L.refh_pinv.argtypes = [_dp, _dp, _dp, C.c_int]
+        _ref = L
+    return _ref
+
+
+# ----------------------------------------------------------------------------- oracle wrappers
+
+def make_op(n, radius=6, a=A_REF, sigma=0.0) -> OpStruct:
+    nx, ny, nz = (n, n, n) if np.isscalar(n) else tuple(n)
+    op = OpStruct()
+    lib().lsgo_op_init(C.byref(op), nx, ny, nz, radius, a, sigma)
+    return op
+
+
+def coefficients(radius: int) -> np.ndarray:
+    c = np.zeros(radius + 1)
+    lib().lsgo_lap_coefficient(c, radius)
+    return c
+
+
+def apply(x: np.ndarray, radius=6, a=A_REF, sigma=0.0) -> np.ndarray:
+    """y = (a*Lap + sigma) x; x shaped (nz, ny, nx) or flat with n given by shape."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    nz, ny, nx = x.shape
+    op = make_op((nx, ny, nz), radius, a, sigma)
+    y = np.empty_like(x)
+    lib().lsgo_apply(C.byref(op), x.reshape(-1), y.reshape(-1))
+    return y
+
+
+def pinv_solve(A: np.ndarray, b: np.ndarray):
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros_like(b)
+    st = lib().lsgo_pinv_solve(A.reshape(-1), b, x, b.shape[0])
+    return x, st
+
+
+def reference_rhs(nx, ny=None, nz=None) -> np.ndarray:
+    ny = nx if ny is None else ny
+    nz = nx if nz is None else nz
+    b = np.empty(nx * ny * nz)
+    lib().lsgo_reference_rhs(nx, ny, nz, b)
+    return b.reshape(nz, ny, nx)
+
+
+def solve(solver: str, b: np.ndarray, x0=None, *, radius=6, a=A_REF, sigma=0.0, precond=True,
+          omega=0.6, beta=0.6, m=7, p=6, max_iter=100000, tol=1e-8, threads=1):
+    """Run one oracle solver; returns (x, result dict).  b shaped (nz, ny, nx)."""
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    nz, ny, nx = b.shape
+    op = make_op((nx, ny, nz), radius, a, sigma)
+    x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
+    res = ResultStruct()
+    L = lib()
+    L.lsgo_set_threads(threads)
+    try:
+        xf, bf = x.reshape(-1), b.reshape(-1)
+        if solver == "aar":
+            L.lsgo_aar(C.byref(op), int(precond), xf, bf, omega, beta, m, p, max_iter, tol, C.byref(res))
+        elif solver == "pgr":
+            L.lsgo_pgr(C.byref(op), int(precond), xf, bf, omega, m, p, max_iter, tol, C.byref(res))
+        elif solver == "pl2r":
+            L.lsgo_pl2r(C.byref(op), int(precond), xf, bf, omega, m, p, max_iter, tol, C.byref(res))
+        elif solver == "cg":
+            L.lsgo_cg(C.byref(op), int(precond), xf, bf, max_iter, tol, C.byref(res))
+        else:
+            raise ValueError(solver)
+    finally:
+        L.lsgo_set_threads(1)
+    return x, dict(iters=res.iters, relres=res.relres, rhs_norm=res.rhs_norm,
+                   converged=bool(res.converged), status=res.status, seconds=res.seconds)
+
+
+def ref_pinv(A: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """The reference's PseudoInverseTimesVec (needs ``make ref``)."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros_like(b)
+    ref().refh_pinv(A.reshape(-1), b, x, b.shape[0])
+    return x
+
+
+def ref_solve(solver: str, b: np.ndarray, x0=None, *, radius=6, a=A_REF, precond=True, omega=0.6,
+              beta=0.6, m=7, p=6, max_iter=100000, tol=1e-8):
+    """Run the compiled reference solver (needs ``make ref``); same conventions as solve()."""
+    b = np.array(b, dtype=np.float64, copy=True)
+    nz, ny, nx = b.shape
+    x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
+    it, rr, sec = C.c_int(0), C.c_double(0), C.c_double(0)
+    rc = ref().refh_solve(SOLVERS[solver], nx, ny, nz, radius, a, int(precond), x.reshape(-1),
+                          b.reshape(-1), omega, beta, m, p, max_iter, tol, C.byref(it),
+                          C.byref(rr), C.byref(sec))
+    if rc != 0:
+        raise RuntimeError(f"reference {solver} printed no report (rc={rc})")
+    return x, dict(iters=it.value, relres=rr.value, seconds=sec.value)
+
+
+# ----------------------------------------------------------------------------- FFT diagonal solve
+
+def symbol(shape, radius=6, a=A_REF, sigma=0.0, coeff=None):
+    """Eigenvalues of the periodic operator a*Lap + sigma on an (nz, ny, nx) grid.
+
+    The operator is a constant-coefficient circulant, so its DFT symbol is
+    a*(3 c_0 + sum_p 2 c_p (cos(2 pi p kx/nx) + cos(.. ky ..) + cos(.. kz ..))) + sigma.
+    """
+    nz, ny, nx = shape
+    c = coefficients(radius) if coeff is None else np.asarray(coeff)
+
+    def axis(n):
+        k = np.arange(n)
+        s = np.zeros(n)
+        for p in range(1, radius + 1):
+            s += 2.0 * c[p] * np.cos(2.0 * np.pi * p * k / n)
+        return s
+
+    lam = (3.0 * c[0] + axis(nz)[:, None, None] + axis(ny)[None, :, None] + axis(nx)[None, None, :])
+    return a * lam + sigma
+
+
+def fft_solve(b: np.ndarray, radius=6, a=A_REF, sigma=0.0, zero_mean=True):
+    """Exact solve of (a*Lap + sigma) x = b on the periodic grid (complex sigma allowed).
+
+    For the singular Poisson operator (sigma = 0) the zero mode is set to 0,
+    i.e. the mean-free solution is returned.
+    """
+    lam = symbol(b.shape, radius, a, 0.0) + sigma
+    bh = np.fft.fftn(b)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        xh = bh / lam
+    if zero_mean or sigma == 0:
+        xh[0, 0, 0] = 0.0 if sigma == 0 else xh[0, 0, 0]
+    x = np.fft.ifftn(xh)
+    if np.isrealobj(b) and np.isrealobj(np.asarray(sigma)):
+        return x.real
+    return x
