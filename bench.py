@@ -1,0 +1,354 @@
+#!/usr/bin/env python
+"""Benchmark: time to 1e-8 relative residual on the 256^3 periodic 12th-order
+Poisson problem with AAR (omega = beta = 0.6, m = 7, p = 6), mixed precision
+(FP32 inner AAR inside FP64 residual refinement) against plain FP64, on one
+GB300, plus the achieved HBM bandwidth of the dominant kernel.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl lsg|reference]
+
+A step is one complete solve from x0 = 0.  Inputs live in HBM before the
+timed region; every solve streams ~17 vectors of 67-134 MB, far more than the
+129 MB L2, so no flush is needed between steps.  For N > 1 (torchrun) each
+rank solves its own copy of the problem (replicas; the path has no data
+exchange on one GPU per rank), and the time is the max over ranks.
+
+--impl reference times the CPU implementation of the same path on the host
+cores: the C restatement of the reference solver (oracle/), run with every
+host thread on a bounded sample of iterations of the same problem and
+extrapolated to the iteration count the full solve needs.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "linear-solver_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+N_GRID = 256
+SEED = 1
+SOLVER_KW = dict(omega=0.6, beta=0.6, m=7, p=6, tol=1e-8)
+METRIC = "time to 1e-8 rel. residual, 256^3 Poisson AAR: mixed vs FP64 on GB300; HBM GB/s"
+WORKLOAD = ("256^3 periodic 12th-order FD Poisson (a = -1/(4 pi), FDn = 6, Jacobi), AAR m=7 p=6 "
+            "omega=beta=0.6, tol 1e-8, b ~ U[-0.5,0.5] seed 1 mean-free, x0 = 0")
+# Iterations the FP64 AAR needs on this workload (the reference's algorithm;
+# the CPU oracle and the GPU FP64 solver agree).  Used to extrapolate the
+# bounded CPU sample.
+LARGE_GOLDEN = os.path.join(ROOT, "tests", "golden", "large_256.json")
+CPU_SAMPLE_ITERS = 24
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            if self.t:
+                self.t.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _max_over_ranks(v: float, ws: int) -> float:
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _large_iters():
+    try:
+        with open(LARGE_GOLDEN) as f:
+            return int(json.load(f)["aar"]["iters"])
+    except Exception:
+        return None
+
+
+def cpu_sample(iters_full: int, threads: int | None = None):
+    """Times CPU_SAMPLE_ITERS iterations of the oracle AAR on the full workload
+    with every host thread; returns (seconds to solution, seconds/iter, threads)."""
+    import numpy as np
+
+    import workloads
+    from oracle import oracle as O
+
+    O.build(with_ref=False)
+    threads = threads or O.lib().lsgo_max_threads()
+    b = workloads.uniform_rhs(N_GRID, SEED)
+    kw = dict(SOLVER_KW)
+    _, r = O.solve("aar", b, None, max_iter=CPU_SAMPLE_ITERS, threads=threads, **kw)
+    per_iter = r["seconds"] / CPU_SAMPLE_ITERS
+    del np
+    return per_iter * iters_full, per_iter, threads
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    iters = _large_iters()
+    if iters is None:
+        print(json.dumps({"impl": "reference", "unavailable": "iteration count of the 256^3 "
+                          "workload not pinned (tests/golden/large_256.json missing)"}))
+        return 0
+    samples = []
+    threads = None
+    for i in range(args.warmup + args.steps):
+        tts, per_iter, threads = cpu_sample(iters)
+        if i >= args.warmup:
+            samples.append(tts)
+    value = statistics.mean(samples)
+    sample = (f"{CPU_SAMPLE_ITERS} of {iters} AAR iterations at 256^3 per step, "
+              f"extrapolated by the iteration count; {threads} threads")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "n": N_GRID, "solver": "AAR FP64",
+                                         "implementation": "C restatement of MPI_REAL AAR (oracle/), OpenMP"},
+        "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_lsg(args):
+    import numpy as np
+    import torch
+
+    import lsg
+    import workloads
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = N_GRID
+    op = lsg.Operator(n)
+    bh = workloads.uniform_rhs(n, SEED)
+    b = torch.from_numpy(bh).to(dev)
+    N = n ** 3
+    stream = torch.cuda.current_stream()
+
+    def solve_mixed():
+        return lsg.aar_mixed(op, b, **SOLVER_KW)
+
+    def solve_fp64():
+        return lsg.aar(op, b, **SOLVER_KW)
+
+    # ---- warm-up (also builds the work arrays)
+    for _ in range(args.warmup):
+        x, info = solve_mixed()
+    torch.cuda.synchronize()
+
+    # ---- timed region: K mixed solves, per-kernel CUDA-event profile on
+    lsg.profile(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    infos = []
+    with ClockSampler(local) as clk:
+        _barrier(ws)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            x, info = solve_mixed()
+            infos.append(info)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        _barrier(ws)
+    lsg.profile(False)
+    prof = lsg.profile_read()
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = _max_over_ranks(ms, ws)
+    value = ms / 1e3
+    true_res = ((b - lsg.apply(op, x)).norm() / b.norm()).item()
+
+    # ---- FP64 AAR (the drop-in's arithmetic) on the same problem
+    x64, i64 = solve_fp64()
+    torch.cuda.synchronize()
+    lsg.profile(True)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    x64, i64 = solve_fp64()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    lsg.profile(False)
+    prof64 = lsg.profile_read()
+    fp64_s = t0.elapsed_time(t1) / 1e3
+    true64 = ((b - lsg.apply(op, x64)).norm() / b.norm()).item()
+
+    # ---- end to end: the reference-prototype AAR(POISSON*, ...) on pinned host
+    # buffers (H2D of x0 and rhs, D2H of x inside the timed region), mixed mode
+    xh = torch.zeros((n, n, n), dtype=torch.float64).pin_memory()
+    rh = torch.from_numpy(bh).pin_memory()
+    lsg.set_compat_mode(True)
+    xh.zero_()
+    lsg.compat_solve("aar", xh.numpy(), rh.numpy(), **SOLVER_KW)  # warm the staging buffers
+    e2e = []
+    for _ in range(args.steps):
+        xh.zero_()
+        torch.cuda.synchronize()
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        ri = lsg.compat_solve("aar", xh.numpy(), rh.numpy(), **SOLVER_KW)
+        c1.record(stream)
+        torch.cuda.synchronize()
+        e2e.append(c0.elapsed_time(c1) / 1e3)
+    lsg.set_compat_mode(False)
+    e2e_s = _max_over_ranks(statistics.mean(e2e), ws)
+    e2e_ok = ri["status"] == 0
+
+    # ---- roofline of the dominant kernel (FP32 fused Richardson step)
+    peak, peak_kind = _peaks()
+    rl, rms = prof["richardson"]
+    rich_ms = rms / max(rl, 1)
+    rich_bytes = 7 * N * 4  # reads x, r, b; writes x', r', DX_col, DF_col
+    achieved = rich_bytes / (rich_ms * 1e-3) / 1e9
+    total_ms = sum(v[1] for v in prof.values())
+    r64l, r64ms = prof64["richardson"]
+    rich64_ms = r64ms / max(r64l, 1)
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        iters_full = i64["iters"]
+        tts, per_iter, threads = cpu_sample(iters_full)
+        cpu = {"value": tts, "unit": "s", "cores": threads, "kind": "port",
+               "sample": f"{CPU_SAMPLE_ITERS} of {iters_full} AAR iterations of the same 256^3 "
+                         f"workload on {threads} threads, extrapolated by the iteration count",
+               "seconds_per_iter": per_iter}
+
+    launches = sum(i["launches"] for i in infos)
+    line = {
+        "metric": METRIC, "value": value, "unit": "s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 inner / f64 refinement", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "solver": "AAR mixed (lsg_aar_mixed)",
+                   "l2": "no flush: each solve streams ~17 vectors of 67-134 MB (> 129 MB L2)",
+                   "parallelism": f"replicas x{ws}"},
+        "mixed": {"inner_iters": infos[-1]["inner_iters"], "outer_iters": infos[-1]["outer_iters"],
+                  "relres": infos[-1]["relres"], "true_relres_fp64": true_res},
+        "fp64": {"seconds": fp64_s, "iters": i64["iters"], "relres": i64["relres"],
+                 "true_relres": true64, "speedup_mixed_vs_fp64": fp64_s / value,
+                 "richardson_ms": rich64_ms,
+                 "richardson_gpts": N / (rich64_ms * 1e-3) / 1e9},
+        "roofline": {"bound": "hbm", "kernel": "richardson<float> (fused stencil step)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
+                     "traffic": None, "bytes_per_launch": rich_bytes, "avg_launch_ms": rich_ms,
+                     "share_of_kernel_time": rms / total_ms if total_ms else None},
+        "kernel_profile_ms": {k: round(v[1] / args.steps, 4) for k, v in prof.items() if v[0]},
+        "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 2 * N * 8,
+                "d2h_bytes_per_step": N * 8, "path": "AAR(POISSON*, ...) drop-in, mixed mode, pinned host buffers",
+                "converged": e2e_ok},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="lsg", choices=["lsg", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_lsg(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,158 @@
+/*
+ * lsg.h — native C ABI of liblsg, the GB300 (sm_103a) AAR / PGR / PL2R / CG
+ * solvers for the periodic high-order finite-difference operator
+ *
+ *     A = a * Lap_h + sigma * I,   Lap_h = 3-D periodic central-difference
+ *                                  Laplacian of half-width `radius` (FDn)
+ *
+ * on an nx x ny x nz grid stored x-fastest (flat index i + j*nx + k*nx*ny,
+ * the layout of MPI_REAL/system.c:82).  Every vector argument is a DEVICE
+ * pointer owned by the caller; the library allocates its own work arrays
+ * (cached per device, grid and history size; see lsg_release_workspaces).
+ *
+ * Plain C: no CUDA or torch types appear here.  `stream` is a cudaStream_t
+ * passed as void* (NULL = the legacy default stream).  Every call returns an
+ * lsg_status; none of them exits or aborts the process.
+ *
+ * The drop-in entry points with the reference's own prototypes (AAR, PGR,
+ * PL2R, CG on host buffers) are declared in lsg_compat.h.
+ */
+#ifndef LSG_H
+#define LSG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LSG_MAX_RADIUS 8
+#define LSG_MAX_M 32
+
+typedef enum lsg_status {
+    LSG_OK = 0,
+    LSG_NOT_CONVERGED = 1,     /* max_iter reached; the result holds the last residual */
+    LSG_NAN_DETECTED = 2,      /* a residual norm or Gram entry became NaN/Inf */
+    LSG_BAD_ARG = 3,           /* invalid size / parameter / NULL pointer */
+    LSG_CUDA_ERROR = 4,        /* a CUDA call failed (message via lsg_last_error) */
+    LSG_TIMEOUT = 5,           /* a bounded device wait gave up */
+    LSG_UNSUPPORTED = 6,       /* valid request this build does not serve */
+    LSG_NO_MEMORY = 7,         /* device allocation failed */
+    LSG_SVD_NO_CONVERGENCE = 8 /* the m x m Jacobi SVD hit its sweep limit */
+} lsg_status;
+
+typedef enum lsg_dtype {
+    LSG_F64 = 0, /* double vectors, FP64 arithmetic */
+    LSG_F32 = 1  /* float vectors and stencil; reductions and the m x m solve in FP64 */
+} lsg_dtype;
+
+/* The operator.  coeff[] are the 1-D Laplacian FD coefficients c_0..c_radius
+ * of MPI_REAL/system.c:480-498 (lsg_lap_coefficient fills them). */
+typedef struct lsg_operator {
+    int n[3];                          /* grid points along x, y, z */
+    int radius;                        /* FDn, 1..LSG_MAX_RADIUS */
+    double coeff[LSG_MAX_RADIUS + 1];  /* c_0..c_radius */
+    double a;                          /* Laplacian scale (the reference passes -1/(4 pi)) */
+    double sigma;                      /* real diagonal shift; 0 = the reference operator */
+    int precond;                       /* 1: Jacobi, f = r / (3 a c_0 + sigma); 0: none */
+} lsg_operator;
+
+/* Solver parameters, named as the reference's arguments (MPI_REAL/AAR.h:18-22). */
+typedef struct lsg_params {
+    double omega;        /* Richardson relaxation (AAR, PGR, PL2R) */
+    double beta;         /* Anderson mixing (AAR) */
+    int m;               /* history depth, 1..LSG_MAX_M */
+    int p;               /* extrapolation / projection period */
+    int max_iter;        /* iteration limit (inner limit for the mixed solver) */
+    double tol;          /* stop when ||b - A x|| <= tol * ||b|| */
+    /* mixed-precision iterative refinement (lsg_aar_mixed) */
+    double inner_tol;    /* relative reduction asked of each FP32 inner solve (0 = 1e-3) */
+    int max_outer;       /* FP64 refinement steps (0 = 50) */
+    /* execution */
+    int check_every;     /* extrapolation cycles enqueued between convergence reads (0 = auto) */
+} lsg_params;
+
+typedef struct lsg_result {
+    int iters;           /* iteration count as the reference reports it (AAR.c:153) */
+    double relres;       /* last computed ||r|| / ||b|| (the reference's printed value) */
+    double rhs_norm;     /* ||b|| */
+    int status;          /* lsg_status of the solve */
+    int outer_iters;     /* mixed solver: FP64 refinement steps taken */
+    int inner_iters;     /* mixed solver: total FP32 iterations */
+    double seconds;      /* host wall time of the call */
+    long long launches;  /* kernels launched by the call */
+} lsg_result;
+
+/* Fills c[0..radius] with the reference FD coefficients.  Returns LSG_BAD_ARG
+ * outside 1..LSG_MAX_RADIUS. */
+int lsg_lap_coefficient(int radius, double *c);
+
+/* Fills op for the reference operator of half-width `radius` scaled by a,
+ * shifted by sigma, with (precond=1) or without Jacobi preconditioning. */
+int lsg_operator_init(lsg_operator *op, int nx, int ny, int nz, int radius, double a,
+                      double sigma, int precond);
+
+/* Reference parameter defaults: omega = beta = 0.6, m = 7, p = 6, tol = 1e-8,
+ * max_iter = 100000 (MPI_REAL/main.c:37, README:18-21). */
+void lsg_params_default(lsg_params *prm);
+
+/* y = A x on the device (replaces MPI_REAL/system.c:80-213). */
+int lsg_apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, void *stream);
+
+/* Solvers.  d_x: initial guess in, solution out.  d_b: right-hand side.
+ * dtype selects double or float vectors.  res may be NULL. */
+int lsg_aar(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
+            const void *d_b, lsg_result *res, void *stream);   /* MPI_REAL/AAR.c:37 */
+int lsg_pgr(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
+            const void *d_b, lsg_result *res, void *stream);   /* MPI_REAL/PGR.c:35 */
+int lsg_pl2r(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
+             const void *d_b, lsg_result *res, void *stream);  /* MPI_REAL/PL2R.c:35 */
+int lsg_cg(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
+           const void *d_b, lsg_result *res, void *stream);    /* MPI_REAL/CG.c:33 */
+
+/* Mixed precision: FP64 x and b; outer FP64 residual refinement around an
+ * FP32 inner AAR (FP32 vectors, history and stencil; FP64 reductions and m x m
+ * solve).  Stops when the FP64 residual satisfies tol. */
+int lsg_aar_mixed(const lsg_operator *op, const lsg_params *prm, double *d_x, const double *d_b,
+                  lsg_result *res, void *stream);
+
+/* m x m pseudo-inverse solve with the reference's semantics
+ * (x = V diag(1/w) V^T b, w < m*wmax*2.22044605e-16 dropped; MPI_REAL/tools.c:52-105),
+ * computed on the device by one warp.  A row-major, device pointers. */
+int lsg_pinv_solve(const double *d_A, const double *d_b, double *d_x, int m, void *stream);
+
+/* Per-kernel-class device time, measured with CUDA events recorded on the
+ * solve's stream around each launch while profiling is on. */
+enum lsg_kernel_class {
+    LSG_K_RICHARDSON = 0, /* fused Richardson stencil step */
+    LSG_K_RESIDUAL = 1,   /* residual / operator stencil */
+    LSG_K_GRAM = 2,       /* history Gram reduction */
+    LSG_K_UPDATE = 3,     /* extrapolation / projection / CG vector updates */
+    LSG_K_SMALL = 4,      /* single-block finalize and m x m solve */
+    LSG_K_CG = 5,         /* CG direction + operator stencil */
+    LSG_K_REFINE = 6,     /* FP64 refinement residual and correction */
+    LSG_K_CLASSES = 8
+};
+typedef struct lsg_kernel_stats {
+    long long launches[LSG_K_CLASSES];
+    double ms[LSG_K_CLASSES];
+} lsg_kernel_stats;
+/* on = 1 starts collecting (and clears the totals), 0 stops. */
+int lsg_profile(int on);
+/* Copies the totals collected so far. */
+int lsg_profile_read(lsg_kernel_stats *stats);
+
+/* Frees every cached work array on the current device. */
+int lsg_release_workspaces(void);
+
+/* Status of the last compat-entry-point call on this thread (AAR/PGR/PL2R/CG
+ * return void) and a human-readable message for the last failure. */
+int lsg_last_status(void);
+const char *lsg_last_error(void);
+const char *lsg_status_string(int status);
+
+/* Library version string. */
+const char *lsg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LSG_H */

@@ -1,0 +1,29 @@
+// lsg_host.h — host-side internals shared by lsg_solvers.cu and lsg_compat.cpp.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/lsg.h"
+
+namespace lsg {
+
+int set_error(int status, const char *fmt, ...);
+void set_last_status(int st);
+int last_status();
+const char *last_error();
+
+// The reference FD coefficients c_0..c_radius (MPI_REAL/system.c:480-498).
+int lap_coefficient(int radius, double *c);
+int check_operator(const lsg_operator *op);
+double jacobi_diag(const lsg_operator *op);
+
+// solver: 0 AAR, 1 PGR, 2 PL2R, 3 CG
+int solve(int solver, const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
+          const void *d_b, lsg_result *res, cudaStream_t s);
+int solve_mixed(const lsg_operator *op, const lsg_params *prm, double *x, const double *b,
+                lsg_result *res, cudaStream_t s);
+int apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, cudaStream_t s);
+int pinv(const double *A, const double *b, double *x, int m, cudaStream_t s);
+int release_workspaces();
+
+}  // namespace lsg

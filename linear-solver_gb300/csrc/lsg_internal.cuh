@@ -1,0 +1,232 @@
+// lsg_internal.cuh — definitions shared by the liblsg kernels and host code.
+//
+// Device-resident solver state, reduction helpers and the kernel launch
+// interface between the per-dtype kernel files and the host solver loops.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/lsg.h"
+
+namespace lsg {
+
+// ----------------------------------------------------------------------------
+// Device control block: one per workspace.  Kernels of a solve read `done`
+// first and return at once when it is set, so the host can enqueue several
+// extrapolation cycles ahead of its convergence read without changing the
+// result (the iteration at which `done` was set is kept in `iters`).
+struct DevCtrl {
+    int done;         // 1: converged, failed or stopped -> later kernels are no-ops
+    int status;       // lsg_status raised on the device (NaN, SVD sweep limit)
+    int iters;        // reference iteration count at exit (AAR.c:153 reports iter-1)
+    int pad0;
+    double rhs_norm;  // ||b||
+    double tol_abs;   // tol * ||b||  (AAR.c:79)
+    double relres;    // last computed ||r|| (absolute)
+    double alpha;     // CG step length
+    double beta;      // CG direction update
+    double delta;     // CG r.s
+    double dq;        // CG d.q
+    double best;      // smallest relres seen (stall detection of inner solves)
+    int stall;        // checks since relres last fell below 0.7 * best
+    int stall_limit;  // 0: off; else stop (done, stalled = 1) after this many checks
+    int stalled;      // set when the stall rule ended the solve
+    int pad1;
+    double s[LSG_MAX_M];  // m x m solve output
+};
+
+// Geometry of one periodic grid.
+struct Geom {
+    int nx, ny, nz;
+    long long nxy;
+    long long n;
+};
+
+inline Geom make_geom(const int n[3]) {
+    Geom g;
+    g.nx = n[0]; g.ny = n[1]; g.nz = n[2];
+    g.nxy = (long long)n[0] * n[1];
+    g.n = g.nxy * n[2];
+    return g;
+}
+
+// Stencil weights in the arithmetic type: w[0] = 3*a*c_0 + sigma (centre),
+// w[p] = a*c_p.  Passed by value (kernel parameter space).
+template <typename T>
+struct Weights {
+    T w[LSG_MAX_RADIUS + 1];
+    int radius;
+};
+
+// ----------------------------------------------------------------------------
+// Reductions.  Every reducing kernel writes one partial per block (FP64) to a
+// partials array; a single-block finalize kernel sums them in a fixed order,
+// so results are run-to-run deterministic.
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sums NV per-thread values over the block and writes them to out[0..NV) from
+// thread 0.  `scratch` needs NV * (blockDim/32) doubles of shared memory.
+template <int NV>
+__device__ __forceinline__ void block_sum_store(double (&v)[NV], double *scratch, double *out) {
+    const int lane = threadIdx.x & 31;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int warp = tid >> 5;
+    const int nwarps = (blockDim.x * blockDim.y) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        double s = warp_sum(v[k]);
+        if ((tid & 31) == 0) scratch[k * nwarps + warp] = s;
+    }
+    (void)lane;
+    __syncthreads();
+    if (tid < 32) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = tid < nwarps ? scratch[k * nwarps + tid] : 0.0;
+            s = warp_sum(s);
+            if (tid == 0) out[k] = s;
+        }
+    }
+}
+
+// Periodic index wrap valid for any integer v and n >= 1.
+__host__ __device__ __forceinline__ int wrap_index(int v, int n) {
+    int r = v % n;
+    return r < 0 ? r + n : r;
+}
+
+// ----------------------------------------------------------------------------
+// Kernel launch interface (implemented per dtype in lsg_kernels.cu).
+
+enum ResidualMode {
+    RES_INIT = 0,     // r = b - A x;                        acc ||r||^2
+    RES_ANDERSON = 1, // r_new = b - A x; DF = (r_new-r)*cf; r = r_new;  acc ||r_new||^2
+    RES_APPLY = 2,    // y = A x (no b, no reduction)
+};
+
+enum RichMode {
+    RICH_AAR = 0,     // DF = (r_new - r) * cf   (difference of preconditioned residuals)
+    RICH_PGR = 1,     // DF = r - r_new          (= A x_new - A x)
+};
+
+enum GramKind {
+    GRAM_SYM = 0,     // G(i,j) = DF_i.DF_j (i <= j, symmetrised), h(j) = DF_j.r * hscale
+    GRAM_GALERKIN = 1 // G(i,j) = DX_i.DF_j (all i,j), h(j) = DX_j.r * hscale
+};
+
+struct StencilLaunch {
+    Geom g;
+    int lz;           // z planes per block
+    cudaStream_t stream;
+};
+
+// Tile shape per vector type: FP64 is ALU-bound (narrower tile, fewer live
+// registers); FP32 is bandwidth-bound (taller tile, less halo per point).
+// A block is 32 x BY threads covering 32 x (BY*NY) columns.
+template <typename T> struct TileOf;
+template <> struct TileOf<double> { static constexpr int BY = 8, NY = 2; };
+template <> struct TileOf<float> { static constexpr int BY = 8, NY = 4; };
+
+inline dim3 stencil_grid(const Geom &g, int ty, int lz) {
+    return dim3((unsigned)((g.nx + 31) / 32), (unsigned)((g.ny + ty - 1) / ty),
+                (unsigned)((g.nz + lz - 1) / lz));
+}
+
+// z planes per block: enough blocks for ~4 per SM, at least 16 planes so the
+// 2R-plane warm-up of the register queue stays a small fraction.
+template <typename T>
+inline int choose_lz(const Geom &g, int sms) {
+    const int ty = TileOf<T>::BY * TileOf<T>::NY;
+    const long long bxy = (long long)((g.nx + 31) / 32) * ((g.ny + ty - 1) / ty);
+    long long chunks = (4LL * sms + bxy - 1) / bxy;
+    if (chunks < 1) chunks = 1;
+    int lz = (int)((g.nz + chunks - 1) / chunks);
+    if (lz < 16) lz = 16;
+    if (lz > g.nz) lz = g.nz;
+    return lz;
+}
+
+// Blocks (and so partial sums) of one stencil launch.
+template <typename T>
+inline long long stencil_blocks(const Geom &g, int lz) {
+    const dim3 d = stencil_grid(g, TileOf<T>::BY * TileOf<T>::NY, lz);
+    return (long long)d.x * d.y * d.z;
+}
+
+template <typename T>
+struct Kernels {
+    // y / r update driven by one stencil pass over x.
+    static cudaError_t residual(const StencilLaunch &L, const Weights<T> &w, int mode,
+                                const T *x, const T *b, T *r, T *df, double cf,
+                                double *partials, const DevCtrl *ctrl);
+    // Fused Richardson step: u = x + c*r at every stencil point; r2 = b - A u;
+    // x2 = u; DX = u - x; DF per mode.
+    static cudaError_t richardson(const StencilLaunch &L, const Weights<T> &w, int mode,
+                                  const T *x, const T *r, const T *b, T *x2, T *r2, T *dx,
+                                  T *df, double c, double cf, const DevCtrl *ctrl);
+    // Gram partials over the history (point-local, grid-stride).
+    static cudaError_t gram(int kind, int m, const T *dx, const T *df, const T *r, long long n,
+                            double *partials, int blocks, const DevCtrl *ctrl, cudaStream_t s);
+    // AAR extrapolation: x += beta*f - sum_j (DX_j + beta DF_j) s_j with f = r*cf;
+    // DX_col = x_new - x_old.
+    static cudaError_t aar_update(int m, int col, T *x, const T *r, T *dx, const T *df,
+                                  double beta, double cf, long long n, const DevCtrl *ctrl,
+                                  cudaStream_t s);
+    // PGR/PL2R projection: tx = DX s, tf = DF s; x += tx; r -= tf; DX_col += tx;
+    // DF_col += tf; partial ||r||^2.
+    static cudaError_t proj_update(int m, int col, T *x, T *r, T *dx, T *df, long long n,
+                                   double *partials, int blocks, const DevCtrl *ctrl,
+                                   cudaStream_t s);
+    // CG: d_new = r*cf + beta*d_old at every stencil point; q = A d_new; partial d.q.
+    static cudaError_t cg_direction(const StencilLaunch &L, const Weights<T> &w, const T *r,
+                                    const T *d_old, T *d_new, T *q, double cf,
+                                    double *partials, const DevCtrl *ctrl);
+    // CG: x += alpha d; r -= alpha q (restart=0) ; partials r.r (and r.s = cf*r.r).
+    static cudaError_t cg_step(T *x, T *r, const T *d, const T *q, long long n, int restart,
+                               double *partials, int blocks, const DevCtrl *ctrl,
+                               cudaStream_t s);
+    // partial ||v||^2 (grid-stride)
+    static cudaError_t norm2(const T *v, long long n, double *partials, int blocks,
+                             const DevCtrl *ctrl, cudaStream_t s);
+    // x += alpha*y  (alpha from the host)
+    static cudaError_t axpy(T *x, const T *y, double alpha, long long n, cudaStream_t s);
+};
+
+// Mixed-precision helpers (lsg_kernels.cu).
+// r32 = float(b - A x64), partial ||b - A x64||^2 (FP64 stencil).
+cudaError_t ir_residual(const StencilLaunch &L, const Weights<double> &w, const double *x,
+                        const double *b, float *r32, double *partials, const DevCtrl *ctrl);
+// x64 += e32
+cudaError_t ir_correct(double *x, const float *e, long long n, cudaStream_t s);
+
+// Finalize kernels (lsg_small.cu).
+enum NormFinal {
+    NF_RHS = 0,       // rhs_norm = sqrt(sum); tol_abs = tol * rhs_norm
+    NF_CHECK = 1,     // relres = sqrt(sum); done if relres <= tol_abs (iters = iter)
+    NF_STORE = 2,     // relres = sqrt(sum) only
+};
+cudaError_t finalize_norm(const double *partials, int nparts, DevCtrl *ctrl, int mode,
+                          double tol, int iter, cudaStream_t s);
+// Sums Gram partials, assembles G (m x m) and h (m), solves s = pinv(G) h with
+// the reference semantics into ctrl->s.  hscale multiplies h.
+cudaError_t finalize_gram_solve(const double *partials, int nparts, int kind, int m,
+                                double hscale, DevCtrl *ctrl, cudaStream_t s);
+// CG scalars: mode 0: alpha = delta / sum(d.q).  mode 1: delta_new = cf*sum(r.r),
+// relres = sqrt(sum r.r), beta = delta_new/delta_old, convergence test.
+cudaError_t finalize_cg(const double *partials, int nparts, DevCtrl *ctrl, int mode, double cf,
+                        int precond, int iter, int max_iter, cudaStream_t s);
+cudaError_t pinv_solve_dev(const double *A, const double *b, double *x, int m, int *status,
+                           cudaStream_t s);
+
+// Number of Gram values per block for a kind and history depth.
+__host__ __device__ inline int gram_values(int kind, int m) {
+    return kind == GRAM_SYM ? (m * (m + 1)) / 2 + m : m * m + m;
+}
+
+}  // namespace lsg

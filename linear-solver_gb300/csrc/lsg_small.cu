@@ -1,0 +1,271 @@
+// lsg_small.cu — single-block kernels that turn per-block partial sums into
+// the scalars a solve needs, and the m x m pseudo-inverse solve.
+//
+//   finalize_norm        ||v|| from partials; convergence test     tools.c:18-28, AAR.c:91,123
+//   finalize_gram_solve  Gram assembly + s = pinv(G) h             AAR.c:212-223; PGR.c:206-217;
+//                                                                  PL2R.c:206-217; tools.c:52-105
+//   finalize_cg          alpha / beta / delta / relres             CG.c:100-104, 131-148
+//
+// The pseudo-inverse keeps the reference's semantics: with A = U W V^T,
+//     x = V diag(1/w_j) V^T b,   terms with w_j < m * wmax * 2.22044605e-16 dropped
+// (tools.c:325-335 assign V to U before forming the product, exact for the
+// symmetric Gram of AAR / PL2R; for PGR's DX^T DF it is (A^T A)^{+1/2} b).
+// The SVD is a one-sided (Hestenes) Jacobi iteration, written here from the
+// mathematics: rotate column pairs of G = A V until they are orthogonal; then
+// w_j = ||G(:,j)|| and V holds the right singular vectors.  Lanes own rows,
+// so the column dot products are warp reductions.  The sweep count is bounded
+// and exhaustion is reported as LSG_SVD_NO_CONVERGENCE (the reference exits
+// the process after 250 iterations, tools.c:270).
+#include "lsg_internal.cuh"
+
+namespace lsg {
+
+constexpr int kFinThreads = 256;
+constexpr int kMaxSweeps = 60;
+constexpr double kPinvEps = 2.22044605e-16;
+
+__device__ __forceinline__ bool ctrl_done(const DevCtrl *c) { return *(volatile const int *)&c->done; }
+
+// Sum of partials[k*stride + off] over k < nparts, block-wide, deterministic.
+__device__ double block_sum_partials(const double *partials, int nparts, int stride, int off,
+                                     double *red) {
+    double s = 0.0;
+    for (int k = threadIdx.x; k < nparts; k += blockDim.x) s += partials[(long long)k * stride + off];
+    s = warp_sum(s);
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[w] = s;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < nw ? red[threadIdx.x] : 0.0;
+        t = warp_sum(t);
+    }
+    return t;  // valid in warp 0
+}
+
+__global__ void finalize_norm_kernel(const double *partials, int nparts, DevCtrl *ctrl, int mode,
+                                     double tol, int iter) {
+    __shared__ double red[32];
+    if (mode != NF_RHS && ctrl_done(ctrl)) return;
+    const double s = block_sum_partials(partials, nparts, 1, 0, red);
+    if (threadIdx.x != 0) return;
+    const double v = sqrt(s);
+    if (mode == NF_RHS) {
+        ctrl->rhs_norm = v;
+        ctrl->tol_abs = tol * v;
+        if (!isfinite(v)) { ctrl->status = LSG_NAN_DETECTED; ctrl->done = 1; ctrl->iters = 0; }
+        return;
+    }
+    ctrl->relres = v;
+    if (mode == NF_CHECK) {
+        if (!isfinite(v)) {
+            ctrl->status = LSG_NAN_DETECTED;
+            ctrl->done = 1;
+            ctrl->iters = iter;
+        } else if (!(v > ctrl->tol_abs)) {  // the loop test of AAR.c:91 fails
+            ctrl->done = 1;
+            ctrl->iters = iter;
+        } else if (ctrl->stall_limit > 0) {
+            if (v < 0.7 * ctrl->best) {
+                ctrl->best = v;
+                ctrl->stall = 0;
+            } else if (++ctrl->stall >= ctrl->stall_limit) {
+                ctrl->done = 1;
+                ctrl->stalled = 1;
+                ctrl->iters = iter;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- m x m solve
+
+// One warp; G and V in shared memory (row-major, ld = m); lane k owns row k.
+// Returns 0 on convergence, LSG_SVD_NO_CONVERGENCE otherwise.
+__device__ int warp_pinv(double *G, double *V, const double *b, double *x, int m) {
+    const int lane = threadIdx.x & 31;
+    for (int i = lane; i < m * m; i += 32) V[i] = (i / m == i % m) ? 1.0 : 0.0;
+    __syncwarp();
+    bool rotated = true;
+    int sweep = 0;
+    for (; sweep < kMaxSweeps && rotated; sweep++) {
+        rotated = false;
+        for (int i = 0; i < m - 1; i++) {
+            for (int j = i + 1; j < m; j++) {
+                double gi = 0.0, gj = 0.0;
+                if (lane < m) { gi = G[lane * m + i]; gj = G[lane * m + j]; }
+                double al = gi * gi, be = gj * gj, ga = gi * gj;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    al += __shfl_xor_sync(0xffffffffu, al, o);
+                    be += __shfl_xor_sync(0xffffffffu, be, o);
+                    ga += __shfl_xor_sync(0xffffffffu, ga, o);
+                }
+                if (ga == 0.0 || fabs(ga) <= kPinvEps * sqrt(al * be)) continue;
+                rotated = true;
+                const double zeta = (be - al) / (2.0 * ga);
+                double t;
+                if (fabs(zeta) > 1e150) t = 0.5 / zeta;
+                else t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                const double c = 1.0 / sqrt(1.0 + t * t);
+                const double s = c * t;
+                if (lane < m) {
+                    G[lane * m + i] = c * gi - s * gj;
+                    G[lane * m + j] = s * gi + c * gj;
+                    const double vi = V[lane * m + i], vj = V[lane * m + j];
+                    V[lane * m + i] = c * vi - s * vj;
+                    V[lane * m + j] = s * vi + c * vj;
+                }
+                __syncwarp();
+            }
+        }
+    }
+    // Singular values, cutoff and x = V diag(1/w) V^T b.
+    double w = 0.0;  // lane j holds w_j
+    for (int j = 0; j < m; j++) {
+        double g = lane < m ? G[lane * m + j] : 0.0;
+        g = g * g;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
+        if (lane == j) w = sqrt(g);
+    }
+    double wmax = lane < m ? w : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wmax = fmax(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+    const double wmin = m * wmax * kPinvEps;
+    // t_j = (V^T b)_j / w_j  (lane j)
+    double tj = 0.0;
+    if (lane < m && w >= wmin && w > 0.0) {
+        for (int i = 0; i < m; i++) tj += V[i * m + lane] * b[i];
+        tj /= w;
+    }
+    // x_i = sum_j V(i,j) t_j  (lane i)
+    double xi = 0.0;
+    for (int j = 0; j < m; j++) {
+        const double t = __shfl_sync(0xffffffffu, tj, j);
+        if (lane < m) xi += V[lane * m + j] * t;
+    }
+    if (lane < m) x[lane] = xi;
+    return rotated ? LSG_SVD_NO_CONVERGENCE : 0;
+}
+
+__global__ void finalize_gram_solve_kernel(const double *partials, int nparts, int kind, int m,
+                                           double hscale, DevCtrl *ctrl) {
+    __shared__ double vals[LSG_MAX_M * LSG_MAX_M + LSG_MAX_M];
+    __shared__ double G[LSG_MAX_M * LSG_MAX_M], V[LSG_MAX_M * LSG_MAX_M];
+    __shared__ double h[LSG_MAX_M], s[LSG_MAX_M];
+    __shared__ int bad;
+    if (ctrl_done(ctrl)) return;
+    const int nv = gram_values(kind, m);
+    const int np = nv - m;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    {
+        // One warp per Gram value, lanes striding over the block partials.
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int v = warp; v < nv; v += nw) {
+            double t = 0.0;
+            for (int k = lane; k < nparts; k += 32) t += partials[(long long)k * nv + v];
+            t = warp_sum(t);
+            if (lane == 0) {
+                vals[v] = t;
+                if (!isfinite(t)) bad = 1;
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        // Assemble G (row-major) and h.
+        if (kind == GRAM_SYM) {
+            for (int k = threadIdx.x; k < np; k += 32) {
+                int j = 0;
+                while ((j + 1) * (j + 2) / 2 <= k) j++;
+                const int a = k - j * (j + 1) / 2;
+                G[a * m + j] = vals[k];
+                G[j * m + a] = vals[k];
+            }
+        } else {
+            for (int k = threadIdx.x; k < np; k += 32) G[k] = vals[k];  // (a, j) = DX_a . DF_j
+        }
+        for (int j = threadIdx.x; j < m; j += 32) h[j] = vals[np + j] * hscale;
+        __syncwarp();
+        int st = 0;
+        if (!bad) st = warp_pinv(G, V, h, s, m);
+        __syncwarp();
+        if (threadIdx.x < m) ctrl->s[threadIdx.x] = bad ? 0.0 : s[threadIdx.x];
+        if (threadIdx.x == 0) {
+            if (bad) { ctrl->status = LSG_NAN_DETECTED; ctrl->done = 1; }
+            else if (st) ctrl->status = st;  // reported, the solve continues
+        }
+    }
+}
+
+__global__ void finalize_cg_kernel(const double *partials, int nparts, DevCtrl *ctrl, int mode,
+                                   double cf, int precond, int iter, int max_iter) {
+    __shared__ double red[32];
+    if (ctrl_done(ctrl)) return;
+    const double sum = block_sum_partials(partials, nparts, 1, 0, red);
+    if (threadIdx.x != 0) return;
+    if (mode == 0) {  // alpha = delta / (d . q)
+        ctrl->dq = sum;
+        ctrl->alpha = ctrl->delta / sum;
+        if (!isfinite(ctrl->alpha)) { ctrl->status = LSG_NAN_DETECTED; ctrl->done = 1; ctrl->iters = iter; }
+        return;
+    }
+    // mode 1: after the residual update of iteration `iter` (1-based count);
+    // mode 2: initial residual (iter = 0).
+    const double delta_new = precond ? cf * sum : sum;
+    const double relres = sqrt(sum);
+    const double delta_old = ctrl->delta;
+    ctrl->delta = delta_new;
+    ctrl->relres = relres;
+    ctrl->beta = mode == 2 ? 0.0 : delta_new / delta_old;
+    if (!isfinite(relres)) {
+        ctrl->status = LSG_NAN_DETECTED;
+        ctrl->done = 1;
+        ctrl->iters = iter;
+    } else if (!(relres > ctrl->tol_abs) || iter >= max_iter) {
+        ctrl->done = 1;
+        ctrl->iters = iter;
+    }
+}
+
+__global__ void pinv_kernel(const double *A, const double *b, double *x, int m, int *status) {
+    __shared__ double G[LSG_MAX_M * LSG_MAX_M], V[LSG_MAX_M * LSG_MAX_M], h[LSG_MAX_M], s[LSG_MAX_M];
+    for (int i = threadIdx.x; i < m * m; i += 32) G[i] = A[i];
+    for (int i = threadIdx.x; i < m; i += 32) h[i] = b[i];
+    __syncwarp();
+    const int st = warp_pinv(G, V, h, s, m);
+    __syncwarp();
+    if (threadIdx.x < m) x[threadIdx.x] = s[threadIdx.x];
+    if (threadIdx.x == 0 && status) *status = st;
+}
+
+// ---------------------------------------------------------------- launchers
+
+cudaError_t finalize_norm(const double *partials, int nparts, DevCtrl *ctrl, int mode, double tol,
+                          int iter, cudaStream_t s) {
+    finalize_norm_kernel<<<1, kFinThreads, 0, s>>>(partials, nparts, ctrl, mode, tol, iter);
+    return cudaGetLastError();
+}
+
+cudaError_t finalize_gram_solve(const double *partials, int nparts, int kind, int m, double hscale,
+                                DevCtrl *ctrl, cudaStream_t s) {
+    finalize_gram_solve_kernel<<<1, kFinThreads, 0, s>>>(partials, nparts, kind, m, hscale, ctrl);
+    return cudaGetLastError();
+}
+
+cudaError_t finalize_cg(const double *partials, int nparts, DevCtrl *ctrl, int mode, double cf,
+                        int precond, int iter, int max_iter, cudaStream_t s) {
+    finalize_cg_kernel<<<1, kFinThreads, 0, s>>>(partials, nparts, ctrl, mode, cf, precond, iter, max_iter);
+    return cudaGetLastError();
+}
+
+cudaError_t pinv_solve_dev(const double *A, const double *b, double *x, int m, int *status,
+                           cudaStream_t s) {
+    pinv_kernel<<<1, 32, 0, s>>>(A, b, x, m, status);
+    return cudaGetLastError();
+}
+
+}  // namespace lsg

@@ -1,0 +1,815 @@
+// lsg_solvers.cu — host side of liblsg: work-array cache, the solver loops
+// and the native C ABI declared in include/lsg.h.
+//
+// The loops restate the control flow of the reference solvers with device-
+// resident state:
+//   lsg_aar   MPI_REAL/AAR.c:37-177       lsg_pgr / lsg_pl2r  PGR.c:35-173, PL2R.c:35-172
+//   lsg_cg    MPI_REAL/CG.c:33-175        lsg_aar_mixed       FP64 refinement around FP32 AAR
+// Iteration numbering, history column selection ((iter-2)%m for AAR written
+// one launch early as (iter-1)%m; (iter-2+m)%m for PGR/PL2R), the residual
+// check only at extrapolation steps and the reported count follow the
+// reference.  Convergence is decided on the device (DevCtrl::done); the host
+// enqueues `check_every` extrapolation cycles ahead and reads the flag
+// through pinned memory, so the GPU never idles waiting for the host.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "lsg_internal.cuh"
+#include "lsg_host.h"
+
+namespace lsg {
+
+// ---------------------------------------------------------------- errors
+
+static thread_local int t_last_status = LSG_OK;
+static thread_local char t_last_error[512] = "";
+
+int set_error(int status, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_last_error, sizeof(t_last_error), fmt, ap);
+    va_end(ap);
+    t_last_status = status;
+    return status;
+}
+
+void set_last_status(int st) { t_last_status = st; if (st == LSG_OK) t_last_error[0] = 0; }
+int last_status() { return t_last_status; }
+const char *last_error() { return t_last_error; }
+
+#define LSG_CUDA(call)                                                                       \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return set_error(e_ == cudaErrorMemoryAllocation ? LSG_NO_MEMORY : LSG_CUDA_ERROR, \
+                             "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+// ---------------------------------------------------------------- device info
+
+static int sm_count() {
+    static std::mutex mu;
+    static std::map<int, int> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> g(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+    cache[dev] = sms;
+    return sms;
+}
+
+// ---------------------------------------------------------------- work arrays
+
+// One allocation per (device, element size, grid points, history depth):
+//   xalt, r0, r1                 three vectors (ping-pong partners)
+//   dx[m], df[m]                 the history, column j at offset j*n
+//   partials                     per-block FP64 sums
+//   ctrl                         DevCtrl
+// The mixed solver adds r32 / e32 (float) on an FP64 key.
+struct Workspace {
+    std::mutex mu;
+    int device = 0;
+    size_t es = 0;
+    long long n = 0;
+    int m = 0;
+    char *base = nullptr;
+    void *xalt = nullptr, *r0 = nullptr, *r1 = nullptr, *dx = nullptr, *df = nullptr;
+    float *r32 = nullptr, *e32 = nullptr;
+    double *partials = nullptr;
+    long long partials_cap = 0;
+    DevCtrl *ctrl = nullptr;
+    DevCtrl *hctrl = nullptr;  // pinned, two slots
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    ~Workspace() {
+        if (base) cudaFree(base);
+        if (hctrl) cudaFreeHost(hctrl);
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
+static std::mutex g_ws_mu;
+static std::map<std::tuple<int, size_t, long long, int, int>, std::unique_ptr<Workspace>> g_ws;
+
+static size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
+
+long long partials_needed(long long n, int m, int sms) {
+    long long cap = 0;
+    // stencil launches (worst case over both tile shapes and lz >= 1 planes)
+    const long long bx = (long long)sms * 8;
+    cap = std::max(cap, bx);
+    // grid-stride reductions use <= 4*sms blocks; Gram writes (m*m+m) values per block
+    cap = std::max(cap, (long long)4 * sms * (m * m + m));
+    (void)n;
+    return cap;
+}
+
+// Fetches (creating on first use) the work arrays; returned locked.
+static int get_workspace(size_t es, long long n, int m, bool mixed, const Geom &g,
+                         Workspace **out, std::unique_lock<std::mutex> *lock) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int sms = sm_count();
+    Workspace *ws;
+    {
+        std::lock_guard<std::mutex> gl(g_ws_mu);
+        auto key = std::make_tuple(dev, es, n, m, mixed ? 1 : 0);
+        auto &slot = g_ws[key];
+        if (!slot) slot.reset(new Workspace());
+        ws = slot.get();
+    }
+    *lock = std::unique_lock<std::mutex>(ws->mu);
+    if (ws->base) { *out = ws; return LSG_OK; }
+    // Partials: stencil grids for this geometry plus the reduction grids.
+    long long cap = partials_needed(n, m, sms);
+    cap = std::max(cap, stencil_blocks<double>(g, choose_lz<double>(g, sms)));
+    cap = std::max(cap, stencil_blocks<float>(g, choose_lz<float>(g, sms)));
+    const size_t vec = align_up((size_t)n * es);
+    size_t bytes = 0;
+    const size_t o_xalt = bytes; bytes += vec;
+    const size_t o_r0 = bytes; bytes += vec;
+    const size_t o_r1 = bytes; bytes += vec;
+    const size_t o_dx = bytes; bytes += align_up((size_t)n * es * (size_t)m);
+    const size_t o_df = bytes; bytes += align_up((size_t)n * es * (size_t)m);
+    size_t o_r32 = 0, o_e32 = 0;
+    if (mixed) {
+        o_r32 = bytes; bytes += align_up((size_t)n * 4);
+        o_e32 = bytes; bytes += align_up((size_t)n * 4);
+    }
+    const size_t o_part = bytes; bytes += align_up((size_t)cap * 8);
+    const size_t o_ctrl = bytes; bytes += align_up(sizeof(DevCtrl));
+    char *base = nullptr;
+    cudaError_t e = cudaMalloc(&base, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(LSG_NO_MEMORY, "cudaMalloc of %zu bytes for work arrays failed: %s", bytes,
+                         cudaGetErrorString(e));
+    }
+    DevCtrl *h = nullptr;
+    e = cudaMallocHost(&h, 2 * sizeof(DevCtrl));
+    if (e != cudaSuccess) {
+        cudaFree(base);
+        return set_error(LSG_NO_MEMORY, "cudaMallocHost failed: %s", cudaGetErrorString(e));
+    }
+    ws->device = dev;
+    ws->es = es;
+    ws->n = n;
+    ws->m = m;
+    ws->base = base;
+    ws->xalt = base + o_xalt;
+    ws->r0 = base + o_r0;
+    ws->r1 = base + o_r1;
+    ws->dx = base + o_dx;
+    ws->df = base + o_df;
+    if (mixed) {
+        ws->r32 = (float *)(base + o_r32);
+        ws->e32 = (float *)(base + o_e32);
+    }
+    ws->partials = (double *)(base + o_part);
+    ws->partials_cap = cap;
+    ws->ctrl = (DevCtrl *)(base + o_ctrl);
+    ws->hctrl = h;
+    cudaEventCreateWithFlags(&ws->ev[0], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ws->ev[1], cudaEventDisableTiming);
+    *out = ws;
+    return LSG_OK;
+}
+
+int release_workspaces() {
+    cudaDeviceSynchronize();
+    std::lock_guard<std::mutex> gl(g_ws_mu);
+    g_ws.clear();
+    return LSG_OK;
+}
+
+// ---------------------------------------------------------------- operator
+
+// system.c:480-498: c_0 = -sum_p 2/p^2; c_p = 2 (-1)^(p+1) (R!/(R-p)!) / ((R+p)!/R!) / p^2,
+// with the same product order so the values match the reference bit for bit.
+int lap_coefficient(int radius, double *c) {
+    c[0] = 0.0;
+    for (int p = 1; p <= radius; p++) c[0] += -(2.0 / (p * p));
+    for (int p = 1; p <= radius; p++) {
+        double nr = 1, dr = 1;
+        for (int i = radius - p + 1; i <= radius; i++) nr *= i;
+        for (int i = radius + 1; i <= radius + p; i++) dr *= i;
+        c[p] = 2 * std::pow(-1.0, p + 1) * (nr / dr) / (p * p);
+    }
+    for (int p = radius + 1; p <= LSG_MAX_RADIUS; p++) c[p] = 0.0;
+    return LSG_OK;
+}
+
+int check_operator(const lsg_operator *op) {
+    if (!op) return set_error(LSG_BAD_ARG, "operator is NULL");
+    for (int d = 0; d < 3; d++)
+        if (op->n[d] < 1) return set_error(LSG_BAD_ARG, "grid size n[%d] = %d < 1", d, op->n[d]);
+    if ((long long)op->n[0] * op->n[1] > (1LL << 31) - 1)
+        return set_error(LSG_BAD_ARG, "nx*ny exceeds 2^31-1");
+    if (op->radius < 1 || op->radius > LSG_MAX_RADIUS)
+        return set_error(LSG_BAD_ARG, "radius %d outside 1..%d", op->radius, LSG_MAX_RADIUS);
+    return LSG_OK;
+}
+
+double jacobi_diag(const lsg_operator *op) { return op->a * (3 * op->coeff[0]) + op->sigma; }
+
+template <typename T>
+static Weights<T> make_weights(const lsg_operator *op) {
+    Weights<T> w;
+    memset(&w, 0, sizeof(w));
+    w.radius = op->radius;
+    w.w[0] = (T)(op->a * 3.0 * op->coeff[0] + op->sigma);
+    for (int p = 1; p <= op->radius; p++) w.w[p] = (T)(op->a * op->coeff[p]);
+    return w;
+}
+
+static int check_params(const lsg_params *prm, bool history) {
+    if (!prm) return set_error(LSG_BAD_ARG, "params is NULL");
+    if (prm->max_iter < 0) return set_error(LSG_BAD_ARG, "max_iter %d < 0", prm->max_iter);
+    if (!(prm->tol >= 0)) return set_error(LSG_BAD_ARG, "tol must be >= 0");
+    if (history) {
+        if (prm->m < 1 || prm->m > LSG_MAX_M)
+            return set_error(LSG_BAD_ARG, "history depth m = %d outside 1..%d", prm->m, LSG_MAX_M);
+        if (prm->p < 1) return set_error(LSG_BAD_ARG, "period p = %d < 1", prm->p);
+    }
+    return LSG_OK;
+}
+
+// ---------------------------------------------------------------- solve driver helpers
+
+// ---------------------------------------------------------------- profiling
+
+// Per-class device time from CUDA events recorded on the solve's stream
+// around each launch (lsg_profile).  Events come from a pool reused across
+// solves; totals are folded in after the solve's final stream synchronize.
+static std::mutex g_prof_mu;
+static bool g_prof_on = false;
+static lsg_kernel_stats g_prof;
+static std::vector<cudaEvent_t> g_ev_pool;
+
+struct ProfRec {
+    int cls;
+    cudaEvent_t a, b;
+};
+
+struct Run {
+    cudaStream_t s;
+    int sms;
+    long long launches = 0;
+    bool prof = false;
+    size_t ev_used = 0;
+    std::vector<ProfRec> recs;
+    Run(cudaStream_t s_, int sms_) : s(s_), sms(sms_) {
+        std::lock_guard<std::mutex> g(g_prof_mu);
+        prof = g_prof_on;
+    }
+    cudaEvent_t event() {
+        // only the thread holding the profile flag draws events; the pool is
+        // guarded by g_prof_mu
+        std::lock_guard<std::mutex> g(g_prof_mu);
+        if (ev_used == g_ev_pool.size()) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+            g_ev_pool.push_back(e);
+        }
+        return g_ev_pool[ev_used++];
+    }
+    // Accumulates recorded launch times; call after the stream is idle.
+    void flush() {
+        if (!prof) return;
+        std::lock_guard<std::mutex> g(g_prof_mu);
+        for (const ProfRec &r : recs) {
+            float ms = 0.f;
+            if (r.a && r.b && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+                g_prof.launches[r.cls]++;
+                g_prof.ms[r.cls] += ms;
+            }
+        }
+        recs.clear();
+        ev_used = 0;
+    }
+};
+
+#define LSG_KC(cls, call)                                                                    \
+    do {                                                                                     \
+        cudaEvent_t ea_ = nullptr;                                                           \
+        if (R.prof && (ea_ = R.event()) != nullptr) cudaEventRecord(ea_, R.s);               \
+        cudaError_t e_ = (call);                                                             \
+        R.launches++;                                                                        \
+        if (e_ != cudaSuccess)                                                               \
+            return set_error(LSG_CUDA_ERROR, "launch %s: %s", #call, cudaGetErrorString(e_)); \
+        if (ea_) {                                                                           \
+            cudaEvent_t eb_ = R.event();                                                     \
+            if (eb_) { cudaEventRecord(eb_, R.s); R.recs.push_back({cls, ea_, eb_}); }       \
+        }                                                                                    \
+    } while (0)
+
+static int reduce_blocks(long long n, int sms) {
+    long long b = (n + 255) / 256;
+    return (int)std::max<long long>(1, std::min<long long>(b, 4LL * sms));
+}
+
+// Initial DevCtrl contents.  relres starts at tol + 1 as in AAR.c:76, so a
+// solve stopped before its first check reports the reference's value.
+static DevCtrl ctrl_init(double tol, int stall_limit) {
+    DevCtrl c;
+    memset(&c, 0, sizeof(c));
+    c.relres = tol + 1.0;
+    c.best = INFINITY;
+    c.stall_limit = stall_limit;
+    return c;
+}
+
+// Enqueues cycles through `enqueue_iter(it)` with a pipelined convergence read
+// every `per_check` checkpoints; `is_check(it)` marks iterations that end with
+// a device-side convergence test.  Returns after the solve stopped.
+template <class Enq, class IsCheck>
+static int pipelined_loop(Run &R, Workspace *ws, int first_iter, int max_iter, int per_check,
+                          Enq &&enqueue_iter, IsCheck &&is_check) {
+    int it = first_iter;
+    int batch = 0;
+    bool stop = false;
+    while (!stop) {
+        int checks = 0;
+        while (it <= max_iter && checks < per_check) {
+            int rc = enqueue_iter(it);
+            if (rc != LSG_OK) return rc;
+            if (is_check(it)) checks++;
+            it++;
+        }
+        const int slot = batch & 1;
+        LSG_CUDA(cudaMemcpyAsync(ws->hctrl + slot, ws->ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost, R.s));
+        LSG_CUDA(cudaEventRecord(ws->ev[slot], R.s));
+        if (batch > 0) {
+            const int prev = slot ^ 1;
+            LSG_CUDA(cudaEventSynchronize(ws->ev[prev]));
+            if (ws->hctrl[prev].done) stop = true;
+        }
+        if (it > max_iter) stop = true;
+        batch++;
+    }
+    LSG_CUDA(cudaStreamSynchronize(R.s));
+    return LSG_OK;
+}
+
+static int default_per_check(const lsg_params *prm, long long n) {
+    if (prm->check_every > 0) return prm->check_every;
+    return n >= (1LL << 21) ? 2 : 8;
+}
+
+static void fill_result(lsg_result *res, const DevCtrl &c, int max_iter, double seconds,
+                        long long launches) {
+    if (!res) return;
+    res->iters = c.done ? c.iters : max_iter;
+    res->rhs_norm = c.rhs_norm;
+    res->relres = c.rhs_norm > 0 ? c.relres / c.rhs_norm : c.relres;
+    if (c.status == LSG_NAN_DETECTED) res->status = LSG_NAN_DETECTED;
+    else if (c.done && !c.stalled && !(c.relres > c.tol_abs)) res->status = LSG_OK;
+    else res->status = (c.status == LSG_SVD_NO_CONVERGENCE) ? LSG_SVD_NO_CONVERGENCE : LSG_NOT_CONVERGED;
+    res->seconds = seconds;
+    res->launches = launches;
+}
+
+static double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// ---------------------------------------------------------------- AAR
+
+// AAR.c:37-177.  x (in/out) and b are device arrays of n values of T.
+template <typename T>
+int aar_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const T *b,
+             Workspace *ws, int stall_limit, DevCtrl *out) {
+    const Geom g = make_geom(op->n);
+    const long long n = g.n;
+    const int m = prm->m, p = prm->p, max_iter = prm->max_iter;
+    const Weights<T> w = make_weights<T>(op);
+    const double cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
+    const int lz = choose_lz<T>(g, R.sms);
+    const StencilLaunch L{g, lz, R.s};
+    const int sb = (int)stencil_blocks<T>(g, lz);
+    const int rb = reduce_blocks(n, R.sms);
+    T *X[2] = {x, (T *)ws->xalt};
+    T *Rv[2] = {(T *)ws->r0, (T *)ws->r1};
+    T *DX = (T *)ws->dx, *DF = (T *)ws->df;
+    DevCtrl *ctrl = ws->ctrl;
+    double *part = ws->partials;
+
+    DevCtrl c0 = ctrl_init(prm->tol, stall_limit);
+    ws->hctrl[0] = c0;
+    LSG_CUDA(cudaMemcpyAsync(ctrl, ws->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, R.s));
+    LSG_CUDA(cudaMemsetAsync(DX, 0, sizeof(T) * (size_t)n * m, R.s));
+    LSG_CUDA(cudaMemsetAsync(DF, 0, sizeof(T) * (size_t)n * m, R.s));
+    // ||b|| and tol *= ||b|| (AAR.c:78-79); f = b - A x (AAR.c:80-82).
+    LSG_KC(LSG_K_UPDATE, Kernels<T>::norm2(b, n, part, rb, ctrl, R.s));
+    LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, R.s));
+    LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, X[0], b, Rv[0], nullptr, cf, part, ctrl));
+
+    int cur = 0;
+    auto is_anderson = [p](int it) { return it % p == 0 && it > 1; };
+    auto enqueue = [&](int it) -> int {
+        const int col = (it - 1) % m;  // the reference writes this column at iteration it+1
+        if (is_anderson(it)) {
+            LSG_KC(LSG_K_GRAM, Kernels<T>::gram(GRAM_SYM, m, DX, DF, Rv[cur], n, part, rb, ctrl, R.s));
+            LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, rb, GRAM_SYM, m, cf, ctrl, R.s));
+            LSG_KC(LSG_K_UPDATE, Kernels<T>::aar_update(m, col, X[cur], Rv[cur], DX, DF, prm->beta, cf, n, ctrl, R.s));
+            LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_ANDERSON, X[cur], b, Rv[cur], DF + (size_t)col * n, cf, part, ctrl));
+            LSG_KC(LSG_K_SMALL, finalize_norm(part, sb, ctrl, NF_CHECK, prm->tol, it, R.s));
+        } else {
+            LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson(L, w, RICH_AAR, X[cur], Rv[cur], b, X[cur ^ 1], Rv[cur ^ 1],
+                                          DX + (size_t)col * n, DF + (size_t)col * n,
+                                          prm->omega * cf, cf, ctrl));
+            cur ^= 1;
+        }
+        return LSG_OK;
+    };
+    int rc = pipelined_loop(R, ws, 1, max_iter, default_per_check(prm, n), enqueue, is_anderson);
+    if (rc != LSG_OK) return rc;
+    DevCtrl c;
+    LSG_CUDA(cudaMemcpy(&c, ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost));
+    // Where the last iterate lives: x moved to the other buffer at every
+    // Richardson iteration up to the final one.
+    const int last = c.done ? c.iters : max_iter;
+    long long rich = last - last / p + (p == 1 && last >= 1 ? 1 : 0);
+    if (last < 1) rich = 0;
+    if (rich & 1) LSG_CUDA(cudaMemcpyAsync(x, X[1], sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, R.s));
+    LSG_CUDA(cudaStreamSynchronize(R.s));
+    *out = c;
+    return LSG_OK;
+}
+
+// PGR.c:35-173 (galerkin) and PL2R.c:35-172.
+template <typename T>
+int prich_core(Run &R, bool galerkin, const lsg_operator *op, const lsg_params *prm, T *x,
+               const T *b, Workspace *ws, DevCtrl *out) {
+    const Geom g = make_geom(op->n);
+    const long long n = g.n;
+    const int m = prm->m, p = prm->p, max_iter = prm->max_iter;
+    const Weights<T> w = make_weights<T>(op);
+    const double cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
+    const int lz = choose_lz<T>(g, R.sms);
+    const StencilLaunch L{g, lz, R.s};
+    const int rb = reduce_blocks(n, R.sms);
+    T *X[2] = {x, (T *)ws->xalt};
+    T *Rv[2] = {(T *)ws->r0, (T *)ws->r1};
+    T *DX = (T *)ws->dx, *DF = (T *)ws->df;
+    DevCtrl *ctrl = ws->ctrl;
+    double *part = ws->partials;
+    const int kind = galerkin ? GRAM_GALERKIN : GRAM_SYM;
+
+    ws->hctrl[0] = ctrl_init(prm->tol, 0);
+    LSG_CUDA(cudaMemcpyAsync(ctrl, ws->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, R.s));
+    LSG_CUDA(cudaMemsetAsync(DX, 0, sizeof(T) * (size_t)n * m, R.s));
+    LSG_CUDA(cudaMemsetAsync(DF, 0, sizeof(T) * (size_t)n * m, R.s));
+    LSG_KC(LSG_K_UPDATE, Kernels<T>::norm2(b, n, part, rb, ctrl, R.s));
+    LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, R.s));
+    LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, X[0], b, Rv[0], nullptr, cf, part, ctrl));
+
+    int cur = 0;
+    auto is_proj = [p](int it) { return it % p == 0; };
+    auto enqueue = [&](int it) -> int {
+        const int col = (it - 2 + m) % m;
+        LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson(L, w, RICH_PGR, X[cur], Rv[cur], b, X[cur ^ 1], Rv[cur ^ 1],
+                                      DX + (size_t)col * n, DF + (size_t)col * n, prm->omega * cf,
+                                      cf, ctrl));
+        cur ^= 1;
+        if (is_proj(it)) {
+            LSG_KC(LSG_K_GRAM, Kernels<T>::gram(kind, m, DX, DF, Rv[cur], n, part, rb, ctrl, R.s));
+            LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, rb, kind, m, 1.0, ctrl, R.s));
+            LSG_KC(LSG_K_UPDATE, Kernels<T>::proj_update(m, col, X[cur], Rv[cur], DX, DF, n, part, rb, ctrl, R.s));
+            LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_CHECK, prm->tol, it, R.s));
+        }
+        return LSG_OK;
+    };
+    int rc = pipelined_loop(R, ws, 1, max_iter, default_per_check(prm, n), enqueue, is_proj);
+    if (rc != LSG_OK) return rc;
+    DevCtrl c;
+    LSG_CUDA(cudaMemcpy(&c, ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost));
+    const int last = c.done ? c.iters : max_iter;
+    if (last & 1) LSG_CUDA(cudaMemcpyAsync(x, X[1], sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, R.s));
+    LSG_CUDA(cudaStreamSynchronize(R.s));
+    *out = c;
+    return LSG_OK;
+}
+
+// CG.c:33-175.  Work vectors: r = r0, d ping-pong = (r1, xalt), q = dx[0].
+template <typename T>
+int cg_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const T *b,
+            Workspace *ws, DevCtrl *out) {
+    const Geom g = make_geom(op->n);
+    const long long n = g.n;
+    const int max_iter = prm->max_iter;
+    const Weights<T> w = make_weights<T>(op);
+    const double cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
+    const int lz = choose_lz<T>(g, R.sms);
+    const StencilLaunch L{g, lz, R.s};
+    const int sb = (int)stencil_blocks<T>(g, lz);
+    const int rb = reduce_blocks(n, R.sms);
+    T *r = (T *)ws->r0;
+    T *D[2] = {(T *)ws->r1, (T *)ws->xalt};
+    T *q = (T *)ws->dx;
+    DevCtrl *ctrl = ws->ctrl;
+    double *part = ws->partials;
+
+    ws->hctrl[0] = ctrl_init(prm->tol, 0);
+    LSG_CUDA(cudaMemcpyAsync(ctrl, ws->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, R.s));
+    LSG_CUDA(cudaMemsetAsync(D[0], 0, sizeof(T) * (size_t)n, R.s));
+    LSG_KC(LSG_K_UPDATE, Kernels<T>::norm2(b, n, part, rb, ctrl, R.s));
+    LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, R.s));
+    // r = b - A x; d = M^-1 r; delta = r.d; relres = ||r|| (CG.c:65-89)
+    LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, x, b, r, nullptr, cf, part, ctrl));
+    LSG_KC(LSG_K_SMALL, finalize_cg(part, sb, ctrl, 2, cf, op->precond, 0, max_iter, R.s));
+
+    int cur = 0;
+    auto always = [](int) { return true; };
+    auto enqueue = [&](int it) -> int {  // it = iter_count + 1
+        const int ic = it - 1;           // iter_count at the top of the loop body
+        LSG_KC(LSG_K_CG, Kernels<T>::cg_direction(L, w, r, D[cur], D[cur ^ 1], q, cf, part, ctrl));
+        cur ^= 1;
+        LSG_KC(LSG_K_SMALL, finalize_cg(part, sb, ctrl, 0, cf, op->precond, it, max_iter, R.s));
+        if (ic % 50 == 0) {  // restart with the true residual (CG.c:109-120)
+            LSG_KC(LSG_K_UPDATE, Kernels<T>::cg_step(x, r, D[cur], q, n, 1, part, rb, ctrl, R.s));
+            LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, x, b, r, nullptr, cf, part, ctrl));
+            LSG_KC(LSG_K_SMALL, finalize_cg(part, sb, ctrl, 1, cf, op->precond, it, max_iter, R.s));
+        } else {
+            LSG_KC(LSG_K_UPDATE, Kernels<T>::cg_step(x, r, D[cur], q, n, 0, part, rb, ctrl, R.s));
+            LSG_KC(LSG_K_SMALL, finalize_cg(part, rb, ctrl, 1, cf, op->precond, it, max_iter, R.s));
+        }
+        return LSG_OK;
+    };
+    const int per = prm->check_every > 0 ? prm->check_every : (n >= (1LL << 21) ? 8 : 32);
+    int rc = pipelined_loop(R, ws, 1, max_iter, per, enqueue, always);
+    if (rc != LSG_OK) return rc;
+    DevCtrl c;
+    LSG_CUDA(cudaMemcpy(&c, ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost));
+    *out = c;
+    return LSG_OK;
+}
+
+// ---------------------------------------------------------------- dispatch
+
+template <typename T>
+static int solve_t(int solver, const lsg_operator *op, const lsg_params *prm, void *d_x,
+                   const void *d_b, lsg_result *res, cudaStream_t s) {
+    const double t0 = now_s();
+    const Geom g = make_geom(op->n);
+    Workspace *ws = nullptr;
+    std::unique_lock<std::mutex> lk;
+    const int mh = solver == 3 ? 1 : prm->m;
+    int rc = get_workspace(sizeof(T), g.n, mh, false, g, &ws, &lk);
+    if (rc != LSG_OK) return rc;
+    Run R(s, sm_count());
+    DevCtrl c;
+    switch (solver) {
+    case 0: rc = aar_core<T>(R, op, prm, (T *)d_x, (const T *)d_b, ws, 0, &c); break;
+    case 1: rc = prich_core<T>(R, true, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
+    case 2: rc = prich_core<T>(R, false, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
+    default: rc = cg_core<T>(R, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
+    }
+    if (rc != LSG_OK) return rc;
+    R.flush();
+    lsg_result tmp;
+    fill_result(&tmp, c, prm->max_iter, now_s() - t0, R.launches);
+    tmp.outer_iters = 0;
+    tmp.inner_iters = 0;
+    if (res) *res = tmp;
+    set_last_status(tmp.status);
+    return tmp.status;
+}
+
+int solve(int solver, const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
+          const void *d_b, lsg_result *res, cudaStream_t s) {
+    int rc = check_operator(op);
+    if (rc) return rc;
+    rc = check_params(prm, solver != 3);
+    if (rc) return rc;
+    if (!d_x || !d_b) return set_error(LSG_BAD_ARG, "NULL vector");
+    if (dtype == LSG_F64) return solve_t<double>(solver, op, prm, d_x, d_b, res, s);
+    if (dtype == LSG_F32) return solve_t<float>(solver, op, prm, d_x, d_b, res, s);
+    return set_error(LSG_BAD_ARG, "unknown dtype %d", dtype);
+}
+
+// ---------------------------------------------------------------- mixed precision
+
+int solve_mixed(const lsg_operator *op, const lsg_params *prm, double *x, const double *b,
+                lsg_result *res, cudaStream_t s) {
+    const double t0 = now_s();
+    int rc = check_operator(op);
+    if (rc) return rc;
+    rc = check_params(prm, true);
+    if (rc) return rc;
+    if (!x || !b) return set_error(LSG_BAD_ARG, "NULL vector");
+    const Geom g = make_geom(op->n);
+    const long long n = g.n;
+    Workspace *wo = nullptr, *wi = nullptr;
+    std::unique_lock<std::mutex> lo, li;
+    rc = get_workspace(sizeof(double), n, 1, true, g, &wo, &lo);  // outer: r32, e32, partials, ctrl
+    if (rc) return rc;
+    rc = get_workspace(sizeof(float), n, prm->m, false, g, &wi, &li);  // inner FP32 AAR
+    if (rc) return rc;
+    Run R(s, sm_count());
+    const Weights<double> w = make_weights<double>(op);
+    const int lz = choose_lz<double>(g, R.sms);
+    const StencilLaunch L{g, lz, s};
+    const int sb = (int)stencil_blocks<double>(g, lz);
+    const int rb = reduce_blocks(n, R.sms);
+    DevCtrl *ctrl = wo->ctrl;
+    double *part = wo->partials;
+    const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
+    lsg_params ip = *prm;
+    ip.tol = prm->inner_tol > 0 ? prm->inner_tol : 1e-3;
+
+    wo->hctrl[0] = ctrl_init(prm->tol, 0);
+    LSG_CUDA(cudaMemcpyAsync(ctrl, wo->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, s));
+    LSG_KC(LSG_K_UPDATE, Kernels<double>::norm2(b, n, part, rb, ctrl, s));
+    LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, s));
+    int outer = 0, inner_total = 0, status = LSG_NOT_CONVERGED;
+    double prev = INFINITY;
+    DevCtrl c;
+    for (;;) {
+        // r = b - A x in FP64, stored as the FP32 right-hand side of the inner solve.
+        LSG_KC(LSG_K_REFINE, ir_residual(L, w, x, b, wo->r32, part, ctrl));
+        LSG_KC(LSG_K_SMALL, finalize_norm(part, sb, ctrl, NF_CHECK, prm->tol, outer, s));
+        LSG_CUDA(cudaMemcpyAsync(&wo->hctrl[0], ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost, s));
+        LSG_CUDA(cudaStreamSynchronize(s));
+        c = wo->hctrl[0];
+        if (c.status == LSG_NAN_DETECTED) { status = LSG_NAN_DETECTED; break; }
+        if (c.done) { status = LSG_OK; break; }
+        if (outer >= max_outer || inner_total >= prm->max_iter) break;
+        if (!(c.relres < prev)) break;  // refinement no longer reduces the FP64 residual
+        prev = c.relres;
+        // Inner FP32 AAR on A e = r, e0 = 0, stopped at inner_tol or when it stalls.
+        LSG_CUDA(cudaMemsetAsync(wo->e32, 0, sizeof(float) * (size_t)n, s));
+        ip.max_iter = prm->max_iter - inner_total;
+        DevCtrl ci;
+        rc = aar_core<float>(R, op, &ip, wo->e32, wo->r32, wi, 12, &ci);
+        if (rc) return rc;
+        inner_total += ci.done ? ci.iters : ip.max_iter;
+        if (ci.status == LSG_NAN_DETECTED) { status = LSG_NAN_DETECTED; break; }
+        LSG_KC(LSG_K_REFINE, ir_correct(x, wo->e32, n, s));
+        outer++;
+    }
+    LSG_CUDA(cudaStreamSynchronize(s));
+    R.flush();
+    if (res) {
+        res->iters = inner_total;
+        res->inner_iters = inner_total;
+        res->outer_iters = outer;
+        res->rhs_norm = c.rhs_norm;
+        res->relres = c.rhs_norm > 0 ? c.relres / c.rhs_norm : c.relres;
+        res->status = status;
+        res->seconds = now_s() - t0;
+        res->launches = R.launches;
+    }
+    set_last_status(status);
+    return status;
+}
+
+int apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, cudaStream_t s) {
+    int rc = check_operator(op);
+    if (rc) return rc;
+    if (!d_x || !d_y) return set_error(LSG_BAD_ARG, "NULL vector");
+    const Geom g = make_geom(op->n);
+    const int sms = sm_count();
+    if (dtype == LSG_F64) {
+        const StencilLaunch L{g, choose_lz<double>(g, sms), s};
+        LSG_CUDA(Kernels<double>::residual(L, make_weights<double>(op), RES_APPLY, (const double *)d_x,
+                                           nullptr, (double *)d_y, nullptr, 1.0, nullptr, nullptr));
+    } else if (dtype == LSG_F32) {
+        const StencilLaunch L{g, choose_lz<float>(g, sms), s};
+        LSG_CUDA(Kernels<float>::residual(L, make_weights<float>(op), RES_APPLY, (const float *)d_x,
+                                          nullptr, (float *)d_y, nullptr, 1.0, nullptr, nullptr));
+    } else {
+        return set_error(LSG_BAD_ARG, "unknown dtype %d", dtype);
+    }
+    return LSG_OK;
+}
+
+int pinv(const double *A, const double *b, double *x, int m, cudaStream_t s) {
+    if (m < 1 || m > LSG_MAX_M) return set_error(LSG_BAD_ARG, "m = %d outside 1..%d", m, LSG_MAX_M);
+    if (!A || !b || !x) return set_error(LSG_BAD_ARG, "NULL pointer");
+    int *dst = nullptr;
+    LSG_CUDA(cudaMallocAsync((void **)&dst, sizeof(int), s));
+    LSG_CUDA(pinv_solve_dev(A, b, x, m, dst, s));
+    int st = 0;
+    LSG_CUDA(cudaMemcpyAsync(&st, dst, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LSG_CUDA(cudaFreeAsync(dst, s));
+    LSG_CUDA(cudaStreamSynchronize(s));
+    return st;
+}
+
+}  // namespace lsg
+
+// ---------------------------------------------------------------- C ABI
+
+extern "C" {
+
+int lsg_lap_coefficient(int radius, double *c) {
+    if (radius < 1 || radius > LSG_MAX_RADIUS || !c) return lsg::set_error(LSG_BAD_ARG, "bad radius");
+    return lsg::lap_coefficient(radius, c);
+}
+
+int lsg_operator_init(lsg_operator *op, int nx, int ny, int nz, int radius, double a, double sigma,
+                      int precond) {
+    if (!op) return lsg::set_error(LSG_BAD_ARG, "operator is NULL");
+    memset(op, 0, sizeof(*op));
+    op->n[0] = nx; op->n[1] = ny; op->n[2] = nz;
+    op->radius = radius;
+    op->a = a;
+    op->sigma = sigma;
+    op->precond = precond;
+    int rc = lsg_lap_coefficient(radius, op->coeff);
+    if (rc) return rc;
+    return lsg::check_operator(op);
+}
+
+void lsg_params_default(lsg_params *prm) {
+    if (!prm) return;
+    memset(prm, 0, sizeof(*prm));
+    prm->omega = 0.6;
+    prm->beta = 0.6;
+    prm->m = 7;
+    prm->p = 6;
+    prm->max_iter = 100000;
+    prm->tol = 1e-8;
+    prm->inner_tol = 1e-3;
+    prm->max_outer = 50;
+}
+
+int lsg_apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, void *stream) {
+    return lsg::apply(op, dtype, d_x, d_y, (cudaStream_t)stream);
+}
+
+int lsg_aar(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, const void *d_b,
+            lsg_result *res, void *stream) {
+    return lsg::solve(0, op, prm, dtype, d_x, d_b, res, (cudaStream_t)stream);
+}
+int lsg_pgr(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, const void *d_b,
+            lsg_result *res, void *stream) {
+    return lsg::solve(1, op, prm, dtype, d_x, d_b, res, (cudaStream_t)stream);
+}
+int lsg_pl2r(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, const void *d_b,
+             lsg_result *res, void *stream) {
+    return lsg::solve(2, op, prm, dtype, d_x, d_b, res, (cudaStream_t)stream);
+}
+int lsg_cg(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, const void *d_b,
+           lsg_result *res, void *stream) {
+    return lsg::solve(3, op, prm, dtype, d_x, d_b, res, (cudaStream_t)stream);
+}
+int lsg_aar_mixed(const lsg_operator *op, const lsg_params *prm, double *d_x, const double *d_b,
+                  lsg_result *res, void *stream) {
+    return lsg::solve_mixed(op, prm, d_x, d_b, res, (cudaStream_t)stream);
+}
+int lsg_pinv_solve(const double *d_A, const double *d_b, double *d_x, int m, void *stream) {
+    return lsg::pinv(d_A, d_b, d_x, m, (cudaStream_t)stream);
+}
+int lsg_release_workspaces(void) { return lsg::release_workspaces(); }
+
+int lsg_profile(int on) {
+    std::lock_guard<std::mutex> g(lsg::g_prof_mu);
+    if (on) memset(&lsg::g_prof, 0, sizeof(lsg::g_prof));
+    lsg::g_prof_on = on != 0;
+    return LSG_OK;
+}
+
+int lsg_profile_read(lsg_kernel_stats *stats) {
+    if (!stats) return lsg::set_error(LSG_BAD_ARG, "NULL stats");
+    std::lock_guard<std::mutex> g(lsg::g_prof_mu);
+    *stats = lsg::g_prof;
+    return LSG_OK;
+}
+int lsg_last_status(void) { return lsg::last_status(); }
+const char *lsg_last_error(void) { return lsg::last_error(); }
+
+const char *lsg_status_string(int st) {
+    switch (st) {
+    case LSG_OK: return "ok";
+    case LSG_NOT_CONVERGED: return "not converged";
+    case LSG_NAN_DETECTED: return "NaN or Inf detected";
+    case LSG_BAD_ARG: return "bad argument";
+    case LSG_CUDA_ERROR: return "CUDA error";
+    case LSG_TIMEOUT: return "device wait timed out";
+    case LSG_UNSUPPORTED: return "unsupported";
+    case LSG_NO_MEMORY: return "out of device memory";
+    case LSG_SVD_NO_CONVERGENCE: return "SVD sweep limit reached";
+    default: return "unknown status";
+    }
+}
+
+const char *lsg_version(void) { return "lsg 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,170 @@
+// lsg_stencil.cuh — z-marching periodic star-stencil driver.
+//
+// Replaces the sequential operator of MPI_REAL/system.c:189-204 (and the MPI
+// halo exchange of :106-188, which one GPU does not need): each thread block
+// owns a TX x TY column tile of the xy plane and a range of lz planes along z.
+// For every plane it
+//   * keeps, per owned column, the 2R+1 values u(z-R .. z+R) in a register
+//     queue (one new plane value loaded per step: the z neighbours),
+//   * stages plane z with an R-wide xy halo in shared memory (the interior
+//     from the queue centre, the halo from global memory with the periodic
+//     wrap applied to the xy coordinates once, before the march), and
+//   * evaluates  Au = w0 u_c + sum_p w_p ((u_x-p + u_x+p) + (u_y-p + u_y+p) + (u_z-p + u_z+p)).
+// The "value" u at a grid point and what happens to Au at the centre are
+// supplied by a functor, so one driver serves the residual, the fused
+// Richardson step, the CG direction update and the FP64 refinement residual.
+//
+// Functor interface (all __device__):
+//   void init()                               read device scalars (once per thread)
+//   T    load(long long idx) const            u at flat index idx
+//   void store(long long idx, T u, T Au, Acc<T> *acc) const   epilogue at a valid centre
+//   static constexpr int NACC                 per-thread accumulators (FP64-class) reduced per block
+//   double *partials                          where the block writes NACC sums (if NACC > 0)
+#pragma once
+
+#include "lsg_internal.cuh"
+#include "lsg_accum.cuh"
+
+namespace lsg {
+
+template <typename T>
+__device__ __forceinline__ T ldg(const T *p) { return __ldg(p); }
+
+// RQ: radius the storage is sized for; the arithmetic uses `radius` (== RQ on
+// the specialised path, <= RQ on the generic path).
+template <typename T, int RQ, int BY, int NY, bool GENERIC, class Op>
+__device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w, int lz, Op &op,
+                                              T *smem) {
+    constexpr int TX = 32;
+    constexpr int TY = BY * NY;
+    constexpr int FX = TX + 2 * RQ;
+    constexpr int FY = TY + 2 * RQ;
+    constexpr int NT = 32 * BY;
+    constexpr int H = 2 * RQ * FX + TY * 2 * RQ;  // halo cells of one plane
+    constexpr int NH = (H + NT - 1) / NT;
+    constexpr int Q = 2 * RQ + 1;
+
+    const int radius = GENERIC ? w.radius : RQ;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * 32 + tx;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int z0 = blockIdx.z * lz;
+    const int z1 = min(z0 + lz, g.nz);
+
+    // Owned columns (periodically wrapped, so partial tiles still hold valid data).
+    const int gx = wrap_index(x0 + tx, g.nx);
+    int col[NY];
+    bool valid[NY];
+#pragma unroll
+    for (int k = 0; k < NY; k++) {
+        const int yy = y0 + ty + BY * k;
+        col[k] = gx + wrap_index(yy, g.ny) * g.nx;
+        valid[k] = (x0 + tx < g.nx) && (yy < g.ny);
+    }
+    // Halo cells this thread fills, as (shared offset, wrapped xy offset).
+    int hs[NH], ho[NH];
+#pragma unroll
+    for (int s = 0; s < NH; s++) {
+        const int h = tid + s * NT;
+        hs[s] = -1;
+        ho[s] = 0;
+        if (h < H) {
+            int fy, fx;
+            if (h < RQ * FX) {                       // top strip
+                fy = h / FX; fx = h % FX;
+            } else if (h < 2 * RQ * FX) {            // bottom strip
+                const int hh = h - RQ * FX;
+                fy = RQ + TY + hh / FX; fx = hh % FX;
+            } else {                                 // left / right strips
+                const int hh = h - 2 * RQ * FX;
+                const int row = hh / (2 * RQ), c = hh % (2 * RQ);
+                fy = RQ + row;
+                fx = c < RQ ? c : TX + c;
+            }
+            hs[s] = fy * FX + fx;
+            ho[s] = wrap_index(x0 - RQ + fx, g.nx) + wrap_index(y0 - RQ + fy, g.ny) * g.nx;
+        }
+    }
+
+    Acc<T> acc[Op::NACC > 0 ? Op::NACC : 1];
+#pragma unroll
+    for (int a = 0; a < (Op::NACC > 0 ? Op::NACC : 1); a++) acc[a].zero();
+
+    T q[NY][Q];
+    // Prologue: planes z0-RQ .. z0+RQ-1 into q[.][1..2RQ].
+    int zl = wrap_index(z0 - RQ, g.nz);
+#pragma unroll
+    for (int s = 0; s < 2 * RQ; s++) {
+        const long long base = (long long)zl * g.nxy;
+#pragma unroll
+        for (int k = 0; k < NY; k++) q[k][s + 1] = op.load(base + col[k]);
+        zl = (zl + 1 == g.nz) ? 0 : zl + 1;
+    }
+
+    for (int z = z0; z < z1; z++) {
+        const long long zbase = (long long)z * g.nxy;
+        const long long lbase = (long long)zl * g.nxy;
+#pragma unroll
+        for (int k = 0; k < NY; k++) {
+#pragma unroll
+            for (int s = 0; s < Q - 1; s++) q[k][s] = q[k][s + 1];
+            q[k][Q - 1] = op.load(lbase + col[k]);
+        }
+        zl = (zl + 1 == g.nz) ? 0 : zl + 1;
+
+        T hv[NH];
+#pragma unroll
+        for (int s = 0; s < NH; s++) hv[s] = hs[s] >= 0 ? op.load(zbase + ho[s]) : T(0);
+
+        __syncthreads();  // previous plane fully consumed
+#pragma unroll
+        for (int k = 0; k < NY; k++) smem[(RQ + ty + BY * k) * FX + RQ + tx] = q[k][RQ];
+#pragma unroll
+        for (int s = 0; s < NH; s++)
+            if (hs[s] >= 0) smem[hs[s]] = hv[s];
+        __syncthreads();
+
+#pragma unroll
+        for (int k = 0; k < NY; k++) {
+            const T *row = smem + (RQ + ty + BY * k) * FX + RQ + tx;
+            T au = w.w[0] * q[k][RQ];
+#pragma unroll
+            for (int p = 1; p <= RQ; p++) {
+                if (GENERIC && p > radius) break;
+                const T sxy = (row[-p] + row[p]) + (row[-p * FX] + row[p * FX]);
+                const T sz = q[k][RQ - p] + q[k][RQ + p];
+                au = fma(w.w[p], sxy + sz, au);
+            }
+            if (valid[k]) op.store(zbase + col[k], q[k][RQ], au, acc);
+        }
+    }
+
+    if (Op::NACC > 0) {
+        constexpr int NA = Op::NACC > 0 ? Op::NACC : 1;
+        __shared__ double red[NA * 32];
+        double v[NA];
+#pragma unroll
+        for (int a = 0; a < NA; a++) v[a] = acc[a].get();
+        const long long blk = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+        block_sum_store<NA>(v, red, op.partials + blk * Op::NACC);
+    }
+}
+
+template <typename T, int RQ, int BY, int NY, bool GENERIC, class Op>
+__global__ void __launch_bounds__(32 * BY) stencil_kernel(Geom g, Weights<T> w, int lz, Op op) {
+    constexpr int FX = 32 + 2 * RQ;
+    constexpr int FY = BY * NY + 2 * RQ;
+    __shared__ T smem[FX * FY];
+    if (op.skip()) {
+        // Solve already finished: keep the block's partials well defined.
+        if (Op::NACC > 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+            const long long blk = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+            for (int a = 0; a < Op::NACC; a++) op.partials[blk * Op::NACC + a] = 0.0;
+        }
+        return;
+    }
+    op.init();
+    stencil_march<T, RQ, BY, NY, GENERIC>(g, w, lz, op, smem);
+}
+
+}  // namespace lsg

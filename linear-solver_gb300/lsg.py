@@ -1,0 +1,410 @@
+"""Python binding of liblsg (ctypes over the C ABI in include/lsg.h).
+
+Device vectors are torch CUDA tensors shaped ``(nz, ny, nx)`` (x fastest, the
+reference layout of MPI_REAL/system.c:82) or flat; PyTorch supplies memory and
+streams only — every operation runs in liblsg's own sm_103a kernels.  If the
+library cannot be loaded the calls raise; there is no fallback path.
+
+    import lsg
+    op = lsg.Operator((256, 256, 256))            # a = -1/(4 pi), FDn = 6, Jacobi
+    x, info = lsg.aar(op, b)                       # b: torch.float64 CUDA tensor
+    x, info = lsg.aar_mixed(op, b, tol=1e-8)       # FP32 inner / FP64 refinement
+
+The reference's own entry points on host arrays (``AAR(POISSON*, ...)``) are
+reachable through ``compat_solve``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblsg.so")
+MAX_RADIUS = 8
+MAX_M = 32
+A_REF = -1.0 / (4.0 * math.pi)  # operator scale of MPI_REAL/main.c:68
+
+F64, F32 = 0, 1
+STATUS = {0: "ok", 1: "not converged", 2: "NaN/Inf detected", 3: "bad argument", 4: "CUDA error",
+          5: "timeout", 6: "unsupported", 7: "out of memory", 8: "SVD sweep limit"}
+
+
+class CudaLibraryError(RuntimeError):
+    pass
+
+
+class _Operator(C.Structure):
+    _fields_ = [("n", C.c_int * 3), ("radius", C.c_int), ("coeff", C.c_double * (MAX_RADIUS + 1)),
+                ("a", C.c_double), ("sigma", C.c_double), ("precond", C.c_int)]
+
+
+class _Params(C.Structure):
+    _fields_ = [("omega", C.c_double), ("beta", C.c_double), ("m", C.c_int), ("p", C.c_int),
+                ("max_iter", C.c_int), ("tol", C.c_double), ("inner_tol", C.c_double),
+                ("max_outer", C.c_int), ("check_every", C.c_int)]
+
+
+class _Result(C.Structure):
+    _fields_ = [("iters", C.c_int), ("relres", C.c_double), ("rhs_norm", C.c_double),
+                ("status", C.c_int), ("outer_iters", C.c_int), ("inner_iters", C.c_int),
+                ("seconds", C.c_double), ("launches", C.c_longlong)]
+
+
+class _KernelStats(C.Structure):
+    _fields_ = [("launches", C.c_longlong * 8), ("ms", C.c_double * 8)]
+
+
+class POISSON(C.Structure):
+    """Leading fields of MPI_REAL/system.h:26-63 (all the library reads)."""
+    _fields_ = [("FDn", C.c_int), ("ssize", C.c_int * 3), ("psize", C.c_int * 3),
+                ("np", C.c_int * 3), ("coords", C.c_int * 3), ("rem", C.c_int * 3),
+                ("send_neighs", C.c_void_p), ("rec_neighs", C.c_void_p),
+                ("send_counts", C.c_void_p), ("rec_counts", C.c_void_p),
+                ("send_layers", C.c_int * 6), ("rec_layers", C.c_int * 6),
+                ("scounts", C.c_void_p), ("sdispls", C.c_void_p), ("rcounts", C.c_void_p),
+                ("rdispls", C.c_void_p), ("n_in", C.c_int), ("n_out", C.c_int),
+                ("phi", C.c_void_p), ("rhs", C.c_void_p), ("Lap_phi", C.c_void_p),
+                ("solver_tol", C.c_double), ("solver_maxiter", C.c_int), ("m", C.c_int),
+                ("p", C.c_int), ("omega", C.c_double), ("beta", C.c_double),
+                ("coeff_lap", C.POINTER(C.c_double)), ("comm_laplacian", C.c_long),
+                ("cart", C.c_long)]
+
+
+LAP_FN = C.CFUNCTYPE(None, C.POINTER(POISSON), C.c_double, C.POINTER(C.c_double),
+                     C.POINTER(C.c_double), C.c_long)
+PRECOND_FN = C.CFUNCTYPE(None, C.c_double, C.POINTER(C.c_double), C.c_int)
+
+_lib = None
+_lock = threading.Lock()
+
+EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "lsg_apply",
+           "lsg_aar", "lsg_pgr", "lsg_pl2r", "lsg_cg", "lsg_aar_mixed", "lsg_pinv_solve",
+           "lsg_release_workspaces", "lsg_last_status", "lsg_last_error", "lsg_status_string",
+           "lsg_version", "AAR", "PGR", "PL2R", "CG", "lsg_register_operator_callback",
+           "lsg_register_precondition_callback", "lsg_set_verbose", "lsg_last_result",
+           "lsg_profile", "lsg_profile_read", "lsg_set_compat_mode"]
+
+KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "unused"]
+
+
+def lib(build_if_missing: bool = True) -> C.CDLL:
+    """Loads liblsg.so (building it first if it is absent and nvcc exists)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH) and build_if_missing:
+            import importlib.util
+            spec = importlib.util.spec_from_file_location("lsg_build", os.path.join(HERE, "build.py"))
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            mod.build()
+        if not os.path.exists(LIB_PATH):
+            raise CudaLibraryError(f"{LIB_PATH} missing: build it with linear-solver_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        vp, ip, dp = C.c_void_p, C.c_int, C.c_double
+        L.lsg_lap_coefficient.argtypes = [ip, C.POINTER(dp)]
+        L.lsg_operator_init.argtypes = [C.POINTER(_Operator), ip, ip, ip, ip, dp, dp, ip]
+        L.lsg_params_default.argtypes = [C.POINTER(_Params)]
+        L.lsg_params_default.restype = None
+        L.lsg_apply.argtypes = [C.POINTER(_Operator), ip, vp, vp, vp]
+        for f in ("lsg_aar", "lsg_pgr", "lsg_pl2r", "lsg_cg"):
+            getattr(L, f).argtypes = [C.POINTER(_Operator), C.POINTER(_Params), ip, vp, vp,
+                                      C.POINTER(_Result), vp]
+        L.lsg_aar_mixed.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), vp, vp,
+                                    C.POINTER(_Result), vp]
+        L.lsg_pinv_solve.argtypes = [vp, vp, vp, ip, vp]
+        L.lsg_last_error.restype = C.c_char_p
+        L.lsg_status_string.restype = C.c_char_p
+        L.lsg_version.restype = C.c_char_p
+        L.lsg_register_operator_callback.argtypes = [vp]
+        L.lsg_register_precondition_callback.argtypes = [vp]
+        L.lsg_set_verbose.argtypes = [ip]
+        L.lsg_set_verbose.restype = None
+        L.lsg_last_result.argtypes = [C.POINTER(_Result)]
+        L.lsg_last_result.restype = None
+        L.AAR.argtypes = [C.POINTER(POISSON), LAP_FN, PRECOND_FN, dp, C.POINTER(dp), C.POINTER(dp),
+                          dp, dp, ip, ip, ip, dp, ip, C.c_long]
+        L.AAR.restype = None
+        for f in ("PGR", "PL2R"):
+            getattr(L, f).argtypes = [C.POINTER(POISSON), LAP_FN, PRECOND_FN, dp, C.POINTER(dp),
+                                      C.POINTER(dp), dp, ip, ip, ip, dp, ip, C.c_long]
+            getattr(L, f).restype = None
+        L.CG.argtypes = [C.POINTER(POISSON), LAP_FN, PRECOND_FN, dp, C.POINTER(dp), C.POINTER(dp),
+                         ip, dp, ip, C.c_long]
+        L.CG.restype = None
+        L.lsg_profile.argtypes = [ip]
+        L.lsg_profile_read.argtypes = [C.POINTER(_KernelStats)]
+        L.lsg_set_compat_mode.argtypes = [ip]
+        L.lsg_set_compat_mode.restype = None
+        _lib = L
+        return L
+
+
+def exported_symbols():
+    return list(EXPORTS)
+
+
+def _check(rc: int, what: str, allow=(0, 1, 2, 8)):
+    if rc not in allow:
+        msg = lib().lsg_last_error().decode(errors="replace")
+        raise CudaLibraryError(f"{what}: {STATUS.get(rc, rc)}: {msg}")
+    return rc
+
+
+def lap_coefficient(radius: int):
+    c = (C.c_double * (MAX_RADIUS + 1))()
+    _check(lib().lsg_lap_coefficient(radius, c), "lsg_lap_coefficient", allow=(0,))
+    return [c[i] for i in range(radius + 1)]
+
+
+class Operator:
+    """A = a * Lap_h + sigma * I on a periodic (nx, ny, nz) grid, FD half-width `radius`."""
+
+    def __init__(self, n, radius: int = 6, a: float = A_REF, sigma: float = 0.0,
+                 precond: bool = True):
+        if isinstance(n, int):
+            n = (n, n, n)
+        self.n = tuple(int(v) for v in n)  # (nx, ny, nz)
+        self.radius, self.a, self.sigma, self.precond = int(radius), float(a), float(sigma), bool(precond)
+        self._s = _Operator()
+        _check(lib().lsg_operator_init(C.byref(self._s), *self.n, self.radius, self.a, self.sigma,
+                                       int(self.precond)), "lsg_operator_init", allow=(0,))
+
+    @property
+    def shape(self):
+        return (self.n[2], self.n[1], self.n[0])
+
+    @property
+    def numel(self):
+        return self.n[0] * self.n[1] * self.n[2]
+
+    @property
+    def diag(self):
+        return self.a * 3.0 * self._s.coeff[0] + self.sigma
+
+    @property
+    def coeff(self):
+        return [self._s.coeff[i] for i in range(self.radius + 1)]
+
+
+def _params(omega=0.6, beta=0.6, m=7, p=6, max_iter=100000, tol=1e-8, inner_tol=1e-3,
+            max_outer=50, check_every=0) -> _Params:
+    prm = _Params()
+    lib().lsg_params_default(C.byref(prm))
+    prm.omega, prm.beta, prm.m, prm.p = omega, beta, m, p
+    prm.max_iter, prm.tol, prm.inner_tol = max_iter, tol, inner_tol
+    prm.max_outer, prm.check_every = max_outer, check_every
+    return prm
+
+
+def _stream_ptr(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _dtype_code(t):
+    import torch
+    if t.dtype == torch.float64:
+        return F64
+    if t.dtype == torch.float32:
+        return F32
+    raise TypeError(f"unsupported dtype {t.dtype}")
+
+
+def _check_vec(t, op: Operator, name: str):
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if t.numel() != op.numel:
+        raise ValueError(f"{name} has {t.numel()} values, grid has {op.numel}")
+
+
+def _result(r: _Result) -> dict:
+    return dict(iters=r.iters, relres=r.relres, rhs_norm=r.rhs_norm, status=r.status,
+                status_name=STATUS.get(r.status, str(r.status)), outer_iters=r.outer_iters,
+                inner_iters=r.inner_iters, seconds=r.seconds, launches=r.launches)
+
+
+def apply(op: Operator, x, out=None, stream=None):
+    """y = A x on the device."""
+    import torch
+    _check_vec(x, op, "x")
+    y = torch.empty_like(x) if out is None else out
+    _check(lib().lsg_apply(C.byref(op._s), _dtype_code(x), C.c_void_p(x.data_ptr()),
+                           C.c_void_p(y.data_ptr()), _stream_ptr(stream)), "lsg_apply", allow=(0,))
+    return y
+
+
+def _solve(fn: str, op: Operator, b, x0=None, stream=None, **kw):
+    import torch
+    _check_vec(b, op, "b")
+    x = torch.zeros_like(b) if x0 is None else x0.clone()
+    _check_vec(x, op, "x0")
+    if x.dtype != b.dtype:
+        raise TypeError("x0 and b dtypes differ")
+    res = _Result()
+    prm = _params(**kw)
+    rc = getattr(lib(), fn)(C.byref(op._s), C.byref(prm), _dtype_code(b), C.c_void_p(x.data_ptr()),
+                            C.c_void_p(b.data_ptr()), C.byref(res), _stream_ptr(stream))
+    _check(rc, fn)
+    return x, _result(res)
+
+
+def aar(op, b, x0=None, **kw):
+    """Alternating Anderson-Richardson (MPI_REAL/AAR.c:37)."""
+    return _solve("lsg_aar", op, b, x0, **kw)
+
+
+def pgr(op, b, x0=None, **kw):
+    """Periodic Galerkin-Richardson (MPI_REAL/PGR.c:35)."""
+    return _solve("lsg_pgr", op, b, x0, **kw)
+
+
+def pl2r(op, b, x0=None, **kw):
+    """Periodic L2-Richardson (MPI_REAL/PL2R.c:35)."""
+    return _solve("lsg_pl2r", op, b, x0, **kw)
+
+
+def cg(op, b, x0=None, **kw):
+    """Jacobi-preconditioned CG (MPI_REAL/CG.c:33)."""
+    return _solve("lsg_cg", op, b, x0, **kw)
+
+
+SOLVERS = {"aar": aar, "pgr": pgr, "pl2r": pl2r, "cg": cg}
+
+
+def aar_mixed(op, b, x0=None, stream=None, **kw):
+    """FP64 iterative refinement around an FP32 AAR; b and x are float64."""
+    import torch
+    if b.dtype != torch.float64:
+        raise TypeError("aar_mixed takes float64 b / x")
+    _check_vec(b, op, "b")
+    x = torch.zeros_like(b) if x0 is None else x0.clone()
+    res = _Result()
+    prm = _params(**kw)
+    rc = lib().lsg_aar_mixed(C.byref(op._s), C.byref(prm), C.c_void_p(x.data_ptr()),
+                             C.c_void_p(b.data_ptr()), C.byref(res), _stream_ptr(stream))
+    _check(rc, "lsg_aar_mixed")
+    return x, _result(res)
+
+
+def pinv_solve(A, b, stream=None):
+    """x = pinv(A) b with the reference semantics (MPI_REAL/tools.c:52-105), one warp on the GPU."""
+    import torch
+    A = A.to(dtype=torch.float64).contiguous()
+    b = b.to(dtype=torch.float64).contiguous()
+    x = torch.zeros_like(b)
+    rc = lib().lsg_pinv_solve(C.c_void_p(A.data_ptr()), C.c_void_p(b.data_ptr()),
+                              C.c_void_p(x.data_ptr()), int(b.numel()), _stream_ptr(stream))
+    _check(rc, "lsg_pinv_solve", allow=(0, 8))
+    return x, rc
+
+
+def profile(on: bool):
+    """Start (clearing totals) or stop per-kernel-class CUDA-event timing."""
+    lib().lsg_profile(1 if on else 0)
+
+
+def profile_read() -> dict:
+    """{class: (launches, total_ms)} collected since profile(True)."""
+    st = _KernelStats()
+    lib().lsg_profile_read(C.byref(st))
+    return {KERNEL_CLASSES[i]: (st.launches[i], st.ms[i]) for i in range(7)}
+
+
+def set_compat_mode(mixed: bool):
+    """Drop-in AAR precision: False = FP64 (reference semantics), True = mixed."""
+    lib().lsg_set_compat_mode(1 if mixed else 0)
+
+
+def release_workspaces():
+    lib().lsg_release_workspaces()
+
+
+# ----------------------------------------------------------------------------- drop-in entry points
+
+_keep = []
+
+
+def _dummy_lap(system, a, x, y, comm):  # never called by the library
+    raise RuntimeError("host operator callback must not be called")
+
+
+def _dummy_pc(diag, r, n):  # never called by the library
+    raise RuntimeError("host preconditioner callback must not be called")
+
+
+def reference_callbacks():
+    """ctypes callbacks registered as the reference operator / Jacobi preconditioner.
+
+    They stand for MPI_REAL/system.c's Lap_Vec_mult and Precondition when the
+    caller is Python; liblsg recognises them by address and never calls them.
+    """
+    if not _keep:
+        lap, pc = LAP_FN(_dummy_lap), PRECOND_FN(_dummy_pc)
+        L = lib()
+        _check(L.lsg_register_operator_callback(C.cast(lap, C.c_void_p)), "register", allow=(0,))
+        _check(L.lsg_register_precondition_callback(C.cast(pc, C.c_void_p)), "register", allow=(0,))
+        _keep.extend([lap, pc])
+    return _keep[0], _keep[1]
+
+
+def make_poisson(n, fdn: int = 6):
+    """A POISSON struct for a one-rank run on an (nx, ny, nz) grid (MPI_REAL/main.c:29-54)."""
+    if isinstance(n, int):
+        n = (n, n, n)
+    s = POISSON()
+    s.FDn = fdn
+    for d in range(3):
+        s.ssize[d] = n[d]
+        s.psize[d] = n[d]
+        s.np[d] = 1
+    coeff = (C.c_double * (fdn + 1))(*lap_coefficient(fdn))
+    s.coeff_lap = C.cast(coeff, C.POINTER(C.c_double))
+    s._coeff_keep = coeff
+    return s
+
+
+def compat_solve(solver: str, x, rhs, *, n=None, fdn=6, a=A_REF, precond=True, omega=0.6,
+                 beta=0.6, m=7, p=6, max_iter=100000, tol=1e-8, verbose=False, system=None,
+                 lap=None, pc=None):
+    """Calls the reference-prototype entry point (AAR/PGR/PL2R/CG) on host numpy arrays.
+
+    x (float64, C-contiguous) is overwritten with the solution, as the
+    reference does.  Returns the lsg_result of the call as a dict.
+    """
+    import numpy as np
+    L = lib()
+    assert x.dtype == np.float64 and x.flags.c_contiguous
+    assert rhs.dtype == np.float64 and rhs.flags.c_contiguous
+    if n is None:
+        nz, ny, nx = x.shape
+        n = (nx, ny, nz)
+    s = make_poisson(n, fdn) if system is None else system
+    rlap, rpc = reference_callbacks()
+    lap = rlap if lap is None else lap
+    pc = (rpc if precond else PRECOND_FN()) if pc is None else pc
+    L.lsg_set_verbose(1 if verbose else 0)
+    dp = C.POINTER(C.c_double)
+    xp, bp = x.ctypes.data_as(dp), rhs.ctypes.data_as(dp)
+    np_ = int(x.size)
+    if solver == "aar":
+        L.AAR(C.byref(s), lap, pc, a, xp, bp, omega, beta, m, p, max_iter, tol, np_, 3)
+    elif solver == "pgr":
+        L.PGR(C.byref(s), lap, pc, a, xp, bp, omega, m, p, max_iter, tol, np_, 3)
+    elif solver == "pl2r":
+        L.PL2R(C.byref(s), lap, pc, a, xp, bp, omega, m, p, max_iter, tol, np_, 3)
+    elif solver == "cg":
+        L.CG(C.byref(s), lap, pc, a, xp, bp, max_iter, tol, np_, 3)
+    else:
+        raise ValueError(solver)
+    res = _Result()
+    L.lsg_last_result(C.byref(res))
+    out = _result(res)
+    out["last_status"] = L.lsg_last_status()
+    return out
