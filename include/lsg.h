@@ -119,6 +119,18 @@ int lsg_aar_mixed(const lsg_operator *op, const lsg_params *prm, double *d_x, co
  * computed on the device by one warp.  A row-major, device pointers. */
 int lsg_pinv_solve(const double *d_A, const double *d_b, double *d_x, int m, void *stream);
 
+/* The same solve without any device allocation (no counterpart in the
+ * reference, whose solver mallocs its work arrays on every call).  For
+ * callers that must not call cudaMalloc -- device memory already owned by an
+ * external pool or capped per client, or a loop that cannot pay for an
+ * allocation per call -- the kernel's status word lives in a 256-byte static
+ * device array that every GPU loading the library holds until exit.  m above
+ * LSG_MAX_M is rejected with LSG_BAD_ARG.  The first call on a device looks up
+ * that array's address and must come before any stream capture.  Calls share
+ * the array: calls that overlap on the GPU race.  Synchronises `stream`. */
+int lsg_pinv_solve_noalloc(const double *d_A, const double *d_b, double *d_x, int m,
+                           void *stream);
+
 /* Per-kernel-class device time, measured with CUDA events recorded on the
  * solve's stream around each launch while profiling is on. */
 enum lsg_kernel_class {

@@ -16,7 +16,10 @@
 // so the column dot products are warp reductions.  The sweep count is bounded
 // and exhaustion is reported as LSG_SVD_NO_CONVERGENCE (the reference exits
 // the process after 250 iterations, tools.c:270).
+#include <mutex>
+
 #include "lsg_internal.cuh"
+#include "lsg_host.h"
 
 namespace lsg {
 
@@ -269,3 +272,75 @@ cudaError_t pinv_solve_dev(const double *A, const double *b, double *x, int m, i
 }
 
 }  // namespace lsg
+
+// ---------------------------------------------------------------- allocation-free pinv solve
+//
+// lsg_pinv_solve_noalloc: the m x m pseudo-inverse solve for callers that must
+// not allocate device memory.  lsg_pinv_solve allocates the kernel's status
+// word with cudaMallocAsync on every call; this variant keeps it in the
+// file-scope array below instead.  Callers that cannot call cudaMalloc
+// include code that runs while the device memory is already owned by an
+// external pool (an application allocator or a memory-capped MPS client,
+// where a new allocation fails or breaks its budget) and latency-bound
+// loops that call the small solve every few iterations and cannot afford an
+// allocation round trip each time.
+//
+// The scratch is LSG_PINV_NOALLOC_SCRATCH_INTS ints (256 bytes), held on
+// every GPU that loads the library until the process exits.  Every call
+// shares it and it keeps the last call's contents, so the status word is
+// cleared on the call's stream before each launch; calls that overlap on the
+// GPU (different streams, or threads) race on it.  The device address of the
+// array is looked up once per device by the first call made with that device
+// current, which therefore must come before any stream capture.
+
+#define LSG_PINV_NOALLOC_SCRATCH_INTS 64
+static __device__ __align__(256) int g_pinv_noalloc_scratch[LSG_PINV_NOALLOC_SCRATCH_INTS];
+
+namespace {
+
+std::mutex g_noalloc_mu;
+constexpr int kNoallocMaxDevices = 64;
+int *g_noalloc_addr[kNoallocMaxDevices];
+
+}  // namespace
+
+extern "C" int lsg_pinv_solve_noalloc(const double *d_A, const double *d_b, double *d_x, int m,
+                                      void *stream) {
+    if (m < 1 || m > LSG_MAX_M)
+        return lsg::set_error(LSG_BAD_ARG,
+                              "lsg_pinv_solve_noalloc: m = %d outside 1..%d (the allocation-free "
+                              "solve keeps its m x m work in shared memory)", m, LSG_MAX_M);
+    if (!d_A || !d_b || !d_x) return lsg::set_error(LSG_BAD_ARG, "lsg_pinv_solve_noalloc: NULL pointer");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return lsg::set_error(LSG_CUDA_ERROR, "cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= kNoallocMaxDevices)
+        return lsg::set_error(LSG_UNSUPPORTED, "lsg_pinv_solve_noalloc: device %d beyond %d", dev,
+                              kNoallocMaxDevices);
+    int *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> g(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            // One-time set-up on this device (current): the host-side name of the
+            // array is not a device address, so ask the runtime for it.
+            void *p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_pinv_noalloc_scratch);
+            if (e != cudaSuccess)
+                return lsg::set_error(LSG_CUDA_ERROR, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+            g_noalloc_addr[dev] = (int *)p;
+        }
+        scratch = g_noalloc_addr[dev];
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    e = cudaMemsetAsync(scratch, 0, sizeof(int), s);
+    if (e != cudaSuccess) return lsg::set_error(LSG_CUDA_ERROR, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+    lsg::pinv_kernel<<<1, 32, 0, s>>>(d_A, d_b, d_x, m, scratch);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return lsg::set_error(LSG_CUDA_ERROR, "pinv launch: %s", cudaGetErrorString(e));
+    int st = 0;
+    e = cudaMemcpyAsync(&st, scratch, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return lsg::set_error(LSG_CUDA_ERROR, "status read: %s", cudaGetErrorString(e));
+    return st;
+}
+
