@@ -337,6 +337,35 @@ def run_lsg(args):
     return 0
 
 
+def run_case(case: str):
+    """Short fixed invocations for profilers (ncu): one launch pattern each.
+
+    rich32 / rich64: 5 AAR iterations (FP32 / FP64 vectors) of the 256^3
+    workload -- a residual and four fused Richardson launches.
+    mixed / fp64: one complete solve of the benchmark workload.
+    """
+    import torch
+
+    import lsg
+    import workloads
+
+    torch.cuda.set_device(0)
+    op = lsg.Operator(N_GRID)
+    b = torch.from_numpy(workloads.uniform_rhs(N_GRID, SEED)).cuda()
+    if case == "rich32":
+        x, info = lsg.aar(op, b.float(), max_iter=5, **{k: v for k, v in SOLVER_KW.items()})
+    elif case == "rich64":
+        x, info = lsg.aar(op, b, max_iter=5, **SOLVER_KW)
+    elif case == "mixed":
+        x, info = lsg.aar_mixed(op, b, **SOLVER_KW)
+    else:
+        x, info = lsg.aar(op, b, **SOLVER_KW)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": case, "iters": info["iters"], "relres": info["relres"],
+                      "launches": info["launches"], "status": info["status_name"]}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -344,7 +373,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="lsg", choices=["lsg", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--case", choices=["rich32", "rich64", "mixed", "fp64"],
+                    help="run one short fixed invocation for a profiler and exit")
     args = ap.parse_args()
+    if args.case:
+        return run_case(args.case)
     if args.impl == "reference":
         return run_reference(args)
     return run_lsg(args)
