@@ -130,24 +130,26 @@ struct StencilLaunch {
 // registers); FP32 is bandwidth-bound (taller tile, less halo per point).
 // A block is 32 x BY threads covering 32 x (BY*NY) columns.
 template <typename T> struct TileOf;
-template <> struct TileOf<double> { static constexpr int BY = 8, NY = 2; };
-template <> struct TileOf<float> { static constexpr int BY = 8, NY = 4; };
+template <> struct TileOf<double> { static constexpr int BY = 8, NY = 2, MINB = 1; };
+template <> struct TileOf<float> { static constexpr int BY = 8, NY = 2, MINB = 3; };
 
 inline dim3 stencil_grid(const Geom &g, int ty, int lz) {
     return dim3((unsigned)((g.nx + 31) / 32), (unsigned)((g.ny + ty - 1) / ty),
                 (unsigned)((g.nz + lz - 1) / lz));
 }
 
-// z planes per block: enough blocks for ~4 per SM, at least 16 planes so the
-// 2R-plane warm-up of the register queue stays a small fraction.
+// z planes per block.  With `slots` = SMs x resident blocks per SM, the xy
+// tiles are split along z into as many chunks as fit in one wave (a second,
+// partial wave would double the time of its blocks); chunks shorter than 8
+// planes are avoided because each chunk re-reads 2R planes to fill its queue.
 template <typename T>
-inline int choose_lz(const Geom &g, int sms) {
+inline int choose_lz(const Geom &g, int slots) {
     const int ty = TileOf<T>::BY * TileOf<T>::NY;
     const long long bxy = (long long)((g.nx + 31) / 32) * ((g.ny + ty - 1) / ty);
-    long long chunks = (4LL * sms + bxy - 1) / bxy;
+    long long chunks = bxy >= slots ? 1 : slots / bxy;
     if (chunks < 1) chunks = 1;
     int lz = (int)((g.nz + chunks - 1) / chunks);
-    if (lz < 16) lz = 16;
+    if (lz < 8) lz = 8;
     if (lz > g.nz) lz = g.nz;
     return lz;
 }
@@ -161,6 +163,8 @@ inline long long stencil_blocks(const Geom &g, int lz) {
 
 template <typename T>
 struct Kernels {
+    // Resident blocks per SM of the fused Richardson stencil kernel.
+    static int stencil_blocks_per_sm();
     // y / r update driven by one stencil pass over x.
     static cudaError_t residual(const StencilLaunch &L, const Weights<T> &w, int mode,
                                 const T *x, const T *b, T *r, T *df, double cf,
@@ -170,6 +174,15 @@ struct Kernels {
     static cudaError_t richardson(const StencilLaunch &L, const Weights<T> &w, int mode,
                                   const T *x, const T *r, const T *b, T *x2, T *r2, T *dx,
                                   T *df, double c, double cf, const DevCtrl *ctrl);
+    // Residual-recurrence Richardson step (FP32 inner solver): r2 = r - c A r,
+    // x += c r in place, DX = x_new - x_old, DF = (r2 - r) cf.
+    static cudaError_t richardson_recur(const StencilLaunch &L, const Weights<T> &w, const T *r,
+                                        T *x, T *r2, T *dx, T *df, double c, double cf,
+                                        const DevCtrl *ctrl);
+    // Extrapolation-step residual by recurrence: r -= A dxc; DF = (r_new - r) cf; ||r||^2.
+    static cudaError_t residual_recur(const StencilLaunch &L, const Weights<T> &w, const T *dxc,
+                                      T *r, T *df, double cf, double *partials,
+                                      const DevCtrl *ctrl);
     // Gram partials over the history (point-local, grid-stride).
     static cudaError_t gram(int kind, int m, const T *dx, const T *df, const T *r, long long n,
                             double *partials, int blocks, const DevCtrl *ctrl, cudaStream_t s);

@@ -11,6 +11,7 @@
 #pragma once
 
 #include <algorithm>
+#include <type_traits>
 
 #include "lsg_stencil.cuh"
 
@@ -24,9 +25,17 @@ __device__ __forceinline__ bool solve_done(const DevCtrl *c) {
 
 // ---------------------------------------------------------------- stencil functors
 
+template <typename T> struct Pair { T a, b; };
+template <typename T> struct Triple { T a, b, c; };
+
+// r = b - A x (RES_INIT, with ||r||^2), the AAR extrapolation residual
+// (RES_ANDERSON: also DF_col = (r_new - r) * cf, r in place), or y = A x.
 template <typename T, int MODE>
 struct ResidualOp {
     static constexpr int NACC = (MODE == RES_APPLY) ? 0 : 1;
+    using Raw = T;
+    using Ctr = typename std::conditional<MODE == RES_ANDERSON, Pair<T>,
+                typename std::conditional<MODE == RES_INIT, T, NoCtr>::type>::type;
     const T *x;
     const T *b;
     T *r;
@@ -36,22 +45,37 @@ struct ResidualOp {
     const DevCtrl *ctrl;
     __device__ bool skip() const { return solve_done(ctrl); }
     __device__ void init() {}
-    __device__ __forceinline__ T load(long long i) const { return ldg(x + i); }
-    __device__ __forceinline__ void store(long long i, T u, T au, Acc<T> *acc) const {
-        if (MODE == RES_APPLY) {
+    __device__ __forceinline__ Raw fetch(long long i) const { return ldg(x + i); }
+    __device__ __forceinline__ T value(const Raw &v) const { return v; }
+    __device__ __forceinline__ Ctr fetch_center(long long i) const {
+        if constexpr (MODE == RES_ANDERSON) return Ctr{ldg(b + i), r[i]};
+        else if constexpr (MODE == RES_INIT) return ldg(b + i);
+        else return Ctr{};
+    }
+    __device__ __forceinline__ void store(long long i, T u, T au, const Ctr &c, Acc<T> *acc) const {
+        if constexpr (MODE == RES_APPLY) {
             r[i] = au;
+        } else if constexpr (MODE == RES_INIT) {
+            const T rn = c - au;
+            r[i] = rn;
+            acc[0].add_prod(rn, rn);
         } else {
-            const T rn = ldg(b + i) - au;
-            if (MODE == RES_ANDERSON) df[i] = (rn - r[i]) * cf;
+            const T rn = c.a - au;
+            df[i] = (rn - c.b) * cf;
             r[i] = rn;
             acc[0].add_prod(rn, rn);
         }
     }
 };
 
+// Fused Richardson step in the reference's form (AAR.c:93-107,134-139;
+// PGR.c:92-109): u = x + omega*cf*r at every stencil point, r2 = b - A u,
+// x2 = u, DX = u - x, DF = (r2 - r) cf (AAR) or r - r2 (PGR / PL2R).
 template <typename T, int MODE>
 struct RichOp {
     static constexpr int NACC = 0;
+    using Raw = Pair<T>;    // (x, r)
+    using Ctr = Triple<T>;  // (b, x, r) at the centre
     const T *x;
     const T *r;
     const T *b;
@@ -65,21 +89,87 @@ struct RichOp {
     const DevCtrl *ctrl;
     __device__ bool skip() const { return solve_done(ctrl); }
     __device__ void init() {}
-    __device__ __forceinline__ T load(long long i) const { return fma(c, ldg(r + i), ldg(x + i)); }
-    __device__ __forceinline__ void store(long long i, T u, T au, Acc<T> *) const {
-        const T rn = ldg(b + i) - au;
-        const T xo = ldg(x + i);
-        const T ro = ldg(r + i);
+    __device__ __forceinline__ Raw fetch(long long i) const { return Raw{ldg(x + i), ldg(r + i)}; }
+    __device__ __forceinline__ T value(const Raw &v) const { return fma(c, v.b, v.a); }
+    __device__ __forceinline__ Ctr fetch_center(long long i) const {
+        return Ctr{ldg(b + i), ldg(x + i), ldg(r + i)};
+    }
+    __device__ __forceinline__ void store(long long i, T u, T au, const Ctr &cc, Acc<T> *) const {
+        const T rn = cc.a - au;
         x2[i] = u;
         r2[i] = rn;
-        dx[i] = u - xo;
-        df[i] = (MODE == RICH_AAR) ? (rn - ro) * cf : (ro - rn);
+        dx[i] = u - cc.b;
+        df[i] = (MODE == RICH_AAR) ? (rn - cc.c) * cf : (cc.c - rn);
     }
 };
 
+// Richardson step of the FP32 inner solver in residual-recurrence form:
+// f = cf r, r2 = r - omega A f, x += omega f (in place), DX = x_new - x,
+// DF = (r2 - r) cf.  Equal in exact arithmetic to the form above; it stages
+// one array (r) instead of two and never reads b, and its rounding is
+// relative to |r| rather than to |x|.
+template <typename T>
+struct RichRecurOp {
+    static constexpr int NACC = 0;
+    using Raw = T;
+    using Ctr = T;  // x at the centre
+    const T *r;
+    T *x;
+    T *r2;
+    T *dx;
+    T *df;
+    T c;    // omega * cf
+    T cf;
+    double *partials;
+    const DevCtrl *ctrl;
+    __device__ bool skip() const { return solve_done(ctrl); }
+    __device__ void init() {}
+    __device__ __forceinline__ Raw fetch(long long i) const { return ldg(r + i); }
+    __device__ __forceinline__ T value(const Raw &v) const { return v; }
+    __device__ __forceinline__ Ctr fetch_center(long long i) const { return x[i]; }
+    __device__ __forceinline__ void store(long long i, T rc, T ar, const Ctr &xo, Acc<T> *) const {
+        const T rn = fma(-c, ar, rc);
+        const T xn = fma(c, rc, xo);
+        x[i] = xn;
+        r2[i] = rn;
+        dx[i] = xn - xo;
+        df[i] = (rn - rc) * cf;
+    }
+};
+
+// Extrapolation-step residual of the FP32 inner solver: the update kernel
+// leaves the step dx_col = x_new - x_old, so r_new = r - A dx_col (r in
+// place), DF_col = (r_new - r) cf, ||r_new||^2.
+template <typename T>
+struct ResRecurOp {
+    static constexpr int NACC = 1;
+    using Raw = T;
+    using Ctr = T;  // r at the centre
+    const T *dxc;
+    T *r;
+    T *df;
+    T cf;
+    double *partials;
+    const DevCtrl *ctrl;
+    __device__ bool skip() const { return solve_done(ctrl); }
+    __device__ void init() {}
+    __device__ __forceinline__ Raw fetch(long long i) const { return ldg(dxc + i); }
+    __device__ __forceinline__ T value(const Raw &v) const { return v; }
+    __device__ __forceinline__ Ctr fetch_center(long long i) const { return r[i]; }
+    __device__ __forceinline__ void store(long long i, T, T au, const Ctr &ro, Acc<T> *acc) const {
+        const T rn = ro - au;
+        df[i] = (rn - ro) * cf;
+        r[i] = rn;
+        acc[0].add_prod(rn, rn);
+    }
+};
+
+// CG: d_new = cf r + beta d_old at every stencil point, q = A d_new, d.q.
 template <typename T>
 struct CgDirOp {
     static constexpr int NACC = 1;
+    using Raw = Pair<T>;  // (r, d_old)
+    using Ctr = NoCtr;
     const T *r;
     const T *d_old;
     T *d_new;
@@ -90,16 +180,21 @@ struct CgDirOp {
     const DevCtrl *ctrl;
     __device__ bool skip() const { return solve_done(ctrl); }
     __device__ void init() { beta = (T)ctrl->beta; }
-    __device__ __forceinline__ T load(long long i) const { return fma(beta, ldg(d_old + i), cf * ldg(r + i)); }
-    __device__ __forceinline__ void store(long long i, T u, T au, Acc<T> *acc) const {
+    __device__ __forceinline__ Raw fetch(long long i) const { return Raw{ldg(r + i), ldg(d_old + i)}; }
+    __device__ __forceinline__ T value(const Raw &v) const { return fma(beta, v.b, cf * v.a); }
+    __device__ __forceinline__ Ctr fetch_center(long long) const { return Ctr{}; }
+    __device__ __forceinline__ void store(long long i, T u, T au, const Ctr &, Acc<T> *acc) const {
         d_new[i] = u;
         q[i] = au;
         acc[0].add_prod(u, au);
     }
 };
 
+// FP64 refinement residual: r32 = float(b - A x), ||b - A x||^2 in FP64.
 struct IrResidualOp {
     static constexpr int NACC = 1;
+    using Raw = double;
+    using Ctr = double;  // b
     const double *x;
     const double *b;
     float *r32;
@@ -107,9 +202,12 @@ struct IrResidualOp {
     const DevCtrl *ctrl;
     __device__ bool skip() const { return solve_done(ctrl); }
     __device__ void init() {}
-    __device__ __forceinline__ double load(long long i) const { return ldg(x + i); }
-    __device__ __forceinline__ void store(long long i, double u, double au, Acc<double> *acc) const {
-        const double rn = ldg(b + i) - au;
+    __device__ __forceinline__ Raw fetch(long long i) const { return ldg(x + i); }
+    __device__ __forceinline__ double value(const Raw &v) const { return v; }
+    __device__ __forceinline__ Ctr fetch_center(long long i) const { return ldg(b + i); }
+    __device__ __forceinline__ void store(long long i, double, double au, const Ctr &bb,
+                                          Acc<double> *acc) const {
+        const double rn = bb - au;
         r32[i] = (float)rn;
         acc[0].add_prod(rn, rn);
     }
@@ -119,22 +217,57 @@ struct IrResidualOp {
 
 template <typename T, class Op>
 cudaError_t launch_stencil(const StencilLaunch &L, const Weights<T> &w, const Op &op) {
-    constexpr int BY = TileOf<T>::BY, NY = TileOf<T>::NY;
+    constexpr int BY = TileOf<T>::BY, NY = TileOf<T>::NY, MB = TileOf<T>::MINB;
     const dim3 grid = stencil_grid(L.g, BY * NY, L.lz);
     const dim3 block(32, BY);
     if (w.radius == 6)
-        stencil_kernel<T, 6, BY, NY, false, Op><<<grid, block, 0, L.stream>>>(L.g, w, L.lz, op);
+        stencil_kernel<T, 6, BY, NY, MB, false, Op><<<grid, block, 0, L.stream>>>(L.g, w, L.lz, op);
     else
-        stencil_kernel<T, LSG_MAX_RADIUS, BY, NY, true, Op><<<grid, block, 0, L.stream>>>(L.g, w, L.lz, op);
+        stencil_kernel<T, LSG_MAX_RADIUS, BY, NY, 1, true, Op><<<grid, block, 0, L.stream>>>(L.g, w, L.lz, op);
     return cudaGetLastError();
+}
+
+template <typename T>
+int Kernels<T>::stencil_blocks_per_sm() {
+    constexpr int BY = TileOf<T>::BY, NY = TileOf<T>::NY;
+    int n = 0;
+    cudaError_t e;
+    if (std::is_same<T, float>::value)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &n, stencil_kernel<T, 6, BY, NY, TileOf<T>::MINB, false, RichRecurOp<T>>, 32 * BY, 0);
+    else
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &n, stencil_kernel<T, 6, BY, NY, TileOf<T>::MINB, false, RichOp<T, RICH_AAR>>, 32 * BY, 0);
+    if (e != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        n = 2;
+    }
+    return n;
 }
 
 // ---------------------------------------------------------------- point-local kernels
 
-// Gram partials for history depth M (register accumulators).  FP32 vectors:
-// products summed in FP32 over runs of kRun points, each run folded into a
-// double-float accumulator; FP64 vectors: plain FP64 sums.
-constexpr int kRun = 8;
+// Gram partials for history depth M (register accumulators), VEC consecutive
+// points per thread and step (one 16-byte load per vector).  FP32 vectors:
+// the VEC products of a step are summed in FP32 and folded into a
+// double-float accumulator (lsg_accum.cuh); FP64 vectors: FP64 FMAs.
+template <typename T> struct Vec4;
+template <> struct Vec4<float> { using type = float4; static constexpr int N = 4; };
+template <> struct Vec4<double> { using type = double2; static constexpr int N = 2; };
+
+template <typename V> __device__ __forceinline__ V ldv(const V *p) { return __ldg(p); }
+
+__device__ __forceinline__ float dotv(const float4 &a, const float4 &b) {
+    float p = a.x * b.x;
+    p = fmaf(a.y, b.y, p);
+    p = fmaf(a.z, b.z, p);
+    return fmaf(a.w, b.w, p);
+}
+__device__ __forceinline__ void accv(Acc<float> &acc, const float4 &a, const float4 &b) { acc.add(dotv(a, b)); }
+__device__ __forceinline__ void accv(Acc<double> &acc, const double2 &a, const double2 &b) {
+    acc.add_prod(a.x, b.x);
+    acc.add_prod(a.y, b.y);
+}
 
 template <typename T, int KIND, int M>
 __global__ void __launch_bounds__(kReduceThreads) gram_kernel(const T *__restrict__ dx,
@@ -142,50 +275,49 @@ __global__ void __launch_bounds__(kReduceThreads) gram_kernel(const T *__restric
                                                               const T *__restrict__ r, long long n,
                                                               double *partials,
                                                               const DevCtrl *ctrl) {
+    using V = typename Vec4<T>::type;
+    constexpr int VN = Vec4<T>::N;
     constexpr int NP = (KIND == GRAM_SYM) ? (M * (M + 1)) / 2 : M * M;
     constexpr int NV = NP + M;
     __shared__ double red[NV * (kReduceThreads / 32)];
     if (solve_done(ctrl)) return;
     Acc<T> acc[NV];
-    T run[NV];
 #pragma unroll
-    for (int k = 0; k < NV; k++) { acc[k].zero(); run[k] = T(0); }
-    int cnt = 0;
+    for (int k = 0; k < NV; k++) acc[k].zero();
+    const long long nv = n / VN;  // caller guarantees n % VN == 0
+    const V *dfv = reinterpret_cast<const V *>(df);
+    const V *dxv = reinterpret_cast<const V *>(dx);
+    const V *rvv = reinterpret_cast<const V *>(r);
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        T f[M], xv[KIND == GRAM_SYM ? 1 : M];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride) {
+        V f[M], xv[KIND == GRAM_SYM ? 1 : M];
 #pragma unroll
-        for (int j = 0; j < M; j++) f[j] = ldg(df + j * n + i);
+        for (int j = 0; j < M; j++) f[j] = ldv(dfv + j * nv + i);
         if (KIND == GRAM_GALERKIN) {
 #pragma unroll
-            for (int j = 0; j < M; j++) xv[j] = ldg(dx + j * n + i);
+            for (int j = 0; j < M; j++) xv[j] = ldv(dxv + j * nv + i);
         }
-        const T rv = ldg(r + i);
+        const V rv = ldv(rvv + i);
         int k = 0;
         if (KIND == GRAM_SYM) {
 #pragma unroll
             for (int j = 0; j < M; j++)
 #pragma unroll
-                for (int a = 0; a <= j; a++) { run[k] = fma(f[a], f[j], run[k]); k++; }
+                for (int a = 0; a <= j; a++) { accv(acc[k], f[a], f[j]); k++; }
 #pragma unroll
-            for (int j = 0; j < M; j++) { run[NP + j] = fma(f[j], rv, run[NP + j]); }
+            for (int j = 0; j < M; j++) accv(acc[NP + j], f[j], rv);
         } else {
 #pragma unroll
             for (int a = 0; a < M; a++)
 #pragma unroll
-                for (int j = 0; j < M; j++) { run[k] = fma(xv[a], f[j], run[k]); k++; }
+                for (int j = 0; j < M; j++) { accv(acc[k], xv[a], f[j]); k++; }
 #pragma unroll
-            for (int j = 0; j < M; j++) { run[NP + j] = fma(xv[j], rv, run[NP + j]); }
-        }
-        if (sizeof(T) == 4 && ++cnt == kRun) {
-#pragma unroll
-            for (int q = 0; q < NV; q++) { acc[q].add(run[q]); run[q] = T(0); }
-            cnt = 0;
+            for (int j = 0; j < M; j++) accv(acc[NP + j], xv[j], rv);
         }
     }
     double v[NV];
 #pragma unroll
-    for (int q = 0; q < NV; q++) { acc[q].add(run[q]); v[q] = acc[q].get(); }
+    for (int q = 0; q < NV; q++) v[q] = acc[q].get();
     block_sum_store<NV>(v, red, partials + (long long)blockIdx.x * NV);
 }
 
@@ -371,11 +503,28 @@ cudaError_t Kernels<T>::richardson(const StencilLaunch &L, const Weights<T> &w, 
     return launch_stencil<T>(L, w, op);
 }
 
+template <typename T>
+cudaError_t Kernels<T>::richardson_recur(const StencilLaunch &L, const Weights<T> &w, const T *r,
+                                         T *x, T *r2, T *dx, T *df, double c, double cf,
+                                         const DevCtrl *ctrl) {
+    RichRecurOp<T> op{r, x, r2, dx, df, (T)c, (T)cf, nullptr, ctrl};
+    return launch_stencil<T>(L, w, op);
+}
+
+template <typename T>
+cudaError_t Kernels<T>::residual_recur(const StencilLaunch &L, const Weights<T> &w, const T *dxc,
+                                       T *r, T *df, double cf, double *partials,
+                                       const DevCtrl *ctrl) {
+    ResRecurOp<T> op{dxc, r, df, (T)cf, partials, ctrl};
+    return launch_stencil<T>(L, w, op);
+}
+
 template <typename T, int KIND>
 static cudaError_t gram_dispatch(int m, const T *dx, const T *df, const T *r, long long n,
                                  double *partials, int blocks, const DevCtrl *ctrl,
                                  cudaStream_t s) {
-    switch (m) {
+    const int vn = Vec4<T>::N;
+    switch (n % vn == 0 ? m : 0) {
 #define LSG_GRAM_CASE(MM) \
     case MM: gram_kernel<T, KIND, MM><<<blocks, kReduceThreads, 0, s>>>(dx, df, r, n, partials, ctrl); break;
         LSG_GRAM_CASE(1) LSG_GRAM_CASE(2) LSG_GRAM_CASE(3) LSG_GRAM_CASE(4)

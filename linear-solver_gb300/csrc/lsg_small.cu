@@ -84,8 +84,40 @@ __global__ void finalize_norm_kernel(const double *partials, int nparts, DevCtrl
 
 // ---------------------------------------------------------------- m x m solve
 
-// One warp; G and V in shared memory (row-major, ld = m); lane k owns row k.
-// Returns 0 on convergence, LSG_SVD_NO_CONVERGENCE otherwise.
+// Stopping test of the Jacobi sweeps: a column pair counts as orthogonal once
+// gamma^2 <= (kJacobiTol)^2 * alpha * beta.
+constexpr double kJacobiTol = 8 * kPinvEps;
+
+// x = V diag(1/w) V^T b from the converged G = A V (lane j of the warp owns
+// column j); shared by both Jacobi variants.  ld: leading dimension of G, V.
+__device__ void pinv_apply(const double *G, const double *V, int ld, const double *b, double *x,
+                           int m, double scale) {
+    const int lane = threadIdx.x & 31;
+    double w = 0.0;
+    if (lane < m) {
+        for (int k = 0; k < m; k++) w = fma(G[k * ld + lane], G[k * ld + lane], w);
+        w = sqrt(w);
+    }
+    double wmax = lane < m ? w : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wmax = fmax(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+    const double wmin = m * wmax * kPinvEps;
+    double tj = 0.0;  // (V^T b)_j / w_j on lane j
+    if (lane < m && w >= wmin && w > 0.0) {
+        for (int i = 0; i < m; i++) tj = fma(V[i * ld + lane], b[i], tj);
+        tj /= w;
+    }
+    double xi = 0.0;
+    for (int j = 0; j < m; j++) {
+        const double t = __shfl_sync(0xffffffffu, tj, j);
+        if (lane < m) xi = fma(V[lane * ld + j], t, xi);
+    }
+    if (lane < m) x[lane] = xi * scale;
+}
+
+// General case, m <= 32: one warp, lane k owns row k, column pairs visited
+// cyclically with the rotation computed in FP64.  Returns 0 on convergence,
+// LSG_SVD_NO_CONVERGENCE otherwise.
 __device__ int warp_pinv(double *G, double *V, const double *b, double *x, int m) {
     const int lane = threadIdx.x & 31;
     for (int i = lane; i < m * m; i += 32) V[i] = (i / m == i % m) ? 1.0 : 0.0;
@@ -105,7 +137,7 @@ __device__ int warp_pinv(double *G, double *V, const double *b, double *x, int m
                     be += __shfl_xor_sync(0xffffffffu, be, o);
                     ga += __shfl_xor_sync(0xffffffffu, ga, o);
                 }
-                if (ga == 0.0 || fabs(ga) <= kPinvEps * sqrt(al * be)) continue;
+                if (ga == 0.0 || ga * ga <= kJacobiTol * kJacobiTol * al * be) continue;
                 rotated = true;
                 const double zeta = (be - al) / (2.0 * ga);
                 double t;
@@ -124,39 +156,120 @@ __device__ int warp_pinv(double *G, double *V, const double *b, double *x, int m
             }
         }
     }
-    // Singular values, cutoff and x = V diag(1/w) V^T b.
-    double w = 0.0;  // lane j holds w_j
-    for (int j = 0; j < m; j++) {
-        double g = lane < m ? G[lane * m + j] : 0.0;
-        g = g * g;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
-        if (lane == j) w = sqrt(g);
-    }
-    double wmax = lane < m ? w : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) wmax = fmax(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
-    const double wmin = m * wmax * kPinvEps;
-    // t_j = (V^T b)_j / w_j  (lane j)
-    double tj = 0.0;
-    if (lane < m && w >= wmin && w > 0.0) {
-        for (int i = 0; i < m; i++) tj += V[i * m + lane] * b[i];
-        tj /= w;
-    }
-    // x_i = sum_j V(i,j) t_j  (lane i)
-    double xi = 0.0;
-    for (int j = 0; j < m; j++) {
-        const double t = __shfl_sync(0xffffffffu, tj, j);
-        if (lane < m) xi += V[lane * m + j] * t;
-    }
-    if (lane < m) x[lane] = xi;
+    pinv_apply(G, V, m, b, x, m, 1.0);
     return rotated ? LSG_SVD_NO_CONVERGENCE : 0;
+}
+
+// Fast case, m <= 8: the columns (padded to an even count M2) are paired by
+// the round-robin ("circle") schedule, so each round rotates M2/2 disjoint
+// pairs at once; lane = 8*q + row works on pair q, row `row`.  G is scaled by
+// a power of two so its largest entry is O(1) (exact; undone at the end); the
+// rotation angle is then computed in FP32 and (c, s) re-normalised to
+// c^2 + s^2 = 1 in FP64 by two Newton steps, so each rotation stays exactly
+// orthogonal in FP64 while its angle is accurate to ~1e-7 -- a pair left
+// slightly non-orthogonal is finished by the next sweep.  Pairs whose FP32
+// angle would underflow use the FP64 formula.  G, V: 8 x 8, row-major, ld 8,
+// rows and columns >= m zero.
+__device__ int warp_pinv8(double *G, double *V, const double *b, double *x, int m) {
+    const int lane = threadIdx.x & 31;
+    const int q = lane >> 3, row = lane & 7;
+    const int M2 = m + (m & 1);
+    // power-of-two normalisation
+    double amax = 0.0;
+    for (int k = lane; k < 64; k += 32) amax = fmax(amax, fabs(G[k]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    int e = 0;
+    if (amax > 0.0) frexp(amax, &e);
+    for (int k = lane; k < 64; k += 32) {
+        G[k] = ldexp(G[k], -e);
+        V[k] = ((k >> 3) == (k & 7)) ? 1.0 : 0.0;
+    }
+    __syncwarp();
+    int sweep = 0;
+    bool any = true;
+    for (; sweep < kMaxSweeps && any; sweep++) {
+        bool rotated = false;
+        for (int r = 0; r < M2 - 1; r++) {
+            int i = -1, j = -1;
+            if (q < M2 / 2) {
+                const int pa = q, pb = M2 - 1 - q;
+                const int ca = pa == 0 ? 0 : 1 + (pa - 1 + r) % (M2 - 1);
+                const int cb = pb == 0 ? 0 : 1 + (pb - 1 + r) % (M2 - 1);
+                i = min(ca, cb);
+                j = max(ca, cb);
+            }
+            const bool active = i >= 0 && j < m;
+            double gi = 0.0, gj = 0.0, vi = 0.0, vj = 0.0;
+            if (active) {
+                gi = G[row * 8 + i]; gj = G[row * 8 + j];
+                vi = V[row * 8 + i]; vj = V[row * 8 + j];
+            }
+            double al = gi * gi, be = gj * gj, ga = gi * gj;
+#pragma unroll
+            for (int o = 1; o < 8; o <<= 1) {
+                al += __shfl_xor_sync(0xffffffffu, al, o);
+                be += __shfl_xor_sync(0xffffffffu, be, o);
+                ga += __shfl_xor_sync(0xffffffffu, ga, o);
+            }
+            if (active && ga != 0.0 && ga * ga > kJacobiTol * kJacobiTol * al * be) {
+                rotated = true;
+                double c, s;
+                const float num = (float)(be - al), den = (float)(2.0 * ga);
+                if (den != 0.0f) {
+                    const float z = num / den;
+                    const float az = fabsf(z);
+                    const float t = az < 1e18f ? copysignf(1.0f, z) / (az + sqrtf(1.0f + z * z)) : 0.5f / z;
+                    const float cf = rsqrtf(1.0f + t * t);
+                    c = (double)cf;
+                    s = (double)(cf * t);
+#pragma unroll
+                    for (int it = 0; it < 2; it++) {
+                        const double k = fma(-0.5, fma(c, c, s * s), 1.5);
+                        c *= k;
+                        s *= k;
+                    }
+                } else {
+                    const double zeta = (be - al) / (2.0 * ga);
+                    const double t = fabs(zeta) > 1e150 ? 0.5 / zeta
+                                   : (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                    c = 1.0 / sqrt(1.0 + t * t);
+                    s = c * t;
+                }
+                G[row * 8 + i] = c * gi - s * gj;
+                G[row * 8 + j] = s * gi + c * gj;
+                V[row * 8 + i] = c * vi - s * vj;
+                V[row * 8 + j] = s * vi + c * vj;
+            }
+            __syncwarp();
+        }
+        any = __any_sync(0xffffffffu, rotated);
+    }
+    pinv_apply(G, V, 8, b, x, m, ldexp(1.0, -e));
+    return any ? LSG_SVD_NO_CONVERGENCE : 0;
+}
+
+// Dispatch on m; G (m x m row-major) is overwritten.  Gs / Vs: 8 x 8 staging
+// for the fast path.  Called by one full warp.
+__device__ int warp_pinv_any(double *G, double *V, const double *b, double *x, int m, double *Gs,
+                             double *Vs) {
+    const int lane = threadIdx.x & 31;
+    if (m <= 8) {
+        for (int k = lane; k < 64; k += 32) {
+            const int r = k >> 3, c = k & 7;
+            Gs[k] = (r < m && c < m) ? G[r * m + c] : 0.0;
+        }
+        __syncwarp();
+        return warp_pinv8(Gs, Vs, b, x, m);
+    }
+    return warp_pinv(G, V, b, x, m);
 }
 
 __global__ void finalize_gram_solve_kernel(const double *partials, int nparts, int kind, int m,
                                            double hscale, DevCtrl *ctrl) {
     __shared__ double vals[LSG_MAX_M * LSG_MAX_M + LSG_MAX_M];
     __shared__ double G[LSG_MAX_M * LSG_MAX_M], V[LSG_MAX_M * LSG_MAX_M];
+    __shared__ double Gs[64], Vs[64];
     __shared__ double h[LSG_MAX_M], s[LSG_MAX_M];
     __shared__ int bad;
     if (ctrl_done(ctrl)) return;
@@ -194,7 +307,7 @@ __global__ void finalize_gram_solve_kernel(const double *partials, int nparts, i
         for (int j = threadIdx.x; j < m; j += 32) h[j] = vals[np + j] * hscale;
         __syncwarp();
         int st = 0;
-        if (!bad) st = warp_pinv(G, V, h, s, m);
+        if (!bad) st = warp_pinv_any(G, V, h, s, m, Gs, Vs);
         __syncwarp();
         if (threadIdx.x < m) ctrl->s[threadIdx.x] = bad ? 0.0 : s[threadIdx.x];
         if (threadIdx.x == 0) {
@@ -236,10 +349,11 @@ __global__ void finalize_cg_kernel(const double *partials, int nparts, DevCtrl *
 
 __global__ void pinv_kernel(const double *A, const double *b, double *x, int m, int *status) {
     __shared__ double G[LSG_MAX_M * LSG_MAX_M], V[LSG_MAX_M * LSG_MAX_M], h[LSG_MAX_M], s[LSG_MAX_M];
+    __shared__ double Gs[64], Vs[64];
     for (int i = threadIdx.x; i < m * m; i += 32) G[i] = A[i];
     for (int i = threadIdx.x; i < m; i += 32) h[i] = b[i];
     __syncwarp();
-    const int st = warp_pinv(G, V, h, s, m);
+    const int st = warp_pinv_any(G, V, h, s, m, Gs, Vs);
     __syncwarp();
     if (threadIdx.x < m) x[threadIdx.x] = s[threadIdx.x];
     if (threadIdx.x == 0 && status) *status = st;

@@ -24,6 +24,7 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "lsg_internal.cuh"
@@ -71,6 +72,15 @@ static int sm_count() {
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
     cache[dev] = sms;
     return sms;
+}
+
+// Resident stencil blocks on the device (one wave).
+template <typename T>
+static int stencil_slots(int sms) {
+    static int bpsm[2] = {0, 0};  // per element size, resolved on first use
+    int &v = bpsm[sizeof(T) == 8 ? 1 : 0];
+    if (v == 0) v = Kernels<T>::stencil_blocks_per_sm();
+    return sms * v;
 }
 
 // ---------------------------------------------------------------- work arrays
@@ -137,8 +147,8 @@ static int get_workspace(size_t es, long long n, int m, bool mixed, const Geom &
     if (ws->base) { *out = ws; return LSG_OK; }
     // Partials: stencil grids for this geometry plus the reduction grids.
     long long cap = partials_needed(n, m, sms);
-    cap = std::max(cap, stencil_blocks<double>(g, choose_lz<double>(g, sms)));
-    cap = std::max(cap, stencil_blocks<float>(g, choose_lz<float>(g, sms)));
+    cap = std::max(cap, stencil_blocks<double>(g, choose_lz<double>(g, stencil_slots<double>(sms))));
+    cap = std::max(cap, stencil_blocks<float>(g, choose_lz<float>(g, stencil_slots<float>(sms))));
     const size_t vec = align_up((size_t)n * es);
     size_t bytes = 0;
     const size_t o_xalt = bytes; bytes += vec;
@@ -399,7 +409,7 @@ int aar_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const 
     const int m = prm->m, p = prm->p, max_iter = prm->max_iter;
     const Weights<T> w = make_weights<T>(op);
     const double cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
-    const int lz = choose_lz<T>(g, R.sms);
+    const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
     const StencilLaunch L{g, lz, R.s};
     const int sb = (int)stencil_blocks<T>(g, lz);
     const int rb = reduce_blocks(n, R.sms);
@@ -419,34 +429,46 @@ int aar_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const 
     LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, R.s));
     LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, X[0], b, Rv[0], nullptr, cf, part, ctrl));
 
-    int cur = 0;
+    // FP64 follows the reference's true-residual form (x and r ping-pong);
+    // FP32 uses the residual recurrence (x in place, only r ping-pongs).
+    constexpr bool recur = std::is_same<T, float>::value;
+    int xc = 0, rc = 0;
     auto is_anderson = [p](int it) { return it % p == 0 && it > 1; };
     auto enqueue = [&](int it) -> int {
         const int col = (it - 1) % m;  // the reference writes this column at iteration it+1
+        T *dxc = DX + (size_t)col * n, *dfc = DF + (size_t)col * n;
         if (is_anderson(it)) {
-            LSG_KC(LSG_K_GRAM, Kernels<T>::gram(GRAM_SYM, m, DX, DF, Rv[cur], n, part, rb, ctrl, R.s));
+            LSG_KC(LSG_K_GRAM, Kernels<T>::gram(GRAM_SYM, m, DX, DF, Rv[rc], n, part, rb, ctrl, R.s));
             LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, rb, GRAM_SYM, m, cf, ctrl, R.s));
-            LSG_KC(LSG_K_UPDATE, Kernels<T>::aar_update(m, col, X[cur], Rv[cur], DX, DF, prm->beta, cf, n, ctrl, R.s));
-            LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_ANDERSON, X[cur], b, Rv[cur], DF + (size_t)col * n, cf, part, ctrl));
+            LSG_KC(LSG_K_UPDATE, Kernels<T>::aar_update(m, col, X[xc], Rv[rc], DX, DF, prm->beta, cf, n, ctrl, R.s));
+            if (recur)
+                LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual_recur(L, w, dxc, Rv[rc], dfc, cf, part, ctrl));
+            else
+                LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_ANDERSON, X[xc], b, Rv[rc], dfc, cf, part, ctrl));
             LSG_KC(LSG_K_SMALL, finalize_norm(part, sb, ctrl, NF_CHECK, prm->tol, it, R.s));
+        } else if (recur) {
+            LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson_recur(L, w, Rv[rc], X[0], Rv[rc ^ 1], dxc, dfc,
+                                                                  prm->omega * cf, cf, ctrl));
+            rc ^= 1;
         } else {
-            LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson(L, w, RICH_AAR, X[cur], Rv[cur], b, X[cur ^ 1], Rv[cur ^ 1],
-                                          DX + (size_t)col * n, DF + (size_t)col * n,
-                                          prm->omega * cf, cf, ctrl));
-            cur ^= 1;
+            LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson(L, w, RICH_AAR, X[xc], Rv[rc], b, X[xc ^ 1], Rv[rc ^ 1],
+                                                            dxc, dfc, prm->omega * cf, cf, ctrl));
+            xc ^= 1;
+            rc ^= 1;
         }
         return LSG_OK;
     };
-    int rc = pipelined_loop(R, ws, 1, max_iter, default_per_check(prm, n), enqueue, is_anderson);
-    if (rc != LSG_OK) return rc;
+    int rcode = pipelined_loop(R, ws, 1, max_iter, default_per_check(prm, n), enqueue, is_anderson);
+    if (rcode != LSG_OK) return rcode;
     DevCtrl c;
     LSG_CUDA(cudaMemcpy(&c, ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost));
-    // Where the last iterate lives: x moved to the other buffer at every
-    // Richardson iteration up to the final one.
+    // Where the last iterate lives: in the reference form x moved to the other
+    // buffer at every Richardson iteration up to the final one.
     const int last = c.done ? c.iters : max_iter;
     long long rich = last - last / p + (p == 1 && last >= 1 ? 1 : 0);
     if (last < 1) rich = 0;
-    if (rich & 1) LSG_CUDA(cudaMemcpyAsync(x, X[1], sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, R.s));
+    if (!recur && (rich & 1))
+        LSG_CUDA(cudaMemcpyAsync(x, X[1], sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, R.s));
     LSG_CUDA(cudaStreamSynchronize(R.s));
     *out = c;
     return LSG_OK;
@@ -461,7 +483,7 @@ int prich_core(Run &R, bool galerkin, const lsg_operator *op, const lsg_params *
     const int m = prm->m, p = prm->p, max_iter = prm->max_iter;
     const Weights<T> w = make_weights<T>(op);
     const double cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
-    const int lz = choose_lz<T>(g, R.sms);
+    const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
     const StencilLaunch L{g, lz, R.s};
     const int rb = reduce_blocks(n, R.sms);
     T *X[2] = {x, (T *)ws->xalt};
@@ -515,7 +537,7 @@ int cg_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const T
     const int max_iter = prm->max_iter;
     const Weights<T> w = make_weights<T>(op);
     const double cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
-    const int lz = choose_lz<T>(g, R.sms);
+    const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
     const StencilLaunch L{g, lz, R.s};
     const int sb = (int)stencil_blocks<T>(g, lz);
     const int rb = reduce_blocks(n, R.sms);
@@ -623,7 +645,7 @@ int solve_mixed(const lsg_operator *op, const lsg_params *prm, double *x, const 
     if (rc) return rc;
     Run R(s, sm_count());
     const Weights<double> w = make_weights<double>(op);
-    const int lz = choose_lz<double>(g, R.sms);
+    const int lz = choose_lz<double>(g, stencil_slots<double>(R.sms));
     const StencilLaunch L{g, lz, s};
     const int sb = (int)stencil_blocks<double>(g, lz);
     const int rb = reduce_blocks(n, R.sms);
@@ -686,11 +708,11 @@ int apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, cudaStr
     const Geom g = make_geom(op->n);
     const int sms = sm_count();
     if (dtype == LSG_F64) {
-        const StencilLaunch L{g, choose_lz<double>(g, sms), s};
+        const StencilLaunch L{g, choose_lz<double>(g, stencil_slots<double>(sms)), s};
         LSG_CUDA(Kernels<double>::residual(L, make_weights<double>(op), RES_APPLY, (const double *)d_x,
                                            nullptr, (double *)d_y, nullptr, 1.0, nullptr, nullptr));
     } else if (dtype == LSG_F32) {
-        const StencilLaunch L{g, choose_lz<float>(g, sms), s};
+        const StencilLaunch L{g, choose_lz<float>(g, stencil_slots<float>(sms)), s};
         LSG_CUDA(Kernels<float>::residual(L, make_weights<float>(op), RES_APPLY, (const float *)d_x,
                                           nullptr, (float *)d_y, nullptr, 1.0, nullptr, nullptr));
     } else {

@@ -2,24 +2,29 @@
 //
 // Replaces the sequential operator of MPI_REAL/system.c:189-204 (and the MPI
 // halo exchange of :106-188, which one GPU does not need): each thread block
-// owns a TX x TY column tile of the xy plane and a range of lz planes along z.
+// owns a 32 x TY column tile of the xy plane and a range of lz planes along z.
 // For every plane it
 //   * keeps, per owned column, the 2R+1 values u(z-R .. z+R) in a register
 //     queue (one new plane value loaded per step: the z neighbours),
 //   * stages plane z with an R-wide xy halo in shared memory (the interior
-//     from the queue centre, the halo from global memory with the periodic
-//     wrap applied to the xy coordinates once, before the march), and
-//   * evaluates  Au = w0 u_c + sum_p w_p ((u_x-p + u_x+p) + (u_y-p + u_y+p) + (u_z-p + u_z+p)).
-// The "value" u at a grid point and what happens to Au at the centre are
-// supplied by a functor, so one driver serves the residual, the fused
-// Richardson step, the CG direction update and the FP64 refinement residual.
+//     from the queue centre, the halo from global memory; the periodic wrap
+//     of the xy coordinates is computed once, before the march),
+//   * evaluates Au = w0 u_c + sum_p w_p ((u_x-p + u_x+p) + (u_y-p + u_y+p) + (u_z-p + u_z+p)),
+// while the global loads of plane z+1 (queue head, halo, centre operands) are
+// already in flight.  The shared plane is double-buffered, so one barrier per
+// plane suffices.
 //
+// The value u at a grid point and what happens to Au at the centre are
+// supplied by a functor, so one driver serves every stencil pass.
 // Functor interface (all __device__):
-//   void init()                               read device scalars (once per thread)
-//   T    load(long long idx) const            u at flat index idx
-//   void store(long long idx, T u, T Au, Acc<T> *acc) const   epilogue at a valid centre
-//   static constexpr int NACC                 per-thread accumulators (FP64-class) reduced per block
-//   double *partials                          where the block writes NACC sums (if NACC > 0)
+//   bool skip() const                     the solve has finished: return at once
+//   void init()                           read device scalars (once per thread)
+//   Raw  fetch(long long idx) const       global loads for u at idx
+//   T    value(const Raw &) const         u from the fetched operands
+//   Ctr  fetch_center(long long idx) const  operands the epilogue needs at a centre
+//   void store(long long idx, T u, T Au, const Ctr &, Acc<T> *acc) const
+//   static constexpr int NACC             per-thread accumulators reduced per block
+//   double *partials                      where the block writes NACC sums
 #pragma once
 
 #include "lsg_internal.cuh"
@@ -30,15 +35,18 @@ namespace lsg {
 template <typename T>
 __device__ __forceinline__ T ldg(const T *p) { return __ldg(p); }
 
+struct NoCtr {};
+
 // RQ: radius the storage is sized for; the arithmetic uses `radius` (== RQ on
 // the specialised path, <= RQ on the generic path).
 template <typename T, int RQ, int BY, int NY, bool GENERIC, class Op>
 __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w, int lz, Op &op,
-                                              T *smem) {
+                                              T *smem0, T *smem1) {
+    using Raw = typename Op::Raw;
+    using Ctr = typename Op::Ctr;
     constexpr int TX = 32;
     constexpr int TY = BY * NY;
     constexpr int FX = TX + 2 * RQ;
-    constexpr int FY = TY + 2 * RQ;
     constexpr int NT = 32 * BY;
     constexpr int H = 2 * RQ * FX + TY * 2 * RQ;  // halo cells of one plane
     constexpr int NH = (H + NT - 1) / NT;
@@ -97,36 +105,57 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
     for (int s = 0; s < 2 * RQ; s++) {
         const long long base = (long long)zl * g.nxy;
 #pragma unroll
-        for (int k = 0; k < NY; k++) q[k][s + 1] = op.load(base + col[k]);
+        for (int k = 0; k < NY; k++) q[k][s + 1] = op.value(op.fetch(base + col[k]));
+        zl = (zl + 1 == g.nz) ? 0 : zl + 1;
+    }
+    // In flight for the next plane: queue head (plane z+RQ), halo and centres (plane z).
+    Raw qn[NY], hn[NH];
+    Ctr cn[NY];
+    {
+        const long long lb = (long long)zl * g.nxy, zb = (long long)z0 * g.nxy;
+#pragma unroll
+        for (int k = 0; k < NY; k++) {
+            qn[k] = op.fetch(lb + col[k]);
+            cn[k] = op.fetch_center(zb + col[k]);
+        }
+#pragma unroll
+        for (int s = 0; s < NH; s++)
+            if (hs[s] >= 0) hn[s] = op.fetch(zb + ho[s]);
         zl = (zl + 1 == g.nz) ? 0 : zl + 1;
     }
 
+    T *sm = smem0;
     for (int z = z0; z < z1; z++) {
         const long long zbase = (long long)z * g.nxy;
-        const long long lbase = (long long)zl * g.nxy;
 #pragma unroll
         for (int k = 0; k < NY; k++) {
 #pragma unroll
             for (int s = 0; s < Q - 1; s++) q[k][s] = q[k][s + 1];
-            q[k][Q - 1] = op.load(lbase + col[k]);
+            q[k][Q - 1] = op.value(qn[k]);
+            sm[(RQ + ty + BY * k) * FX + RQ + tx] = q[k][RQ];
         }
-        zl = (zl + 1 == g.nz) ? 0 : zl + 1;
-
-        T hv[NH];
-#pragma unroll
-        for (int s = 0; s < NH; s++) hv[s] = hs[s] >= 0 ? op.load(zbase + ho[s]) : T(0);
-
-        __syncthreads();  // previous plane fully consumed
-#pragma unroll
-        for (int k = 0; k < NY; k++) smem[(RQ + ty + BY * k) * FX + RQ + tx] = q[k][RQ];
 #pragma unroll
         for (int s = 0; s < NH; s++)
-            if (hs[s] >= 0) smem[hs[s]] = hv[s];
-        __syncthreads();
-
+            if (hs[s] >= 0) sm[hs[s]] = op.value(hn[s]);
+        Ctr cc[NY];
+#pragma unroll
+        for (int k = 0; k < NY; k++) cc[k] = cn[k];
+        if (z + 1 < z1) {  // issue plane z+1's loads before computing plane z
+            const long long lb = (long long)zl * g.nxy, nb = zbase + g.nxy;
+#pragma unroll
+            for (int k = 0; k < NY; k++) {
+                qn[k] = op.fetch(lb + col[k]);
+                cn[k] = op.fetch_center(nb + col[k]);
+            }
+#pragma unroll
+            for (int s = 0; s < NH; s++)
+                if (hs[s] >= 0) hn[s] = op.fetch(nb + ho[s]);
+            zl = (zl + 1 == g.nz) ? 0 : zl + 1;
+        }
+        __syncthreads();  // plane z staged (the other buffer is still being read by no one)
 #pragma unroll
         for (int k = 0; k < NY; k++) {
-            const T *row = smem + (RQ + ty + BY * k) * FX + RQ + tx;
+            const T *row = sm + (RQ + ty + BY * k) * FX + RQ + tx;
             T au = w.w[0] * q[k][RQ];
 #pragma unroll
             for (int p = 1; p <= RQ; p++) {
@@ -135,8 +164,9 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
                 const T sz = q[k][RQ - p] + q[k][RQ + p];
                 au = fma(w.w[p], sxy + sz, au);
             }
-            if (valid[k]) op.store(zbase + col[k], q[k][RQ], au, acc);
+            if (valid[k]) op.store(zbase + col[k], q[k][RQ], au, cc[k], acc);
         }
+        sm = (sm == smem0) ? smem1 : smem0;
     }
 
     if (Op::NACC > 0) {
@@ -150,21 +180,14 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
     }
 }
 
-template <typename T, int RQ, int BY, int NY, bool GENERIC, class Op>
-__global__ void __launch_bounds__(32 * BY) stencil_kernel(Geom g, Weights<T> w, int lz, Op op) {
+template <typename T, int RQ, int BY, int NY, int MINB, bool GENERIC, class Op>
+__global__ void __launch_bounds__(32 * BY, MINB) stencil_kernel(Geom g, Weights<T> w, int lz, Op op) {
     constexpr int FX = 32 + 2 * RQ;
     constexpr int FY = BY * NY + 2 * RQ;
-    __shared__ T smem[FX * FY];
-    if (op.skip()) {
-        // Solve already finished: keep the block's partials well defined.
-        if (Op::NACC > 0 && threadIdx.x == 0 && threadIdx.y == 0) {
-            const long long blk = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
-            for (int a = 0; a < Op::NACC; a++) op.partials[blk * Op::NACC + a] = 0.0;
-        }
-        return;
-    }
+    __shared__ T smem[2][FX * FY];
+    if (op.skip()) return;
     op.init();
-    stencil_march<T, RQ, BY, NY, GENERIC>(g, w, lz, op, smem);
+    stencil_march<T, RQ, BY, NY, GENERIC>(g, w, lz, op, smem[0], smem[1]);
 }
 
 }  // namespace lsg
