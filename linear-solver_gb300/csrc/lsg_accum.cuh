@@ -50,4 +50,62 @@ struct Acc<float> {
     __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
 };
 
+// Warp-wide sum of double-float pairs (FP32 instructions only).
+__device__ __forceinline__ void df_warp_sum(float &hi, float &lo) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+        const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+        float s, e;
+        two_sum(hi, h2, s, e);
+        hi = s;
+        lo += l2 + e;
+    }
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sums NV per-thread accumulators over the block and writes the NV totals
+// (FP64) to out[0..NV).  `scratch` is NV * 32 doubles of shared memory.
+// FP32 accumulators are reduced as double-float pairs with FP32 instructions;
+// only the NV final conversions to double touch the (slow) FP64 pipe.
+template <int NV, typename T>
+__device__ __forceinline__ void block_reduce_store(Acc<T> (&acc)[NV], double *scratch, double *out) {
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int nwarps = (blockDim.x * blockDim.y) >> 5;
+    if constexpr (sizeof(T) == 8) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            const double s = warp_sum_d(acc[k].get());
+            if (lane == 0) scratch[k * nwarps + warp] = s;
+        }
+        __syncthreads();
+        for (int k = warp; k < NV; k += nwarps) {
+            double s = lane < nwarps ? scratch[k * nwarps + lane] : 0.0;
+            s = warp_sum_d(s);
+            if (lane == 0) out[k] = s;
+        }
+    } else {
+        float2 *sf = reinterpret_cast<float2 *>(scratch);
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            float hi = acc[k].hi, lo = acc[k].lo;
+            df_warp_sum(hi, lo);
+            if (lane == 0) sf[k * nwarps + warp] = make_float2(hi, lo);
+        }
+        __syncthreads();
+        for (int k = warp; k < NV; k += nwarps) {
+            float hi = 0.f, lo = 0.f;
+            if (lane < nwarps) { const float2 v = sf[k * nwarps + lane]; hi = v.x; lo = v.y; }
+            df_warp_sum(hi, lo);
+            if (lane == 0) out[k] = (double)hi + (double)lo;
+        }
+    }
+}
+
 }  // namespace lsg

@@ -131,7 +131,7 @@ struct StencilLaunch {
 // A block is 32 x BY threads covering 32 x (BY*NY) columns.
 template <typename T> struct TileOf;
 template <> struct TileOf<double> { static constexpr int BY = 8, NY = 2, MINB = 1; };
-template <> struct TileOf<float> { static constexpr int BY = 8, NY = 2, MINB = 3; };
+template <> struct TileOf<float> { static constexpr int BY = 4, NY = 4, MINB = 4; };
 
 inline dim3 stencil_grid(const Geom &g, int ty, int lz) {
     return dim3((unsigned)((g.nx + 31) / 32), (unsigned)((g.ny + ty - 1) / ty),
@@ -165,32 +165,35 @@ template <typename T>
 struct Kernels {
     // Resident blocks per SM of the fused Richardson stencil kernel.
     static int stencil_blocks_per_sm();
-    // y / r update driven by one stencil pass over x.
+    // y / r update driven by one stencil pass over x.  RES_ANDERSON also
+    // completes the history column hc (holding x_new - x_old) with hb * DF_col.
     static cudaError_t residual(const StencilLaunch &L, const Weights<T> &w, int mode,
-                                const T *x, const T *b, T *r, T *df, double cf,
+                                const T *x, const T *b, T *r, T *df, T *hc, double cf, double hb,
                                 double *partials, const DevCtrl *ctrl);
     // Fused Richardson step: u = x + c*r at every stencil point; r2 = b - A u;
-    // x2 = u; DX = u - x; DF per mode.
+    // x2 = u; DF per mode; history column dx = (u - x) + hb * DF.
     static cudaError_t richardson(const StencilLaunch &L, const Weights<T> &w, int mode,
                                   const T *x, const T *r, const T *b, T *x2, T *r2, T *dx,
-                                  T *df, double c, double cf, const DevCtrl *ctrl);
+                                  T *df, double c, double cf, double hb, const DevCtrl *ctrl);
     // Residual-recurrence Richardson step (FP32 inner solver): r2 = r - c A r,
-    // x += c r in place, DX = x_new - x_old, DF = (r2 - r) cf.
+    // x += c r in place, DF = (r2 - r) cf, H = (x_new - x_old) + hb DF.
     static cudaError_t richardson_recur(const StencilLaunch &L, const Weights<T> &w, const T *r,
                                         T *x, T *r2, T *dx, T *df, double c, double cf,
-                                        const DevCtrl *ctrl);
-    // Extrapolation-step residual by recurrence: r -= A dxc; DF = (r_new - r) cf; ||r||^2.
-    static cudaError_t residual_recur(const StencilLaunch &L, const Weights<T> &w, const T *dxc,
-                                      T *r, T *df, double cf, double *partials,
-                                      const DevCtrl *ctrl);
+                                        double hb, const DevCtrl *ctrl);
+    // Extrapolation-step residual by recurrence: r -= A step; DF = (r_new - r) cf;
+    // H_col = step + hb DF; ||r||^2.
+    static cudaError_t residual_recur(const StencilLaunch &L, const Weights<T> &w, const T *step,
+                                      T *r, T *df, T *hc, double cf, double hb,
+                                      double *partials, const DevCtrl *ctrl);
+    // Grid of one Gram launch (one wave); partials written = grid * values.
+    static int gram_grid(int kind, int m, long long n, int sms);
     // Gram partials over the history (point-local, grid-stride).
     static cudaError_t gram(int kind, int m, const T *dx, const T *df, const T *r, long long n,
                             double *partials, int blocks, const DevCtrl *ctrl, cudaStream_t s);
-    // AAR extrapolation: x += beta*f - sum_j (DX_j + beta DF_j) s_j with f = r*cf;
-    // DX_col = x_new - x_old.
-    static cudaError_t aar_update(int m, int col, T *x, const T *r, T *dx, const T *df,
-                                  double beta, double cf, long long n, const DevCtrl *ctrl,
-                                  cudaStream_t s);
+    // AAR extrapolation: x += beta*f - sum_j H_j s_j with f = r*cf and
+    // H_j = DX_j + beta DF_j; step = x_new - x_old.
+    static cudaError_t aar_update(int m, T *x, const T *r, const T *h, T *step, double beta,
+                                  double cf, long long n, const DevCtrl *ctrl, cudaStream_t s);
     // PGR/PL2R projection: tx = DX s, tf = DF s; x += tx; r -= tf; DX_col += tx;
     // DF_col += tf; partial ||r||^2.
     static cudaError_t proj_update(int m, int col, T *x, T *r, T *dx, T *df, long long n,

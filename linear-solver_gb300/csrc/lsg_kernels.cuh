@@ -29,30 +29,34 @@ template <typename T> struct Pair { T a, b; };
 template <typename T> struct Triple { T a, b, c; };
 
 // r = b - A x (RES_INIT, with ||r||^2), the AAR extrapolation residual
-// (RES_ANDERSON: also DF_col = (r_new - r) * cf, r in place), or y = A x.
+// (RES_ANDERSON: also DF_col = (r_new - r) cf, r in place, and the history
+// column H_col, which holds the step x_new - x_old, completed to
+// x_new - x_old + beta DF_col), or y = A x.
 template <typename T, int MODE>
 struct ResidualOp {
     static constexpr int NACC = (MODE == RES_APPLY) ? 0 : 1;
     using Raw = T;
-    using Ctr = typename std::conditional<MODE == RES_ANDERSON, Pair<T>,
+    using Ctr = typename std::conditional<MODE == RES_ANDERSON, Triple<T>,
                 typename std::conditional<MODE == RES_INIT, T, NoCtr>::type>::type;
     const T *x;
     const T *b;
     T *r;
     T *df;
+    T *hc;
     T cf;
+    T hb;
     double *partials;
     const DevCtrl *ctrl;
     __device__ bool skip() const { return solve_done(ctrl); }
     __device__ void init() {}
-    __device__ __forceinline__ Raw fetch(long long i) const { return ldg(x + i); }
+    __device__ __forceinline__ Raw fetch(unsigned i) const { return ldg(x + i); }
     __device__ __forceinline__ T value(const Raw &v) const { return v; }
-    __device__ __forceinline__ Ctr fetch_center(long long i) const {
-        if constexpr (MODE == RES_ANDERSON) return Ctr{ldg(b + i), r[i]};
+    __device__ __forceinline__ Ctr fetch_center(unsigned i) const {
+        if constexpr (MODE == RES_ANDERSON) return Ctr{ldg(b + i), r[i], hc[i]};
         else if constexpr (MODE == RES_INIT) return ldg(b + i);
         else return Ctr{};
     }
-    __device__ __forceinline__ void store(long long i, T u, T au, const Ctr &c, Acc<T> *acc) const {
+    __device__ __forceinline__ void store(unsigned i, T u, T au, const Ctr &c, Acc<T> *acc) const {
         if constexpr (MODE == RES_APPLY) {
             r[i] = au;
         } else if constexpr (MODE == RES_INIT) {
@@ -61,7 +65,9 @@ struct ResidualOp {
             acc[0].add_prod(rn, rn);
         } else {
             const T rn = c.a - au;
-            df[i] = (rn - c.b) * cf;
+            const T dfv = (rn - c.b) * cf;
+            df[i] = dfv;
+            hc[i] = fma(hb, dfv, c.c);
             r[i] = rn;
             acc[0].add_prod(rn, rn);
         }
@@ -70,7 +76,10 @@ struct ResidualOp {
 
 // Fused Richardson step in the reference's form (AAR.c:93-107,134-139;
 // PGR.c:92-109): u = x + omega*cf*r at every stencil point, r2 = b - A u,
-// x2 = u, DX = u - x, DF = (r2 - r) cf (AAR) or r - r2 (PGR / PL2R).
+// x2 = u, DF = (r2 - r) cf (AAR) or r - r2 (PGR / PL2R), and the history
+// column dx = (u - x) + hb DF.  AAR only ever uses DX_j + beta DF_j
+// (AAR.c:228), so it stores that combination (hb = beta); PGR / PL2R store
+// DX itself (hb = 0).
 template <typename T, int MODE>
 struct RichOp {
     static constexpr int NACC = 0;
@@ -85,27 +94,29 @@ struct RichOp {
     T *df;
     T c;   // omega * cf
     T cf;  // 1/diag (or 1 without preconditioning)
+    T hb;  // beta (AAR) or 0
     double *partials;
     const DevCtrl *ctrl;
     __device__ bool skip() const { return solve_done(ctrl); }
     __device__ void init() {}
-    __device__ __forceinline__ Raw fetch(long long i) const { return Raw{ldg(x + i), ldg(r + i)}; }
+    __device__ __forceinline__ Raw fetch(unsigned i) const { return Raw{ldg(x + i), ldg(r + i)}; }
     __device__ __forceinline__ T value(const Raw &v) const { return fma(c, v.b, v.a); }
-    __device__ __forceinline__ Ctr fetch_center(long long i) const {
+    __device__ __forceinline__ Ctr fetch_center(unsigned i) const {
         return Ctr{ldg(b + i), ldg(x + i), ldg(r + i)};
     }
-    __device__ __forceinline__ void store(long long i, T u, T au, const Ctr &cc, Acc<T> *) const {
+    __device__ __forceinline__ void store(unsigned i, T u, T au, const Ctr &cc, Acc<T> *) const {
         const T rn = cc.a - au;
+        const T dfv = (MODE == RICH_AAR) ? (rn - cc.c) * cf : (cc.c - rn);
         x2[i] = u;
         r2[i] = rn;
-        dx[i] = u - cc.b;
-        df[i] = (MODE == RICH_AAR) ? (rn - cc.c) * cf : (cc.c - rn);
+        dx[i] = fma(hb, dfv, u - cc.b);
+        df[i] = dfv;
     }
 };
 
 // Richardson step of the FP32 inner solver in residual-recurrence form:
-// f = cf r, r2 = r - omega A f, x += omega f (in place), DX = x_new - x,
-// DF = (r2 - r) cf.  Equal in exact arithmetic to the form above; it stages
+// f = cf r, r2 = r - omega A f, x += omega f (in place), DF = (r2 - r) cf,
+// history column H = (x_new - x) + beta DF.  Equal in exact arithmetic to the form above; it stages
 // one array (r) instead of two and never reads b, and its rounding is
 // relative to |r| rather than to |x|.
 template <typename T>
@@ -120,26 +131,28 @@ struct RichRecurOp {
     T *df;
     T c;    // omega * cf
     T cf;
+    T hb;   // beta
     double *partials;
     const DevCtrl *ctrl;
     __device__ bool skip() const { return solve_done(ctrl); }
     __device__ void init() {}
-    __device__ __forceinline__ Raw fetch(long long i) const { return ldg(r + i); }
+    __device__ __forceinline__ Raw fetch(unsigned i) const { return ldg(r + i); }
     __device__ __forceinline__ T value(const Raw &v) const { return v; }
-    __device__ __forceinline__ Ctr fetch_center(long long i) const { return x[i]; }
-    __device__ __forceinline__ void store(long long i, T rc, T ar, const Ctr &xo, Acc<T> *) const {
+    __device__ __forceinline__ Ctr fetch_center(unsigned i) const { return x[i]; }
+    __device__ __forceinline__ void store(unsigned i, T rc, T ar, const Ctr &xo, Acc<T> *) const {
         const T rn = fma(-c, ar, rc);
         const T xn = fma(c, rc, xo);
+        const T dfv = (rn - rc) * cf;
         x[i] = xn;
         r2[i] = rn;
-        dx[i] = xn - xo;
-        df[i] = (rn - rc) * cf;
+        dx[i] = fma(hb, dfv, xn - xo);
+        df[i] = dfv;
     }
 };
 
 // Extrapolation-step residual of the FP32 inner solver: the update kernel
-// leaves the step dx_col = x_new - x_old, so r_new = r - A dx_col (r in
-// place), DF_col = (r_new - r) cf, ||r_new||^2.
+// leaves the step s = x_new - x_old in a scratch vector, so r_new = r - A s
+// (r in place), DF_col = (r_new - r) cf, H_col = s + beta DF_col, ||r_new||^2.
 template <typename T>
 struct ResRecurOp {
     static constexpr int NACC = 1;
@@ -148,17 +161,21 @@ struct ResRecurOp {
     const T *dxc;
     T *r;
     T *df;
+    T *hc;
     T cf;
+    T hb;
     double *partials;
     const DevCtrl *ctrl;
     __device__ bool skip() const { return solve_done(ctrl); }
     __device__ void init() {}
-    __device__ __forceinline__ Raw fetch(long long i) const { return ldg(dxc + i); }
+    __device__ __forceinline__ Raw fetch(unsigned i) const { return ldg(dxc + i); }
     __device__ __forceinline__ T value(const Raw &v) const { return v; }
-    __device__ __forceinline__ Ctr fetch_center(long long i) const { return r[i]; }
-    __device__ __forceinline__ void store(long long i, T, T au, const Ctr &ro, Acc<T> *acc) const {
+    __device__ __forceinline__ Ctr fetch_center(unsigned i) const { return r[i]; }
+    __device__ __forceinline__ void store(unsigned i, T step, T au, const Ctr &ro, Acc<T> *acc) const {
         const T rn = ro - au;
-        df[i] = (rn - ro) * cf;
+        const T dfv = (rn - ro) * cf;
+        df[i] = dfv;
+        hc[i] = fma(hb, dfv, step);
         r[i] = rn;
         acc[0].add_prod(rn, rn);
     }
@@ -180,10 +197,10 @@ struct CgDirOp {
     const DevCtrl *ctrl;
     __device__ bool skip() const { return solve_done(ctrl); }
     __device__ void init() { beta = (T)ctrl->beta; }
-    __device__ __forceinline__ Raw fetch(long long i) const { return Raw{ldg(r + i), ldg(d_old + i)}; }
+    __device__ __forceinline__ Raw fetch(unsigned i) const { return Raw{ldg(r + i), ldg(d_old + i)}; }
     __device__ __forceinline__ T value(const Raw &v) const { return fma(beta, v.b, cf * v.a); }
-    __device__ __forceinline__ Ctr fetch_center(long long) const { return Ctr{}; }
-    __device__ __forceinline__ void store(long long i, T u, T au, const Ctr &, Acc<T> *acc) const {
+    __device__ __forceinline__ Ctr fetch_center(unsigned) const { return Ctr{}; }
+    __device__ __forceinline__ void store(unsigned i, T u, T au, const Ctr &, Acc<T> *acc) const {
         d_new[i] = u;
         q[i] = au;
         acc[0].add_prod(u, au);
@@ -202,10 +219,10 @@ struct IrResidualOp {
     const DevCtrl *ctrl;
     __device__ bool skip() const { return solve_done(ctrl); }
     __device__ void init() {}
-    __device__ __forceinline__ Raw fetch(long long i) const { return ldg(x + i); }
+    __device__ __forceinline__ Raw fetch(unsigned i) const { return ldg(x + i); }
     __device__ __forceinline__ double value(const Raw &v) const { return v; }
-    __device__ __forceinline__ Ctr fetch_center(long long i) const { return ldg(b + i); }
-    __device__ __forceinline__ void store(long long i, double, double au, const Ctr &bb,
+    __device__ __forceinline__ Ctr fetch_center(unsigned i) const { return ldg(b + i); }
+    __device__ __forceinline__ void store(unsigned i, double, double au, const Ctr &bb,
                                           Acc<double> *acc) const {
         const double rn = bb - au;
         r32[i] = (float)rn;
@@ -315,10 +332,7 @@ __global__ void __launch_bounds__(kReduceThreads) gram_kernel(const T *__restric
             for (int j = 0; j < M; j++) accv(acc[NP + j], xv[j], rv);
         }
     }
-    double v[NV];
-#pragma unroll
-    for (int q = 0; q < NV; q++) v[q] = acc[q].get();
-    block_sum_store<NV>(v, red, partials + (long long)blockIdx.x * NV);
+    block_reduce_store<NV, T>(acc, red, partials + (long long)blockIdx.x * NV);
 }
 
 // Generic Gram (any m <= LSG_MAX_M): one value per (block, thread-slot), the
@@ -355,19 +369,21 @@ __global__ void __launch_bounds__(kReduceThreads) gram_generic_kernel(int kind, 
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
         acc.add_prod(ldg(u + i), ldg(w + i));
-    double s[1] = {acc.get()};
-    double out;
-    block_sum_store<1>(s, red, &out);
+    __shared__ double out;
+    Acc<T> a1[1] = {acc};
+    block_reduce_store<1, T>(a1, red, &out);
+    __syncthreads();
     if (threadIdx.x == 0) partials[(long long)blockIdx.x * nv + v] = out;
 }
 
+// x_new = x + beta cf r - sum_j H_j s_j with H_j = DX_j + beta DF_j
+// (AAR.c:116-117, 225-231); the step x_new - x_old goes to `step`.
 template <typename T>
 __global__ void __launch_bounds__(kReduceThreads) aar_update_kernel(int m, T *__restrict__ x,
                                                                     const T *__restrict__ r,
-                                                                    T *__restrict__ dx,
-                                                                    const T *__restrict__ df,
-                                                                    int col, T beta, T cf,
-                                                                    long long n,
+                                                                    const T *__restrict__ h,
+                                                                    T *__restrict__ step, T beta,
+                                                                    T cf, long long n,
                                                                     const DevCtrl *ctrl) {
     __shared__ T s[LSG_MAX_M];
     if (solve_done(ctrl)) return;
@@ -376,11 +392,11 @@ __global__ void __launch_bounds__(kReduceThreads) aar_update_kernel(int m, T *__
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         T am = T(0);
-        for (int j = 0; j < m; j++) am = fma(fma(beta, ldg(df + j * n + i), ldg(dx + j * n + i)), s[j], am);
+        for (int j = 0; j < m; j++) am = fma(ldg(h + j * n + i), s[j], am);
         const T xo = x[i];
         const T xn = fma(beta, r[i] * cf, xo) - am;
         x[i] = xn;
-        dx[(long long)col * n + i] = xn - xo;
+        step[i] = xn - xo;
     }
 }
 
@@ -413,8 +429,8 @@ __global__ void __launch_bounds__(kReduceThreads) proj_update_kernel(int m, T *_
         df[(long long)col * n + i] += tf;
         acc.add_prod(rn, rn);
     }
-    double v[1] = {acc.get()};
-    block_sum_store<1>(v, red, partials + blockIdx.x);
+    Acc<T> a1[1] = {acc};
+    block_reduce_store<1, T>(a1, red, partials + blockIdx.x);
 }
 
 template <typename T>
@@ -440,8 +456,8 @@ __global__ void __launch_bounds__(kReduceThreads) cg_step_kernel(T *__restrict__
         }
     }
     if (!restart) {
-        double v[1] = {acc.get()};
-        block_sum_store<1>(v, red, partials + blockIdx.x);
+        Acc<T> a1[1] = {acc};
+        block_reduce_store<1, T>(a1, red, partials + blockIdx.x);
     }
 }
 
@@ -458,8 +474,8 @@ __global__ void __launch_bounds__(kReduceThreads) norm2_kernel(const T *__restri
         const T a = ldg(v + i);
         acc.add_prod(a, a);
     }
-    double s[1] = {acc.get()};
-    block_sum_store<1>(s, red, partials + blockIdx.x);
+    Acc<T> a1[1] = {acc};
+    block_reduce_store<1, T>(a1, red, partials + blockIdx.x);
 }
 
 template <typename T>
@@ -473,19 +489,19 @@ __global__ void axpy_kernel(T *__restrict__ x, const T *__restrict__ y, T alpha,
 
 template <typename T>
 cudaError_t Kernels<T>::residual(const StencilLaunch &L, const Weights<T> &w, int mode,
-                                 const T *x, const T *b, T *r, T *df, double cf,
+                                 const T *x, const T *b, T *r, T *df, T *hc, double cf, double hb,
                                  double *partials, const DevCtrl *ctrl) {
     switch (mode) {
     case RES_INIT: {
-        ResidualOp<T, RES_INIT> op{x, b, r, df, (T)cf, partials, ctrl};
+        ResidualOp<T, RES_INIT> op{x, b, r, df, nullptr, (T)cf, T(0), partials, ctrl};
         return launch_stencil<T>(L, w, op);
     }
     case RES_ANDERSON: {
-        ResidualOp<T, RES_ANDERSON> op{x, b, r, df, (T)cf, partials, ctrl};
+        ResidualOp<T, RES_ANDERSON> op{x, b, r, df, hc, (T)cf, (T)hb, partials, ctrl};
         return launch_stencil<T>(L, w, op);
     }
     default: {
-        ResidualOp<T, RES_APPLY> op{x, b, r, df, (T)cf, partials, ctrl};
+        ResidualOp<T, RES_APPLY> op{x, b, r, df, nullptr, (T)cf, T(0), partials, ctrl};
         return launch_stencil<T>(L, w, op);
     }
     }
@@ -494,28 +510,28 @@ cudaError_t Kernels<T>::residual(const StencilLaunch &L, const Weights<T> &w, in
 template <typename T>
 cudaError_t Kernels<T>::richardson(const StencilLaunch &L, const Weights<T> &w, int mode,
                                    const T *x, const T *r, const T *b, T *x2, T *r2, T *dx,
-                                   T *df, double c, double cf, const DevCtrl *ctrl) {
+                                   T *df, double c, double cf, double hb, const DevCtrl *ctrl) {
     if (mode == RICH_AAR) {
-        RichOp<T, RICH_AAR> op{x, r, b, x2, r2, dx, df, (T)c, (T)cf, nullptr, ctrl};
+        RichOp<T, RICH_AAR> op{x, r, b, x2, r2, dx, df, (T)c, (T)cf, (T)hb, nullptr, ctrl};
         return launch_stencil<T>(L, w, op);
     }
-    RichOp<T, RICH_PGR> op{x, r, b, x2, r2, dx, df, (T)c, (T)cf, nullptr, ctrl};
+    RichOp<T, RICH_PGR> op{x, r, b, x2, r2, dx, df, (T)c, (T)cf, T(0), nullptr, ctrl};
     return launch_stencil<T>(L, w, op);
 }
 
 template <typename T>
 cudaError_t Kernels<T>::richardson_recur(const StencilLaunch &L, const Weights<T> &w, const T *r,
                                          T *x, T *r2, T *dx, T *df, double c, double cf,
-                                         const DevCtrl *ctrl) {
-    RichRecurOp<T> op{r, x, r2, dx, df, (T)c, (T)cf, nullptr, ctrl};
+                                         double hb, const DevCtrl *ctrl) {
+    RichRecurOp<T> op{r, x, r2, dx, df, (T)c, (T)cf, (T)hb, nullptr, ctrl};
     return launch_stencil<T>(L, w, op);
 }
 
 template <typename T>
-cudaError_t Kernels<T>::residual_recur(const StencilLaunch &L, const Weights<T> &w, const T *dxc,
-                                       T *r, T *df, double cf, double *partials,
-                                       const DevCtrl *ctrl) {
-    ResRecurOp<T> op{dxc, r, df, (T)cf, partials, ctrl};
+cudaError_t Kernels<T>::residual_recur(const StencilLaunch &L, const Weights<T> &w, const T *step,
+                                       T *r, T *df, T *hc, double cf, double hb,
+                                       double *partials, const DevCtrl *ctrl) {
+    ResRecurOp<T> op{step, r, df, hc, (T)cf, (T)hb, partials, ctrl};
     return launch_stencil<T>(L, w, op);
 }
 
@@ -539,6 +555,33 @@ static cudaError_t gram_dispatch(int m, const T *dx, const T *df, const T *r, lo
     return cudaGetLastError();
 }
 
+// One wave of the Gram kernel: resident blocks per SM x SMs (cached per kind, m).
+template <typename T>
+int Kernels<T>::gram_grid(int kind, int m, long long n, int sms) {
+    static int cache[2][LSG_MAX_M + 1];
+    int &occ = cache[kind == GRAM_SYM ? 0 : 1][m];
+    if (occ == 0) {
+        int v = 0;
+        cudaError_t e = cudaSuccess;
+        switch (m) {
+#define LSG_GRAM_OCC(MM)                                                                                  \
+    case MM:                                                                                              \
+        e = kind == GRAM_SYM                                                                              \
+                ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, gram_kernel<T, GRAM_SYM, MM>, kReduceThreads, 0) \
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, gram_kernel<T, GRAM_GALERKIN, MM>, kReduceThreads, 0); \
+        break;
+            LSG_GRAM_OCC(1) LSG_GRAM_OCC(2) LSG_GRAM_OCC(3) LSG_GRAM_OCC(4)
+            LSG_GRAM_OCC(5) LSG_GRAM_OCC(6) LSG_GRAM_OCC(7) LSG_GRAM_OCC(8)
+#undef LSG_GRAM_OCC
+        default: v = 4;
+        }
+        if (e != cudaSuccess || v < 1) { cudaGetLastError(); v = 2; }
+        occ = v;
+    }
+    const long long need = (n + kReduceThreads - 1) / kReduceThreads;
+    return (int)std::max<long long>(1, std::min<long long>(need, (long long)occ * sms));
+}
+
 template <typename T>
 cudaError_t Kernels<T>::gram(int kind, int m, const T *dx, const T *df, const T *r, long long n,
                              double *partials, int blocks, const DevCtrl *ctrl, cudaStream_t s) {
@@ -547,11 +590,10 @@ cudaError_t Kernels<T>::gram(int kind, int m, const T *dx, const T *df, const T 
 }
 
 template <typename T>
-cudaError_t Kernels<T>::aar_update(int m, int col, T *x, const T *r, T *dx, const T *df,
-                                   double beta, double cf, long long n, const DevCtrl *ctrl,
-                                   cudaStream_t s) {
+cudaError_t Kernels<T>::aar_update(int m, T *x, const T *r, const T *h, T *step, double beta,
+                                   double cf, long long n, const DevCtrl *ctrl, cudaStream_t s) {
     const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 8);
-    aar_update_kernel<T><<<blocks, kReduceThreads, 0, s>>>(m, x, r, dx, df, col, (T)beta, (T)cf, n, ctrl);
+    aar_update_kernel<T><<<blocks, kReduceThreads, 0, s>>>(m, x, r, h, step, (T)beta, (T)cf, n, ctrl);
     return cudaGetLastError();
 }
 

@@ -123,8 +123,9 @@ long long partials_needed(long long n, int m, int sms) {
     // stencil launches (worst case over both tile shapes and lz >= 1 planes)
     const long long bx = (long long)sms * 8;
     cap = std::max(cap, bx);
-    // grid-stride reductions use <= 4*sms blocks; Gram writes (m*m+m) values per block
-    cap = std::max(cap, (long long)4 * sms * (m * m + m));
+    // grid-stride reductions use <= 4*sms blocks; a Gram launch (<= 8 resident
+    // 256-thread blocks per SM) writes up to m*m+m values per block
+    cap = std::max(cap, (long long)8 * sms * (m * m + m));
     (void)n;
     return cap;
 }
@@ -228,8 +229,9 @@ int check_operator(const lsg_operator *op) {
     if (!op) return set_error(LSG_BAD_ARG, "operator is NULL");
     for (int d = 0; d < 3; d++)
         if (op->n[d] < 1) return set_error(LSG_BAD_ARG, "grid size n[%d] = %d < 1", d, op->n[d]);
-    if ((long long)op->n[0] * op->n[1] > (1LL << 31) - 1)
-        return set_error(LSG_BAD_ARG, "nx*ny exceeds 2^31-1");
+    if ((long long)op->n[0] * op->n[1] * op->n[2] > 4294967295LL)
+        return set_error(LSG_BAD_ARG, "grid of %lld points exceeds 2^32-1",
+                         (long long)op->n[0] * op->n[1] * op->n[2]);
     if (op->radius < 1 || op->radius > LSG_MAX_RADIUS)
         return set_error(LSG_BAD_ARG, "radius %d outside 1..%d", op->radius, LSG_MAX_RADIUS);
     return LSG_OK;
@@ -413,6 +415,7 @@ int aar_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const 
     const StencilLaunch L{g, lz, R.s};
     const int sb = (int)stencil_blocks<T>(g, lz);
     const int rb = reduce_blocks(n, R.sms);
+    const int gb = Kernels<T>::gram_grid(GRAM_SYM, m, n, R.sms);
     T *X[2] = {x, (T *)ws->xalt};
     T *Rv[2] = {(T *)ws->r0, (T *)ws->r1};
     T *DX = (T *)ws->dx, *DF = (T *)ws->df;
@@ -427,7 +430,7 @@ int aar_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const 
     // ||b|| and tol *= ||b|| (AAR.c:78-79); f = b - A x (AAR.c:80-82).
     LSG_KC(LSG_K_UPDATE, Kernels<T>::norm2(b, n, part, rb, ctrl, R.s));
     LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, R.s));
-    LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, X[0], b, Rv[0], nullptr, cf, part, ctrl));
+    LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, X[0], b, Rv[0], nullptr, nullptr, cf, 0.0, part, ctrl));
 
     // FP64 follows the reference's true-residual form (x and r ping-pong);
     // FP32 uses the residual recurrence (x in place, only r ping-pongs).
@@ -438,21 +441,26 @@ int aar_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const 
         const int col = (it - 1) % m;  // the reference writes this column at iteration it+1
         T *dxc = DX + (size_t)col * n, *dfc = DF + (size_t)col * n;
         if (is_anderson(it)) {
-            LSG_KC(LSG_K_GRAM, Kernels<T>::gram(GRAM_SYM, m, DX, DF, Rv[rc], n, part, rb, ctrl, R.s));
-            LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, rb, GRAM_SYM, m, cf, ctrl, R.s));
-            LSG_KC(LSG_K_UPDATE, Kernels<T>::aar_update(m, col, X[xc], Rv[rc], DX, DF, prm->beta, cf, n, ctrl, R.s));
-            if (recur)
-                LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual_recur(L, w, dxc, Rv[rc], dfc, cf, part, ctrl));
-            else
-                LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_ANDERSON, X[xc], b, Rv[rc], dfc, cf, part, ctrl));
+            LSG_KC(LSG_K_GRAM, Kernels<T>::gram(GRAM_SYM, m, DX, DF, Rv[rc], n, part, gb, ctrl, R.s));
+            LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, gb, GRAM_SYM, m, cf, ctrl, R.s));
+            if (recur) {
+                // the step goes to the spare vector: the residual reads it as its stencil input
+                T *step = (T *)ws->xalt;
+                LSG_KC(LSG_K_UPDATE, Kernels<T>::aar_update(m, X[0], Rv[rc], DX, step, prm->beta, cf, n, ctrl, R.s));
+                LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual_recur(L, w, step, Rv[rc], dfc, dxc, cf, prm->beta, part, ctrl));
+            } else {
+                LSG_KC(LSG_K_UPDATE, Kernels<T>::aar_update(m, X[xc], Rv[rc], DX, dxc, prm->beta, cf, n, ctrl, R.s));
+                LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_ANDERSON, X[xc], b, Rv[rc], dfc, dxc, cf,
+                                                            prm->beta, part, ctrl));
+            }
             LSG_KC(LSG_K_SMALL, finalize_norm(part, sb, ctrl, NF_CHECK, prm->tol, it, R.s));
         } else if (recur) {
             LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson_recur(L, w, Rv[rc], X[0], Rv[rc ^ 1], dxc, dfc,
-                                                                  prm->omega * cf, cf, ctrl));
+                                                                  prm->omega * cf, cf, prm->beta, ctrl));
             rc ^= 1;
         } else {
             LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson(L, w, RICH_AAR, X[xc], Rv[rc], b, X[xc ^ 1], Rv[rc ^ 1],
-                                                            dxc, dfc, prm->omega * cf, cf, ctrl));
+                                                            dxc, dfc, prm->omega * cf, cf, prm->beta, ctrl));
             xc ^= 1;
             rc ^= 1;
         }
@@ -492,6 +500,7 @@ int prich_core(Run &R, bool galerkin, const lsg_operator *op, const lsg_params *
     DevCtrl *ctrl = ws->ctrl;
     double *part = ws->partials;
     const int kind = galerkin ? GRAM_GALERKIN : GRAM_SYM;
+    const int gb = Kernels<T>::gram_grid(kind, m, n, R.sms);
 
     ws->hctrl[0] = ctrl_init(prm->tol, 0);
     LSG_CUDA(cudaMemcpyAsync(ctrl, ws->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, R.s));
@@ -499,7 +508,7 @@ int prich_core(Run &R, bool galerkin, const lsg_operator *op, const lsg_params *
     LSG_CUDA(cudaMemsetAsync(DF, 0, sizeof(T) * (size_t)n * m, R.s));
     LSG_KC(LSG_K_UPDATE, Kernels<T>::norm2(b, n, part, rb, ctrl, R.s));
     LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, R.s));
-    LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, X[0], b, Rv[0], nullptr, cf, part, ctrl));
+    LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, X[0], b, Rv[0], nullptr, nullptr, cf, 0.0, part, ctrl));
 
     int cur = 0;
     auto is_proj = [p](int it) { return it % p == 0; };
@@ -507,11 +516,11 @@ int prich_core(Run &R, bool galerkin, const lsg_operator *op, const lsg_params *
         const int col = (it - 2 + m) % m;
         LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson(L, w, RICH_PGR, X[cur], Rv[cur], b, X[cur ^ 1], Rv[cur ^ 1],
                                       DX + (size_t)col * n, DF + (size_t)col * n, prm->omega * cf,
-                                      cf, ctrl));
+                                      cf, 0.0, ctrl));
         cur ^= 1;
         if (is_proj(it)) {
-            LSG_KC(LSG_K_GRAM, Kernels<T>::gram(kind, m, DX, DF, Rv[cur], n, part, rb, ctrl, R.s));
-            LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, rb, kind, m, 1.0, ctrl, R.s));
+            LSG_KC(LSG_K_GRAM, Kernels<T>::gram(kind, m, DX, DF, Rv[cur], n, part, gb, ctrl, R.s));
+            LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, gb, kind, m, 1.0, ctrl, R.s));
             LSG_KC(LSG_K_UPDATE, Kernels<T>::proj_update(m, col, X[cur], Rv[cur], DX, DF, n, part, rb, ctrl, R.s));
             LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_CHECK, prm->tol, it, R.s));
         }
@@ -553,7 +562,7 @@ int cg_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const T
     LSG_KC(LSG_K_UPDATE, Kernels<T>::norm2(b, n, part, rb, ctrl, R.s));
     LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, R.s));
     // r = b - A x; d = M^-1 r; delta = r.d; relres = ||r|| (CG.c:65-89)
-    LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, x, b, r, nullptr, cf, part, ctrl));
+    LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, x, b, r, nullptr, nullptr, cf, 0.0, part, ctrl));
     LSG_KC(LSG_K_SMALL, finalize_cg(part, sb, ctrl, 2, cf, op->precond, 0, max_iter, R.s));
 
     int cur = 0;
@@ -565,7 +574,7 @@ int cg_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const T
         LSG_KC(LSG_K_SMALL, finalize_cg(part, sb, ctrl, 0, cf, op->precond, it, max_iter, R.s));
         if (ic % 50 == 0) {  // restart with the true residual (CG.c:109-120)
             LSG_KC(LSG_K_UPDATE, Kernels<T>::cg_step(x, r, D[cur], q, n, 1, part, rb, ctrl, R.s));
-            LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, x, b, r, nullptr, cf, part, ctrl));
+            LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, x, b, r, nullptr, nullptr, cf, 0.0, part, ctrl));
             LSG_KC(LSG_K_SMALL, finalize_cg(part, sb, ctrl, 1, cf, op->precond, it, max_iter, R.s));
         } else {
             LSG_KC(LSG_K_UPDATE, Kernels<T>::cg_step(x, r, D[cur], q, n, 0, part, rb, ctrl, R.s));
@@ -710,11 +719,11 @@ int apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, cudaStr
     if (dtype == LSG_F64) {
         const StencilLaunch L{g, choose_lz<double>(g, stencil_slots<double>(sms)), s};
         LSG_CUDA(Kernels<double>::residual(L, make_weights<double>(op), RES_APPLY, (const double *)d_x,
-                                           nullptr, (double *)d_y, nullptr, 1.0, nullptr, nullptr));
+                                           nullptr, (double *)d_y, nullptr, nullptr, 1.0, 0.0, nullptr, nullptr));
     } else if (dtype == LSG_F32) {
         const StencilLaunch L{g, choose_lz<float>(g, stencil_slots<float>(sms)), s};
         LSG_CUDA(Kernels<float>::residual(L, make_weights<float>(op), RES_APPLY, (const float *)d_x,
-                                          nullptr, (float *)d_y, nullptr, 1.0, nullptr, nullptr));
+                                          nullptr, (float *)d_y, nullptr, nullptr, 1.0, 0.0, nullptr, nullptr));
     } else {
         return set_error(LSG_BAD_ARG, "unknown dtype %d", dtype);
     }

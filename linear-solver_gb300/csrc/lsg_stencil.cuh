@@ -19,13 +19,16 @@
 // Functor interface (all __device__):
 //   bool skip() const                     the solve has finished: return at once
 //   void init()                           read device scalars (once per thread)
-//   Raw  fetch(long long idx) const       global loads for u at idx
+//   Raw  fetch(unsigned idx) const        global loads for u at idx
 //   T    value(const Raw &) const         u from the fetched operands
-//   Ctr  fetch_center(long long idx) const  operands the epilogue needs at a centre
-//   void store(long long idx, T u, T Au, const Ctr &, Acc<T> *acc) const
+//   Ctr  fetch_center(unsigned idx) const operands the epilogue needs at a centre
+//   void store(unsigned idx, T u, T Au, const Ctr &, Acc<T> *acc) const
+// Flat indices are 32-bit: grids are limited to 2^32 - 1 points.
 //   static constexpr int NACC             per-thread accumulators reduced per block
 //   double *partials                      where the block writes NACC sums
 #pragma once
+
+#include <type_traits>
 
 #include "lsg_internal.cuh"
 #include "lsg_accum.cuh"
@@ -36,6 +39,18 @@ template <typename T>
 __device__ __forceinline__ T ldg(const T *p) { return __ldg(p); }
 
 struct NoCtr {};
+
+// Calls f(integral_constant<P>), f(integral_constant<P+1>), ... up to Q-1
+// while f returns true; returns false as soon as one call does.
+template <int P, int Q, class F>
+__device__ __forceinline__ bool unrolled_steps(F &f) {
+    if constexpr (P < Q) {
+        if (!f(std::integral_constant<int, P>{})) return false;
+        return unrolled_steps<P + 1, Q>(f);
+    } else {
+        return true;
+    }
+}
 
 // RQ: radius the storage is sized for; the arithmetic uses `radius` (== RQ on
 // the specialised path, <= RQ on the generic path).
@@ -98,21 +113,26 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
 #pragma unroll
     for (int a = 0; a < (Op::NACC > 0 ? Op::NACC : 1); a++) acc[a].zero();
 
+    // The register queue is a ring: at phase P (= step index mod Q) slot j
+    // holds plane z - RQ + ((j - P) mod Q).  The march is unrolled Q times so
+    // every slot index is a compile-time constant and advancing the ring
+    // costs no register moves.
     T q[NY][Q];
-    // Prologue: planes z0-RQ .. z0+RQ-1 into q[.][1..2RQ].
-    int zl = wrap_index(z0 - RQ, g.nz);
+    // Prologue: planes z0-RQ .. z0+RQ-1 into slots 0..2RQ-1.
+    unsigned zl = (unsigned)wrap_index(z0 - RQ, g.nz);
+    const unsigned nxy = (unsigned)g.nxy, nz = (unsigned)g.nz;
 #pragma unroll
     for (int s = 0; s < 2 * RQ; s++) {
-        const long long base = (long long)zl * g.nxy;
+        const unsigned base = zl * nxy;
 #pragma unroll
-        for (int k = 0; k < NY; k++) q[k][s + 1] = op.value(op.fetch(base + col[k]));
-        zl = (zl + 1 == g.nz) ? 0 : zl + 1;
+        for (int k = 0; k < NY; k++) q[k][s] = op.value(op.fetch(base + col[k]));
+        zl = (zl + 1 == nz) ? 0u : zl + 1;
     }
     // In flight for the next plane: queue head (plane z+RQ), halo and centres (plane z).
     Raw qn[NY], hn[NH];
     Ctr cn[NY];
     {
-        const long long lb = (long long)zl * g.nxy, zb = (long long)z0 * g.nxy;
+        const unsigned lb = zl * nxy, zb = (unsigned)z0 * nxy;
 #pragma unroll
         for (int k = 0; k < NY; k++) {
             qn[k] = op.fetch(lb + col[k]);
@@ -121,18 +141,20 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
 #pragma unroll
         for (int s = 0; s < NH; s++)
             if (hs[s] >= 0) hn[s] = op.fetch(zb + ho[s]);
-        zl = (zl + 1 == g.nz) ? 0 : zl + 1;
+        zl = (zl + 1 == nz) ? 0u : zl + 1;
     }
 
     T *sm = smem0;
-    for (int z = z0; z < z1; z++) {
-        const long long zbase = (long long)z * g.nxy;
+    int z = z0;
+    auto step = [&](auto phase) -> bool {
+        constexpr int P = decltype(phase)::value;
+        constexpr int HEAD = (P + Q - 1) % Q;  // slot receiving plane z+RQ
+        constexpr int CEN = (P + RQ) % Q;      // slot of plane z
+        const unsigned zbase = (unsigned)z * nxy;
 #pragma unroll
         for (int k = 0; k < NY; k++) {
-#pragma unroll
-            for (int s = 0; s < Q - 1; s++) q[k][s] = q[k][s + 1];
-            q[k][Q - 1] = op.value(qn[k]);
-            sm[(RQ + ty + BY * k) * FX + RQ + tx] = q[k][RQ];
+            q[k][HEAD] = op.value(qn[k]);
+            sm[(RQ + ty + BY * k) * FX + RQ + tx] = q[k][CEN];
         }
 #pragma unroll
         for (int s = 0; s < NH; s++)
@@ -141,7 +163,7 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
 #pragma unroll
         for (int k = 0; k < NY; k++) cc[k] = cn[k];
         if (z + 1 < z1) {  // issue plane z+1's loads before computing plane z
-            const long long lb = (long long)zl * g.nxy, nb = zbase + g.nxy;
+            const unsigned lb = zl * nxy, nb = zbase + nxy;
 #pragma unroll
             for (int k = 0; k < NY; k++) {
                 qn[k] = op.fetch(lb + col[k]);
@@ -150,33 +172,34 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
 #pragma unroll
             for (int s = 0; s < NH; s++)
                 if (hs[s] >= 0) hn[s] = op.fetch(nb + ho[s]);
-            zl = (zl + 1 == g.nz) ? 0 : zl + 1;
+            zl = (zl + 1 == nz) ? 0u : zl + 1;
         }
-        __syncthreads();  // plane z staged (the other buffer is still being read by no one)
+        __syncthreads();  // plane z staged; the other buffer is no longer read
 #pragma unroll
         for (int k = 0; k < NY; k++) {
             const T *row = sm + (RQ + ty + BY * k) * FX + RQ + tx;
-            T au = w.w[0] * q[k][RQ];
+            T au = w.w[0] * q[k][CEN];
 #pragma unroll
             for (int p = 1; p <= RQ; p++) {
                 if (GENERIC && p > radius) break;
                 const T sxy = (row[-p] + row[p]) + (row[-p * FX] + row[p * FX]);
-                const T sz = q[k][RQ - p] + q[k][RQ + p];
+                const T sz = q[k][(CEN + Q - p) % Q] + q[k][(CEN + p) % Q];
                 au = fma(w.w[p], sxy + sz, au);
             }
-            if (valid[k]) op.store(zbase + col[k], q[k][RQ], au, cc[k], acc);
+            if (valid[k]) op.store(zbase + col[k], q[k][CEN], au, cc[k], acc);
         }
         sm = (sm == smem0) ? smem1 : smem0;
+        return ++z < z1;
+    };
+    while (z < z1) {
+        if (!unrolled_steps<0, Q>(step)) break;
     }
 
     if (Op::NACC > 0) {
         constexpr int NA = Op::NACC > 0 ? Op::NACC : 1;
         __shared__ double red[NA * 32];
-        double v[NA];
-#pragma unroll
-        for (int a = 0; a < NA; a++) v[a] = acc[a].get();
         const long long blk = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
-        block_sum_store<NA>(v, red, op.partials + blk * Op::NACC);
+        block_reduce_store<NA, T>(acc, red, op.partials + blk * Op::NACC);
     }
 }
 
