@@ -63,9 +63,9 @@ typedef struct lsg_params {
     int p;               /* extrapolation / projection period */
     int max_iter;        /* iteration limit (inner limit for the mixed solver) */
     double tol;          /* stop when ||b - A x|| <= tol * ||b|| */
-    /* mixed-precision iterative refinement (lsg_aar_mixed) */
-    double inner_tol;    /* relative reduction asked of each FP32 inner solve (0 = 1e-3) */
-    int max_outer;       /* FP64 refinement steps (0 = 50) */
+    /* mixed precision (lsg_aar_mixed) */
+    double inner_tol;    /* FP32 residual reduction between FP64 residual replacements (0 = 3e-2) */
+    int max_outer;       /* FP64 residual replacements (0 = 50) */
     /* execution */
     int check_every;     /* extrapolation cycles enqueued between convergence reads (0 = auto) */
 } lsg_params;
@@ -108,9 +108,13 @@ int lsg_pl2r(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x
 int lsg_cg(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
            const void *d_b, lsg_result *res, void *stream);    /* MPI_REAL/CG.c:33 */
 
-/* Mixed precision: FP64 x and b; outer FP64 residual refinement around an
- * FP32 inner AAR (FP32 vectors, history and stencil; FP64 reductions and m x m
- * solve).  Stops when the FP64 residual satisfies tol. */
+/* Mixed precision: FP64 x and b.  One FP32 AAR (FP32 vectors, history and
+ * stencil; FP64-class reductions and m x m solve) runs on the correction;
+ * each time its residual has dropped by inner_tol the correction is folded
+ * into x (FP64), r = b - A x is recomputed in FP64 and the FP32 iteration
+ * resumes from it with its history intact.  Stops when the FP64 residual
+ * satisfies tol.  res->iters counts FP32 iterations, res->outer_iters the
+ * FP64 residual replacements. */
 int lsg_aar_mixed(const lsg_operator *op, const lsg_params *prm, double *d_x, const double *d_b,
                   lsg_result *res, void *stream);
 

@@ -32,7 +32,7 @@ struct DevCtrl {
     int stall;        // checks since relres last fell below 0.7 * best
     int stall_limit;  // 0: off; else stop (done, stalled = 1) after this many checks
     int stalled;      // set when the stall rule ended the solve
-    int pad1;
+    int svd_fallbacks;  // extrapolation steps whose Gram needed the Jacobi SVD
     double s[LSG_MAX_M];  // m x m solve output
 };
 
@@ -218,8 +218,8 @@ struct Kernels {
 // r32 = float(b - A x64), partial ||b - A x64||^2 (FP64 stencil).
 cudaError_t ir_residual(const StencilLaunch &L, const Weights<double> &w, const double *x,
                         const double *b, float *r32, double *partials, const DevCtrl *ctrl);
-// x64 += e32
-cudaError_t ir_correct(double *x, const float *e, long long n, cudaStream_t s);
+// x64 += e32; e32 = 0
+cudaError_t ir_correct(double *x, float *e, long long n, cudaStream_t s);
 
 // Finalize kernels (lsg_small.cu).
 enum NormFinal {

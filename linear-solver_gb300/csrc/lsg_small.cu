@@ -249,6 +249,110 @@ __device__ int warp_pinv8(double *G, double *V, const double *b, double *x, int 
     return any ? LSG_SVD_NO_CONVERGENCE : 0;
 }
 
+// 1/d in FP64 from an FP32 seed and two Newton steps (no FP64 divide).
+__device__ __forceinline__ double rcp_newton(double d) {
+    double r = (double)(1.0f / (float)d);
+    r = r * fma(-d, r, 2.0);
+    r = r * fma(-d, r, 2.0);
+    return r;
+}
+
+// Fast path for a symmetric positive semi-definite G (the AAR / PL2R Gram):
+// x = G^-1 h by a lane-parallel LDL^T factorisation, taken only when it is
+// provably what the reference's truncated pseudo-inverse returns.  Rows and
+// columns of G that are exactly zero (history columns not yet written) have
+// exactly-zero singular values, which the reference drops; they are dropped
+// here too and x is 0 there.  For the rest, kappa_2(G) <= trace(G) *
+// trace(G^-1); when that bound is below 1 / (100 m eps) no singular value can
+// fall under the cutoff m * wmax * eps (MPI_REAL/tools.c:331-335), so the
+// pseudo-inverse is the inverse.  Returns false (caller falls back to the
+// Jacobi SVD) when G is not of that kind.  G: m x m row-major (ld m) in shared
+// memory; Ls, Wi: m x m shared scratch; dd: m doubles.  One warp.
+__device__ bool warp_ldl_solve(const double *G, const double *h, double *x, int m, double *Ls,
+                               double *Wi, double *dd) {
+    const int lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    bool act = false, bad = false;
+    double trg = 0.0;
+    if (lane < m) {
+        const double gii = G[lane * m + lane];
+        act = gii != 0.0;
+        bad = gii < 0.0 || !isfinite(gii);
+        if (!act)
+            for (int j = 0; j < m; j++) bad |= G[lane * m + j] != 0.0 || G[j * m + lane] != 0.0;
+        trg = gii;
+    }
+    if (__any_sync(full, bad)) return false;
+    const unsigned amask = __ballot_sync(full, act);
+    if (amask == 0) {  // G = 0: the reference's pinv returns 0
+        if (lane < m) x[lane] = 0.0;
+        return true;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) trg += __shfl_xor_sync(full, trg, o);
+    // Work on sc * G with sc a power of two making the trace O(1), so every
+    // pivot lies in the range where the FP32-seeded reciprocal is valid
+    // (an out-of-range pivot gives a non-finite bound and the fallback).
+    int ex = 0;
+    frexp(trg, &ex);
+    const double sc = ldexp(1.0, -ex);
+    trg *= sc;
+    for (int k = lane; k < m * m; k += 32) Ls[k] = 0.0;
+    __syncwarp();
+    // LDL^T over the active indices: lane r holds row r of L.
+    double rinv = 0.0;  // lane j: 1 / d_j
+    for (int j = 0; j < m; j++) {
+        if (!((amask >> j) & 1u)) continue;
+        double acc = 0.0;
+        if (lane < m) {
+            acc = G[lane * m + j] * sc;
+            for (int t = 0; t < j; t++)
+                if ((amask >> t) & 1u) acc = fma(-Ls[lane * m + t] * dd[t], Ls[j * m + t], acc);
+        }
+        const double dj = __shfl_sync(full, acc, j);
+        if (!(dj > 0.0)) return false;
+        const double inv = rcp_newton(dj);
+        if (lane == j) { dd[j] = dj; Ls[j * m + j] = 1.0; rinv = inv; }
+        if (lane < m && lane > j && act) Ls[lane * m + j] = acc * inv;
+        __syncwarp();
+    }
+    // kappa bound: trace(G^-1) = sum_k (1/d_k) ||row k of L^-1||^2.  Lane c
+    // builds column c of L^-1 by forward substitution.
+    if (lane < m) {
+        for (int r = 0; r < m; r++) {
+            double v = (r == lane) ? 1.0 : 0.0;
+            if (((amask >> r) & 1u) && r > lane)
+                for (int t = lane; t < r; t++) v = fma(-Ls[r * m + t], Wi[t * m + lane], v);
+            Wi[r * m + lane] = ((amask >> r) & 1u) ? v : 0.0;
+        }
+    }
+    __syncwarp();
+    double tri = 0.0;
+    if (lane < m && act) {
+        double rn = 0.0;
+        for (int c = 0; c < m; c++) rn = fma(Wi[lane * m + c], Wi[lane * m + c], rn);
+        tri = rn * rinv;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tri += __shfl_xor_sync(full, tri, o);
+    if (!(trg * tri * (100.0 * m * kPinvEps) < 1.0)) return false;
+    // Solve L z = h, z /= d, L^T x = z.
+    double sv = (lane < m && act) ? h[lane] : 0.0;
+    for (int t = 0; t < m; t++) {
+        if (!((amask >> t) & 1u)) continue;
+        const double zt = __shfl_sync(full, sv, t);
+        if (lane < m && lane > t && act) sv = fma(-Ls[lane * m + t], zt, sv);
+    }
+    sv *= rinv;
+    for (int t = m - 1; t >= 0; t--) {
+        if (!((amask >> t) & 1u)) continue;
+        const double xt = __shfl_sync(full, sv, t);
+        if (lane < m && lane < t && act) sv = fma(-Ls[t * m + lane], xt, sv);
+    }
+    if (lane < m) x[lane] = act ? sv * sc : 0.0;
+    return true;
+}
+
 // Dispatch on m; G (m x m row-major) is overwritten.  Gs / Vs: 8 x 8 staging
 // for the fast path.  Called by one full warp.
 __device__ int warp_pinv_any(double *G, double *V, const double *b, double *x, int m, double *Gs,
@@ -269,8 +373,8 @@ __global__ void finalize_gram_solve_kernel(const double *partials, int nparts, i
                                            double hscale, DevCtrl *ctrl) {
     __shared__ double vals[LSG_MAX_M * LSG_MAX_M + LSG_MAX_M];
     __shared__ double G[LSG_MAX_M * LSG_MAX_M], V[LSG_MAX_M * LSG_MAX_M];
-    __shared__ double Gs[64], Vs[64];
-    __shared__ double h[LSG_MAX_M], s[LSG_MAX_M];
+    __shared__ double Gs[LSG_MAX_M * LSG_MAX_M], Vs[64];
+    __shared__ double h[LSG_MAX_M], s[LSG_MAX_M], dd[LSG_MAX_M];
     __shared__ int bad;
     if (ctrl_done(ctrl)) return;
     const int nv = gram_values(kind, m);
@@ -307,7 +411,14 @@ __global__ void finalize_gram_solve_kernel(const double *partials, int nparts, i
         for (int j = threadIdx.x; j < m; j += 32) h[j] = vals[np + j] * hscale;
         __syncwarp();
         int st = 0;
-        if (!bad) st = warp_pinv_any(G, V, h, s, m, Gs, Vs);
+        if (!bad) {
+            // symmetric PSD Gram: LDL^T when provably equal to the truncated pinv
+            const bool fast = kind == GRAM_SYM && warp_ldl_solve(G, h, s, m, V, Gs + 0, dd);
+            if (!fast) {
+                if (kind == GRAM_SYM && threadIdx.x == 0) ctrl->svd_fallbacks++;
+                st = warp_pinv_any(G, V, h, s, m, Gs, Vs);
+            }
+        }
         __syncwarp();
         if (threadIdx.x < m) ctrl->s[threadIdx.x] = bad ? 0.0 : s[threadIdx.x];
         if (threadIdx.x == 0) {

@@ -402,42 +402,74 @@ static double now_s() {
 
 // ---------------------------------------------------------------- AAR
 
-// AAR.c:37-177.  x (in/out) and b are device arrays of n values of T.
+// Number of Richardson (non-extrapolation) iterations among 1..last: the
+// parity of the r (and, in the reference form, x) ping-pong after `last`.
+static long long richardson_count(int last, int p) {
+    if (last < 1) return 0;
+    return last - last / p + (p == 1 ? 1 : 0);
+}
+
+// The AAR iteration (AAR.c:91-148) as a resumable object: enqueue(it) issues
+// iteration `it`; the caller drives it with pipelined_loop and may pause it
+// (the device sets ctrl->done) and resume from any iteration.
+//   FP64 follows the reference's true-residual form: x and r ping-pong.
+//   FP32 uses the residual recurrence: x in place, only r ping-pongs, and
+//   b is not read after the initial residual.
 template <typename T>
-int aar_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const T *b,
-             Workspace *ws, int stall_limit, DevCtrl *out) {
-    const Geom g = make_geom(op->n);
-    const long long n = g.n;
-    const int m = prm->m, p = prm->p, max_iter = prm->max_iter;
-    const Weights<T> w = make_weights<T>(op);
-    const double cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
-    const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
-    const StencilLaunch L{g, lz, R.s};
-    const int sb = (int)stencil_blocks<T>(g, lz);
-    const int rb = reduce_blocks(n, R.sms);
-    const int gb = Kernels<T>::gram_grid(GRAM_SYM, m, n, R.sms);
-    T *X[2] = {x, (T *)ws->xalt};
-    T *Rv[2] = {(T *)ws->r0, (T *)ws->r1};
-    T *DX = (T *)ws->dx, *DF = (T *)ws->df;
-    DevCtrl *ctrl = ws->ctrl;
-    double *part = ws->partials;
-
-    DevCtrl c0 = ctrl_init(prm->tol, stall_limit);
-    ws->hctrl[0] = c0;
-    LSG_CUDA(cudaMemcpyAsync(ctrl, ws->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, R.s));
-    LSG_CUDA(cudaMemsetAsync(DX, 0, sizeof(T) * (size_t)n * m, R.s));
-    LSG_CUDA(cudaMemsetAsync(DF, 0, sizeof(T) * (size_t)n * m, R.s));
-    // ||b|| and tol *= ||b|| (AAR.c:78-79); f = b - A x (AAR.c:80-82).
-    LSG_KC(LSG_K_UPDATE, Kernels<T>::norm2(b, n, part, rb, ctrl, R.s));
-    LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, R.s));
-    LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_INIT, X[0], b, Rv[0], nullptr, nullptr, cf, 0.0, part, ctrl));
-
-    // FP64 follows the reference's true-residual form (x and r ping-pong);
-    // FP32 uses the residual recurrence (x in place, only r ping-pongs).
-    constexpr bool recur = std::is_same<T, float>::value;
+struct AarLoop {
+    static constexpr bool recur = std::is_same<T, float>::value;
+    Run &R;
+    const lsg_params *prm;
+    Workspace *ws;
+    const T *b;
+    long long n;
+    int m, p;
+    Weights<T> w;
+    double cf;
+    StencilLaunch L;
+    int sb, rb, gb;
+    T *X[2];
+    T *Rv[2];
+    T *DX, *DF;
+    DevCtrl *ctrl;
+    double *part;
     int xc = 0, rc = 0;
-    auto is_anderson = [p](int it) { return it % p == 0 && it > 1; };
-    auto enqueue = [&](int it) -> int {
+
+    AarLoop(Run &R_, const lsg_operator *op, const lsg_params *prm_, T *x, const T *b_, Workspace *ws_)
+        : R(R_), prm(prm_), ws(ws_), b(b_) {
+        const Geom g = make_geom(op->n);
+        n = g.n;
+        m = prm->m;
+        p = prm->p;
+        w = make_weights<T>(op);
+        cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
+        const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
+        L = StencilLaunch{g, lz, R.s};
+        sb = (int)stencil_blocks<T>(g, lz);
+        rb = reduce_blocks(n, R.sms);
+        gb = Kernels<T>::gram_grid(GRAM_SYM, m, n, R.sms);
+        X[0] = x;
+        X[1] = (T *)ws->xalt;
+        Rv[0] = (T *)ws->r0;
+        Rv[1] = (T *)ws->r1;
+        DX = (T *)ws->dx;
+        DF = (T *)ws->df;
+        ctrl = ws->ctrl;
+        part = ws->partials;
+    }
+    bool is_anderson(int it) const { return it % p == 0 && it > 1; }
+    // r buffer holding the residual after iteration `last`
+    void sync_parity(int last) {
+        const long long rich = richardson_count(last, p);
+        rc = (int)(rich & 1);
+        xc = recur ? 0 : rc;
+    }
+    int reset_history() {
+        LSG_CUDA(cudaMemsetAsync(DX, 0, sizeof(T) * (size_t)n * m, R.s));
+        LSG_CUDA(cudaMemsetAsync(DF, 0, sizeof(T) * (size_t)n * m, R.s));
+        return LSG_OK;
+    }
+    int enqueue(int it) {
         const int col = (it - 1) % m;  // the reference writes this column at iteration it+1
         T *dxc = DX + (size_t)col * n, *dfc = DF + (size_t)col * n;
         if (is_anderson(it)) {
@@ -465,18 +497,38 @@ int aar_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const 
             rc ^= 1;
         }
         return LSG_OK;
-    };
-    int rcode = pipelined_loop(R, ws, 1, max_iter, default_per_check(prm, n), enqueue, is_anderson);
-    if (rcode != LSG_OK) return rcode;
+    }
+    // Runs iterations first..max_iter until the device pauses or stops.
+    int run(int first) {
+        auto enq = [this](int it) { return enqueue(it); };
+        auto chk = [this](int it) { return is_anderson(it); };
+        return pipelined_loop(R, ws, first, prm->max_iter, default_per_check(prm, n), enq, chk);
+    }
+};
+
+// AAR.c:37-177.  x (in/out) and b are device arrays of n values of T.
+template <typename T>
+int aar_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const T *b,
+             Workspace *ws, DevCtrl *out) {
+    AarLoop<T> A(R, op, prm, x, b, ws);
+    ws->hctrl[0] = ctrl_init(prm->tol, 0);
+    LSG_CUDA(cudaMemcpyAsync(A.ctrl, ws->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, R.s));
+    int rc = A.reset_history();
+    if (rc) return rc;
+    // ||b|| and tol *= ||b|| (AAR.c:78-79); f = b - A x (AAR.c:80-82).
+    LSG_KC(LSG_K_UPDATE, Kernels<T>::norm2(b, A.n, A.part, A.rb, A.ctrl, R.s));
+    LSG_KC(LSG_K_SMALL, finalize_norm(A.part, A.rb, A.ctrl, NF_RHS, prm->tol, 0, R.s));
+    LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(A.L, A.w, RES_INIT, x, b, A.Rv[0], nullptr, nullptr, A.cf, 0.0,
+                                                A.part, A.ctrl));
+    rc = A.run(1);
+    if (rc != LSG_OK) return rc;
     DevCtrl c;
-    LSG_CUDA(cudaMemcpy(&c, ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost));
+    LSG_CUDA(cudaMemcpy(&c, A.ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost));
     // Where the last iterate lives: in the reference form x moved to the other
     // buffer at every Richardson iteration up to the final one.
-    const int last = c.done ? c.iters : max_iter;
-    long long rich = last - last / p + (p == 1 && last >= 1 ? 1 : 0);
-    if (last < 1) rich = 0;
-    if (!recur && (rich & 1))
-        LSG_CUDA(cudaMemcpyAsync(x, X[1], sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, R.s));
+    const int last = c.done ? c.iters : prm->max_iter;
+    if (!AarLoop<T>::recur && (richardson_count(last, prm->p) & 1))
+        LSG_CUDA(cudaMemcpyAsync(x, A.X[1], sizeof(T) * (size_t)A.n, cudaMemcpyDeviceToDevice, R.s));
     LSG_CUDA(cudaStreamSynchronize(R.s));
     *out = c;
     return LSG_OK;
@@ -606,7 +658,7 @@ static int solve_t(int solver, const lsg_operator *op, const lsg_params *prm, vo
     Run R(s, sm_count());
     DevCtrl c;
     switch (solver) {
-    case 0: rc = aar_core<T>(R, op, prm, (T *)d_x, (const T *)d_b, ws, 0, &c); break;
+    case 0: rc = aar_core<T>(R, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
     case 1: rc = prich_core<T>(R, true, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
     case 2: rc = prich_core<T>(R, false, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
     default: rc = cg_core<T>(R, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
@@ -636,6 +688,15 @@ int solve(int solver, const lsg_operator *op, const lsg_params *prm, int dtype, 
 
 // ---------------------------------------------------------------- mixed precision
 
+// FP32 AAR with FP64 residual replacement.  One FP32 AAR iteration runs on the
+// correction e (x = x64 + e), its residual carried by the FP32 recurrence.
+// Whenever the FP32 residual has fallen by the factor rho = inner_tol since
+// the last replacement (or stalls, or passes tol), the device pauses the
+// iteration; the host then folds e into x64 (x64 += e, e = 0), recomputes
+// r = b - A x64 in FP64, stores it as the FP32 residual and resumes -- with the
+// Anderson history intact, so no iterations are spent rebuilding it.  FP64
+// is used only for that residual, x64, the reductions and the m x m solve.
+// Convergence is decided on the FP64 residual.
 int solve_mixed(const lsg_operator *op, const lsg_params *prm, double *x, const double *b,
                 lsg_result *res, cudaStream_t s) {
     const double t0 = now_s();
@@ -648,60 +709,74 @@ int solve_mixed(const lsg_operator *op, const lsg_params *prm, double *x, const 
     const long long n = g.n;
     Workspace *wo = nullptr, *wi = nullptr;
     std::unique_lock<std::mutex> lo, li;
-    rc = get_workspace(sizeof(double), n, 1, true, g, &wo, &lo);  // outer: r32, e32, partials, ctrl
+    rc = get_workspace(sizeof(double), n, 1, true, g, &wo, &lo);  // outer: e32, partials, ctrl
     if (rc) return rc;
-    rc = get_workspace(sizeof(float), n, prm->m, false, g, &wi, &li);  // inner FP32 AAR
+    rc = get_workspace(sizeof(float), n, prm->m, false, g, &wi, &li);  // FP32 AAR work arrays
     if (rc) return rc;
     Run R(s, sm_count());
-    const Weights<double> w = make_weights<double>(op);
+    const Weights<double> w64 = make_weights<double>(op);
     const int lz = choose_lz<double>(g, stencil_slots<double>(R.sms));
-    const StencilLaunch L{g, lz, s};
-    const int sb = (int)stencil_blocks<double>(g, lz);
+    const StencilLaunch L64{g, lz, s};
+    const int sb64 = (int)stencil_blocks<double>(g, lz);
     const int rb = reduce_blocks(n, R.sms);
-    DevCtrl *ctrl = wo->ctrl;
-    double *part = wo->partials;
+    DevCtrl *octrl = wo->ctrl;
+    double *opart = wo->partials;
     const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
-    lsg_params ip = *prm;
-    ip.tol = prm->inner_tol > 0 ? prm->inner_tol : 1e-3;
+    const double rho = prm->inner_tol > 0 ? prm->inner_tol : 3e-2;
+    AarLoop<float> A(R, op, prm, wo->e32, nullptr, wi);
 
     wo->hctrl[0] = ctrl_init(prm->tol, 0);
-    LSG_CUDA(cudaMemcpyAsync(ctrl, wo->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, s));
-    LSG_KC(LSG_K_UPDATE, Kernels<double>::norm2(b, n, part, rb, ctrl, s));
-    LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, s));
-    int outer = 0, inner_total = 0, status = LSG_NOT_CONVERGED;
-    double prev = INFINITY;
-    DevCtrl c;
+    LSG_CUDA(cudaMemcpyAsync(octrl, wo->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, s));
+    LSG_CUDA(cudaMemsetAsync(wo->e32, 0, sizeof(float) * (size_t)n, s));
+    rc = A.reset_history();
+    if (rc) return rc;
+    LSG_KC(LSG_K_UPDATE, Kernels<double>::norm2(b, n, opart, rb, octrl, s));
+    LSG_KC(LSG_K_SMALL, finalize_norm(opart, rb, octrl, NF_RHS, prm->tol, 0, s));
+
+    int status = LSG_NOT_CONVERGED, replacements = 0, it = 1, iters = 0;
+    DevCtrl co, ci;
     for (;;) {
-        // r = b - A x in FP64, stored as the FP32 right-hand side of the inner solve.
-        LSG_KC(LSG_K_REFINE, ir_residual(L, w, x, b, wo->r32, part, ctrl));
-        LSG_KC(LSG_K_SMALL, finalize_norm(part, sb, ctrl, NF_CHECK, prm->tol, outer, s));
-        LSG_CUDA(cudaMemcpyAsync(&wo->hctrl[0], ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost, s));
+        // r = b - A x64 in FP64, stored as the FP32 residual the iteration continues from
+        A.sync_parity(it - 1);
+        LSG_KC(LSG_K_REFINE, ir_residual(L64, w64, x, b, A.Rv[A.rc], opart, octrl));
+        LSG_KC(LSG_K_SMALL, finalize_norm(opart, sb64, octrl, NF_CHECK, prm->tol, it - 1, s));
+        LSG_CUDA(cudaMemcpyAsync(&wo->hctrl[0], octrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost, s));
         LSG_CUDA(cudaStreamSynchronize(s));
-        c = wo->hctrl[0];
-        if (c.status == LSG_NAN_DETECTED) { status = LSG_NAN_DETECTED; break; }
-        if (c.done) { status = LSG_OK; break; }
-        if (outer >= max_outer || inner_total >= prm->max_iter) break;
-        if (!(c.relres < prev)) break;  // refinement no longer reduces the FP64 residual
-        prev = c.relres;
-        // Inner FP32 AAR on A e = r, e0 = 0, stopped at inner_tol or when it stalls.
-        LSG_CUDA(cudaMemsetAsync(wo->e32, 0, sizeof(float) * (size_t)n, s));
-        ip.max_iter = prm->max_iter - inner_total;
-        DevCtrl ci;
-        rc = aar_core<float>(R, op, &ip, wo->e32, wo->r32, wi, 12, &ci);
-        if (rc) return rc;
-        inner_total += ci.done ? ci.iters : ip.max_iter;
+        co = wo->hctrl[0];
+        if (co.status == LSG_NAN_DETECTED) { status = LSG_NAN_DETECTED; break; }
+        if (co.done) { status = LSG_OK; break; }
+        if (it > prm->max_iter || replacements >= max_outer) break;
+        // resume (or start) the FP32 iteration with its next pause target
+        if (it == 1) {
+            ci = ctrl_init(prm->tol, 12);
+        } else {
+            ci.done = 0;
+            ci.stall = 0;
+            ci.stalled = 0;
+            ci.best = INFINITY;
+        }
+        ci.tol_abs = std::max(co.tol_abs, rho * co.relres);
+        ci.rhs_norm = co.rhs_norm;
+        wi->hctrl[0] = ci;
+        LSG_CUDA(cudaMemcpyAsync(A.ctrl, wi->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, s));
+        rc = A.run(it);
+        if (rc != LSG_OK) return rc;
+        LSG_CUDA(cudaMemcpy(&ci, A.ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost));
         if (ci.status == LSG_NAN_DETECTED) { status = LSG_NAN_DETECTED; break; }
+        iters = ci.done ? ci.iters : prm->max_iter;
+        // fold the correction into x64 (e = 0 afterwards) and replace the residual
         LSG_KC(LSG_K_REFINE, ir_correct(x, wo->e32, n, s));
-        outer++;
+        replacements++;
+        it = iters + 1;
     }
     LSG_CUDA(cudaStreamSynchronize(s));
     R.flush();
     if (res) {
-        res->iters = inner_total;
-        res->inner_iters = inner_total;
-        res->outer_iters = outer;
-        res->rhs_norm = c.rhs_norm;
-        res->relres = c.rhs_norm > 0 ? c.relres / c.rhs_norm : c.relres;
+        res->iters = iters;
+        res->inner_iters = iters;
+        res->outer_iters = replacements;
+        res->rhs_norm = co.rhs_norm;
+        res->relres = co.rhs_norm > 0 ? co.relres / co.rhs_norm : co.relres;
         res->status = status;
         res->seconds = now_s() - t0;
         res->launches = R.launches;
@@ -777,7 +852,7 @@ void lsg_params_default(lsg_params *prm) {
     prm->p = 6;
     prm->max_iter = 100000;
     prm->tol = 1e-8;
-    prm->inner_tol = 1e-3;
+    prm->inner_tol = 3e-2;
     prm->max_outer = 50;
 }
 

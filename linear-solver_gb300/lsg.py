@@ -190,7 +190,7 @@ class Operator:
         return [self._s.coeff[i] for i in range(self.radius + 1)]
 
 
-def _params(omega=0.6, beta=0.6, m=7, p=6, max_iter=100000, tol=1e-8, inner_tol=1e-3,
+def _params(omega=0.6, beta=0.6, m=7, p=6, max_iter=100000, tol=1e-8, inner_tol=3e-2,
             max_outer=50, check_every=0) -> _Params:
     prm = _Params()
     lib().lsg_params_default(C.byref(prm))
@@ -279,7 +279,7 @@ SOLVERS = {"aar": aar, "pgr": pgr, "pl2r": pl2r, "cg": cg}
 
 
 def aar_mixed(op, b, x0=None, stream=None, **kw):
-    """FP64 iterative refinement around an FP32 AAR; b and x are float64."""
+    """FP32 AAR with FP64 residual replacement (include/lsg.h); b and x are float64."""
     import torch
     if b.dtype != torch.float64:
         raise TypeError("aar_mixed takes float64 b / x")
