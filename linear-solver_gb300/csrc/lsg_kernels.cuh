@@ -378,7 +378,10 @@ __global__ void __launch_bounds__(kReduceThreads) gram_generic_kernel(int kind, 
 
 // x_new = x + beta cf r - sum_j H_j s_j with H_j = DX_j + beta DF_j
 // (AAR.c:116-117, 225-231); the step x_new - x_old goes to `step`.
-template <typename T>
+// M: history depth known at compile time (all m loads in flight at once),
+// VN points per thread and step through 16-byte vectors; M = 0 is the
+// generic path (runtime m, scalar).
+template <typename T, int M>
 __global__ void __launch_bounds__(kReduceThreads) aar_update_kernel(int m, T *__restrict__ x,
                                                                     const T *__restrict__ r,
                                                                     const T *__restrict__ h,
@@ -390,13 +393,46 @@ __global__ void __launch_bounds__(kReduceThreads) aar_update_kernel(int m, T *__
     if (threadIdx.x < m) s[threadIdx.x] = (T)ctrl->s[threadIdx.x];
     __syncthreads();
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        T am = T(0);
-        for (int j = 0; j < m; j++) am = fma(ldg(h + j * n + i), s[j], am);
-        const T xo = x[i];
-        const T xn = fma(beta, r[i] * cf, xo) - am;
-        x[i] = xn;
-        step[i] = xn - xo;
+    if constexpr (M > 0) {
+        using V = typename Vec4<T>::type;
+        constexpr int VN = Vec4<T>::N;
+        const long long nv = n / VN;  // caller guarantees n % VN == 0
+        const V *hv = reinterpret_cast<const V *>(h);
+        V *xv = reinterpret_cast<V *>(x);
+        const V *rv = reinterpret_cast<const V *>(r);
+        V *sv = reinterpret_cast<V *>(step);
+        T sj[M];
+#pragma unroll
+        for (int j = 0; j < M; j++) sj[j] = s[j];
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride) {
+            V hj[M];
+#pragma unroll
+            for (int j = 0; j < M; j++) hj[j] = ldv(hv + j * nv + i);
+            const V xo = xv[i], ro = rv[i];
+            T *xs = (T *)&xo;
+            const T *rs = (const T *)&ro;
+            V xn, st;
+            T *xns = (T *)&xn, *sts = (T *)&st;
+#pragma unroll
+            for (int e = 0; e < VN; e++) {
+                T am = T(0);
+#pragma unroll
+                for (int j = 0; j < M; j++) am = fma(((const T *)&hj[j])[e], sj[j], am);
+                xns[e] = fma(beta, rs[e] * cf, xs[e]) - am;
+                sts[e] = xns[e] - xs[e];
+            }
+            xv[i] = xn;
+            sv[i] = st;
+        }
+    } else {
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            T am = T(0);
+            for (int j = 0; j < m; j++) am = fma(ldg(h + j * n + i), s[j], am);
+            const T xo = x[i];
+            const T xn = fma(beta, r[i] * cf, xo) - am;
+            x[i] = xn;
+            step[i] = xn - xo;
+        }
     }
 }
 
@@ -593,7 +629,15 @@ template <typename T>
 cudaError_t Kernels<T>::aar_update(int m, T *x, const T *r, const T *h, T *step, double beta,
                                    double cf, long long n, const DevCtrl *ctrl, cudaStream_t s) {
     const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 8);
-    aar_update_kernel<T><<<blocks, kReduceThreads, 0, s>>>(m, x, r, h, step, (T)beta, (T)cf, n, ctrl);
+    const bool vec = n % Vec4<T>::N == 0;
+    switch (vec ? m : 0) {
+#define LSG_UPD_CASE(MM) \
+    case MM: aar_update_kernel<T, MM><<<blocks, kReduceThreads, 0, s>>>(m, x, r, h, step, (T)beta, (T)cf, n, ctrl); break;
+        LSG_UPD_CASE(1) LSG_UPD_CASE(2) LSG_UPD_CASE(3) LSG_UPD_CASE(4)
+        LSG_UPD_CASE(5) LSG_UPD_CASE(6) LSG_UPD_CASE(7) LSG_UPD_CASE(8)
+#undef LSG_UPD_CASE
+    default: aar_update_kernel<T, 0><<<blocks, kReduceThreads, 0, s>>>(m, x, r, h, step, (T)beta, (T)cf, n, ctrl);
+    }
     return cudaGetLastError();
 }
 

@@ -408,3 +408,75 @@ def compat_solve(solver: str, x, rhs, *, n=None, fdn=6, a=A_REF, precond=True, o
     out = _result(res)
     out["last_status"] = L.lsg_last_status()
     return out
+
+
+# ----------------------------------------------------------------------------- differentiation
+
+def _solve_for(precision: str, op: Operator, rhs, kw: dict):
+    import torch
+    if precision == "mixed":
+        return aar_mixed(op, rhs.to(torch.float64).contiguous(), **kw)
+    if precision == "fp64":
+        return aar(op, rhs.to(torch.float64).contiguous(), **kw)
+    if precision == "fp32":
+        return aar(op, rhs.to(torch.float32).contiguous(), **kw)
+    raise ValueError(precision)
+
+
+class _ShiftedSolve:
+    """x = A(sigma)^-1 b with A = a * Lap_h + sigma * I (real, symmetric).
+
+    Backward is the adjoint solve on the same kernels: A^T = A, so
+    lambda = A^-1 (dL/dx), dL/db = lambda and dL/dsigma = -lambda . x.
+    """
+
+    @staticmethod
+    def build():
+        import torch
+
+        class Fn(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, b, sigma, grid, radius, a, precision, kw):
+                s = float(sigma.detach().cpu()) if torch.is_tensor(sigma) else float(sigma)
+                op = Operator(grid, radius=radius, a=a, sigma=s)
+                x, info = _solve_for(precision, op, b.detach(), kw)
+                if info["status"] != 0:
+                    raise CudaLibraryError(f"forward solve: {info['status_name']} ({info})")
+                x = x.to(b.dtype)
+                ctx.op, ctx.precision, ctx.kw = op, precision, kw
+                ctx.sigma_is_tensor = torch.is_tensor(sigma)
+                ctx.sigma_dtype = sigma.dtype if torch.is_tensor(sigma) else torch.float64
+                ctx.save_for_backward(x)
+                return x
+
+            @staticmethod
+            def backward(ctx, gx):
+                (x,) = ctx.saved_tensors
+                lam, info = _solve_for(ctx.precision, ctx.op, gx.contiguous(), ctx.kw)
+                if info["status"] != 0:
+                    raise CudaLibraryError(f"adjoint solve: {info['status_name']} ({info})")
+                lam = lam.to(x.dtype)
+                gsig = None
+                if ctx.sigma_is_tensor and ctx.needs_input_grad[1]:
+                    gsig = -(lam.double() * x.double()).sum().to(ctx.sigma_dtype)
+                gb = lam if ctx.needs_input_grad[0] else None
+                return gb, gsig, None, None, None, None, None
+
+        return Fn
+
+
+_Fn = None
+
+
+def solve_shifted(b, sigma, *, a=A_REF, radius=6, precision="mixed", **kw):
+    """Differentiable x = (a Lap_h + sigma I)^-1 b on the periodic grid of b.
+
+    b: CUDA tensor (nz, ny, nx); sigma: float or 0-dim tensor (may require
+    grad).  precision: "mixed" (FP32 AAR + FP64 residual replacement), "fp64"
+    or "fp32" AAR.  kw: solver parameters (tol, m, p, omega, beta, ...).
+    """
+    global _Fn
+    if _Fn is None:
+        _Fn = _ShiftedSolve.build()
+    nz, ny, nx = b.shape
+    return _Fn.apply(b, sigma, (nx, ny, nz), radius, a, precision, dict(kw))
