@@ -45,6 +45,10 @@ WORKLOAD = ("256^3 periodic 12th-order FD Poisson (a = -1/(4 pi), FDn = 6, Jacob
 # bounded CPU sample.
 LARGE_GOLDEN = os.path.join(ROOT, "tests", "golden", "large_256.json")
 CPU_SAMPLE_ITERS = 24
+# DRAM bytes (read + write) of one launch of the dominant kernel at this
+# workload, from the ncu capture summarised in
+# profiles/richardson_f32_recurrence_256cube.md.
+RICH32_TRAFFIC_BYTES = 358.4e6
 
 
 def _peaks():
@@ -321,7 +325,8 @@ def run_lsg(args):
         "roofline": {"bound": "hbm", "kernel": "stencil_kernel<float, RichRecurOp> (fused Richardson step)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
-                     "traffic": None, "bytes_per_launch": rich_bytes, "avg_launch_ms": rich_ms,
+                     "traffic": RICH32_TRAFFIC_BYTES, "traffic_unit": "bytes per launch (ncu)",
+                     "bytes_per_launch": rich_bytes, "avg_launch_ms": rich_ms,
                      "share_of_kernel_time": rms / total_ms if total_ms else None},
         "kernel_profile_ms": {k: round(v[1] / args.steps, 4) for k, v in prof.items() if v[0]},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 2 * N * 8,
