@@ -40,8 +40,10 @@ typedef enum lsg_status {
 } lsg_status;
 
 typedef enum lsg_dtype {
-    LSG_F64 = 0, /* double vectors, FP64 arithmetic */
-    LSG_F32 = 1  /* float vectors and stencil; reductions and the m x m solve in FP64 */
+    LSG_F64 = 0,  /* double vectors, FP64 arithmetic */
+    LSG_F32 = 1,  /* float vectors and stencil; reductions and the m x m solve in FP64 */
+    LSG_C128 = 2, /* complex double (re, im interleaved) vectors; AAR only */
+    LSG_C64 = 3   /* complex float vectors; AAR only */
 } lsg_dtype;
 
 /* The operator.  coeff[] are the 1-D Laplacian FD coefficients c_0..c_radius
@@ -51,8 +53,11 @@ typedef struct lsg_operator {
     int radius;                        /* FDn, 1..LSG_MAX_RADIUS */
     double coeff[LSG_MAX_RADIUS + 1];  /* c_0..c_radius */
     double a;                          /* Laplacian scale (the reference passes -1/(4 pi)) */
-    double sigma;                      /* real diagonal shift; 0 = the reference operator */
+    double sigma;                      /* diagonal shift, real part; 0 = the reference operator */
     int precond;                       /* 1: Jacobi, f = r / (3 a c_0 + sigma); 0: none */
+    double sigma_im;                   /* imaginary part of the shift (complex dtypes only):
+                                          A = a Lap + (sigma + i sigma_im) I, the shifted
+                                          Helmholtz operator of PETSC_COMPLEX/system.c:209-272 */
 } lsg_operator;
 
 /* Solver parameters, named as the reference's arguments (MPI_REAL/AAR.h:18-22). */
@@ -108,7 +113,8 @@ int lsg_pl2r(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x
 int lsg_cg(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
            const void *d_b, lsg_result *res, void *stream);    /* MPI_REAL/CG.c:33 */
 
-/* Mixed precision: FP64 x and b.  One FP32 AAR (FP32 vectors, history and
+/* Mixed precision: FP64 x and b (lsg_aar_mixed_c: complex128 x and b with a
+ * complex64 inner iteration).  One FP32 AAR (FP32 vectors, history and
  * stencil; FP64-class reductions and m x m solve) runs on the correction;
  * each time its residual has dropped by inner_tol the correction is folded
  * into x (FP64), r = b - A x is recomputed in FP64 and the FP32 iteration
@@ -117,6 +123,8 @@ int lsg_cg(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
  * FP64 residual replacements. */
 int lsg_aar_mixed(const lsg_operator *op, const lsg_params *prm, double *d_x, const double *d_b,
                   lsg_result *res, void *stream);
+int lsg_aar_mixed_c(const lsg_operator *op, const lsg_params *prm, void *d_x, const void *d_b,
+                    lsg_result *res, void *stream);
 
 /* m x m pseudo-inverse solve with the reference's semantics
  * (x = V diag(1/w) V^T b, w < m*wmax*2.22044605e-16 dropped; MPI_REAL/tools.c:52-105),

@@ -22,6 +22,8 @@ int solve(int solver, const lsg_operator *op, const lsg_params *prm, int dtype, 
           const void *d_b, lsg_result *res, cudaStream_t s);
 int solve_mixed(const lsg_operator *op, const lsg_params *prm, double *x, const double *b,
                 lsg_result *res, cudaStream_t s);
+int solve_mixed_c(const lsg_operator *op, const lsg_params *prm, void *x, const void *b,
+                  lsg_result *res, cudaStream_t s);
 int apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, cudaStream_t s);
 int pinv(const double *A, const double *b, double *x, int m, cudaStream_t s);
 int release_workspaces();

@@ -8,6 +8,7 @@
 #include <stdint.h>
 
 #include "../../include/lsg.h"
+#include "lsg_complex.cuh"
 
 namespace lsg {
 
@@ -50,6 +51,11 @@ inline Geom make_geom(const int n[3]) {
     g.n = g.nxy * n[2];
     return g;
 }
+
+// Host-side scalar of a vector type: double for real vectors, cplx<double>
+// for complex ones (the complex shift, Jacobi factor and Anderson weights).
+template <typename T> struct ScalarOf { using type = double; };
+template <typename R> struct ScalarOf<cplx<R>> { using type = cplx<double>; };
 
 // Stencil weights in the arithmetic type: w[0] = 3*a*c_0 + sigma (centre),
 // w[p] = a*c_p.  Passed by value (kernel parameter space).
@@ -132,6 +138,8 @@ struct StencilLaunch {
 template <typename T> struct TileOf;
 template <> struct TileOf<double> { static constexpr int BY = 8, NY = 2, MINB = 1; };
 template <> struct TileOf<float> { static constexpr int BY = 4, NY = 4, MINB = 4; };
+template <> struct TileOf<cplx<double>> { static constexpr int BY = 8, NY = 1, MINB = 1; };
+template <> struct TileOf<cplx<float>> { static constexpr int BY = 8, NY = 2, MINB = 2; };
 
 inline dim3 stencil_grid(const Geom &g, int ty, int lz) {
     return dim3((unsigned)((g.nx + 31) / 32), (unsigned)((g.ny + ty - 1) / ty),
@@ -163,37 +171,39 @@ inline long long stencil_blocks(const Geom &g, int lz) {
 
 template <typename T>
 struct Kernels {
+    using S = typename ScalarOf<T>::type;
     // Resident blocks per SM of the fused Richardson stencil kernel.
     static int stencil_blocks_per_sm();
     // y / r update driven by one stencil pass over x.  RES_ANDERSON also
     // completes the history column hc (holding x_new - x_old) with hb * DF_col.
     static cudaError_t residual(const StencilLaunch &L, const Weights<T> &w, int mode,
-                                const T *x, const T *b, T *r, T *df, T *hc, double cf, double hb,
+                                const T *x, const T *b, T *r, T *df, T *hc, S cf, double hb,
                                 double *partials, const DevCtrl *ctrl);
     // Fused Richardson step: u = x + c*r at every stencil point; r2 = b - A u;
     // x2 = u; DF per mode; history column dx = (u - x) + hb * DF.
     static cudaError_t richardson(const StencilLaunch &L, const Weights<T> &w, int mode,
                                   const T *x, const T *r, const T *b, T *x2, T *r2, T *dx,
-                                  T *df, double c, double cf, double hb, const DevCtrl *ctrl);
+                                  T *df, S c, S cf, double hb, const DevCtrl *ctrl);
     // Residual-recurrence Richardson step (FP32 inner solver): r2 = r - c A r,
     // x += c r in place, DF = (r2 - r) cf, H = (x_new - x_old) + hb DF.
     static cudaError_t richardson_recur(const StencilLaunch &L, const Weights<T> &w, const T *r,
-                                        T *x, T *r2, T *dx, T *df, double c, double cf,
-                                        double hb, const DevCtrl *ctrl);
+                                        T *x, T *r2, T *dx, T *df, S c, S cf, double hb,
+                                        const DevCtrl *ctrl);
     // Extrapolation-step residual by recurrence: r -= A step; DF = (r_new - r) cf;
     // H_col = step + hb DF; ||r||^2.
     static cudaError_t residual_recur(const StencilLaunch &L, const Weights<T> &w, const T *step,
-                                      T *r, T *df, T *hc, double cf, double hb,
-                                      double *partials, const DevCtrl *ctrl);
+                                      T *r, T *df, T *hc, S cf, double hb, double *partials,
+                                      const DevCtrl *ctrl);
     // Grid of one Gram launch (one wave); partials written = grid * values.
     static int gram_grid(int kind, int m, long long n, int sms);
-    // Gram partials over the history (point-local, grid-stride).
+    // Gram partials over the history (point-local, grid-stride).  Complex
+    // vectors: G(i,j) = DF_i^H DF_j, h_j = DF_j^H r (PETSC_COMPLEX/AAR_Complex.c:213-216).
     static cudaError_t gram(int kind, int m, const T *dx, const T *df, const T *r, long long n,
                             double *partials, int blocks, const DevCtrl *ctrl, cudaStream_t s);
     // AAR extrapolation: x += beta*f - sum_j H_j s_j with f = r*cf and
     // H_j = DX_j + beta DF_j; step = x_new - x_old.
     static cudaError_t aar_update(int m, T *x, const T *r, const T *h, T *step, double beta,
-                                  double cf, long long n, const DevCtrl *ctrl, cudaStream_t s);
+                                  S cf, long long n, const DevCtrl *ctrl, cudaStream_t s);
     // PGR/PL2R projection: tx = DX s, tf = DF s; x += tx; r -= tf; DX_col += tx;
     // DF_col += tf; partial ||r||^2.
     static cudaError_t proj_update(int m, int col, T *x, T *r, T *dx, T *df, long long n,
@@ -207,19 +217,21 @@ struct Kernels {
     static cudaError_t cg_step(T *x, T *r, const T *d, const T *q, long long n, int restart,
                                double *partials, int blocks, const DevCtrl *ctrl,
                                cudaStream_t s);
-    // partial ||v||^2 (grid-stride)
+    // partial ||v||^2 (grid-stride); complex vectors write (||v||^2, 0) pairs
     static cudaError_t norm2(const T *v, long long n, double *partials, int blocks,
                              const DevCtrl *ctrl, cudaStream_t s);
     // x += alpha*y  (alpha from the host)
     static cudaError_t axpy(T *x, const T *y, double alpha, long long n, cudaStream_t s);
 };
 
-// Mixed-precision helpers (lsg_kernels.cu).
+// Mixed-precision helpers (lsg_kernels_f64.cu, lsg_kernels_c128.cu).
 // r32 = float(b - A x64), partial ||b - A x64||^2 (FP64 stencil).
-cudaError_t ir_residual(const StencilLaunch &L, const Weights<double> &w, const double *x,
-                        const double *b, float *r32, double *partials, const DevCtrl *ctrl);
+template <typename T64, typename T32>
+cudaError_t ir_residual(const StencilLaunch &L, const Weights<T64> &w, const T64 *x,
+                        const T64 *b, T32 *r32, double *partials, const DevCtrl *ctrl);
 // x64 += e32; e32 = 0
-cudaError_t ir_correct(double *x, float *e, long long n, cudaStream_t s);
+template <typename T64, typename T32>
+cudaError_t ir_correct(T64 *x, T32 *e, long long n, cudaStream_t s);
 
 // Finalize kernels (lsg_small.cu).
 enum NormFinal {
@@ -227,12 +239,18 @@ enum NormFinal {
     NF_CHECK = 1,     // relres = sqrt(sum); done if relres <= tol_abs (iters = iter)
     NF_STORE = 2,     // relres = sqrt(sum) only
 };
+// `width` = reals per partial (1 real, 2 complex: the norm is the real part).
 cudaError_t finalize_norm(const double *partials, int nparts, DevCtrl *ctrl, int mode,
-                          double tol, int iter, cudaStream_t s);
+                          double tol, int iter, cudaStream_t s, int width = 1);
 // Sums Gram partials, assembles G (m x m) and h (m), solves s = pinv(G) h with
 // the reference semantics into ctrl->s.  hscale multiplies h.
 cudaError_t finalize_gram_solve(const double *partials, int nparts, int kind, int m,
                                 double hscale, DevCtrl *ctrl, cudaStream_t s);
+// Complex Hermitian variant: G(i,j) = DF_i^H DF_j, h = hscale * DF^H r; solved
+// as its real 2m x 2m representation with zgelsd's cutoff (eps * sigma_max,
+// PETSC_COMPLEX/AAR_Complex.c:239); ctrl->s holds (re, im) pairs, m <= 16.
+cudaError_t finalize_gram_solve_c(const double *partials, int nparts, int m, cplx<double> hscale,
+                                  DevCtrl *ctrl, cudaStream_t s);
 // CG scalars: mode 0: alpha = delta / sum(d.q).  mode 1: delta_new = cf*sum(r.r),
 // relres = sqrt(sum r.r), beta = delta_new/delta_old, convergence test.
 cudaError_t finalize_cg(const double *partials, int nparts, DevCtrl *ctrl, int mode, double cf,

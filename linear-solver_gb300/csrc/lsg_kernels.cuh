@@ -23,6 +23,17 @@ __device__ __forceinline__ bool solve_done(const DevCtrl *c) {
     return c != nullptr && *(volatile const int *)&c->done;
 }
 
+// j-th extrapolation coefficient from the m x m solve (complex: (re, im) pairs).
+template <typename T>
+__device__ __forceinline__ T ctrl_s(const DevCtrl *c, int j) {
+    if constexpr (IsCplx<T>::value) {
+        using R = typename RealOf<T>::type;
+        return T((R)c->s[2 * j], (R)c->s[2 * j + 1]);
+    } else {
+        return (T)c->s[j];
+    }
+}
+
 // ---------------------------------------------------------------- stencil functors
 
 template <typename T> struct Pair { T a, b; };
@@ -207,25 +218,26 @@ struct CgDirOp {
     }
 };
 
-// FP64 refinement residual: r32 = float(b - A x), ||b - A x||^2 in FP64.
+// FP64 refinement residual: r32 = float(b - A x), ||b - A x||^2 in FP64
+// (T64 / T32: double / float or their complex forms).
+template <typename T64, typename T32>
 struct IrResidualOp {
     static constexpr int NACC = 1;
-    using Raw = double;
-    using Ctr = double;  // b
-    const double *x;
-    const double *b;
-    float *r32;
+    using Raw = T64;
+    using Ctr = T64;  // b
+    const T64 *x;
+    const T64 *b;
+    T32 *r32;
     double *partials;
     const DevCtrl *ctrl;
     __device__ bool skip() const { return solve_done(ctrl); }
     __device__ void init() {}
     __device__ __forceinline__ Raw fetch(unsigned i) const { return ldg(x + i); }
-    __device__ __forceinline__ double value(const Raw &v) const { return v; }
+    __device__ __forceinline__ T64 value(const Raw &v) const { return v; }
     __device__ __forceinline__ Ctr fetch_center(unsigned i) const { return ldg(b + i); }
-    __device__ __forceinline__ void store(unsigned i, double, double au, const Ctr &bb,
-                                          Acc<double> *acc) const {
-        const double rn = bb - au;
-        r32[i] = (float)rn;
+    __device__ __forceinline__ void store(unsigned i, T64, T64 au, const Ctr &bb, Acc<T64> *acc) const {
+        const T64 rn = bb - au;
+        r32[i] = (T32)rn;
         acc[0].add_prod(rn, rn);
     }
 };
@@ -332,7 +344,7 @@ __global__ void __launch_bounds__(kReduceThreads) gram_kernel(const T *__restric
             for (int j = 0; j < M; j++) accv(acc[NP + j], xv[j], rv);
         }
     }
-    block_reduce_store<NV, T>(acc, red, partials + (long long)blockIdx.x * NV);
+    block_reduce_store<NV>(acc, red, partials + (long long)blockIdx.x * NV);
 }
 
 // Generic Gram (any m <= LSG_MAX_M): one value per (block, thread-slot), the
@@ -345,7 +357,7 @@ __global__ void __launch_bounds__(kReduceThreads) gram_generic_kernel(int kind, 
                                                                       long long n, int nv,
                                                                       double *partials,
                                                                       const DevCtrl *ctrl) {
-    __shared__ double red[kReduceThreads / 32];
+    __shared__ double red[(kReduceThreads / 32) * AccWidth<T>::value];
     if (solve_done(ctrl)) return;
     const int v = blockIdx.y;  // value index
     const int np = kind == GRAM_SYM ? (m * (m + 1)) / 2 : m * m;
@@ -371,7 +383,7 @@ __global__ void __launch_bounds__(kReduceThreads) gram_generic_kernel(int kind, 
         acc.add_prod(ldg(u + i), ldg(w + i));
     __shared__ double out;
     Acc<T> a1[1] = {acc};
-    block_reduce_store<1, T>(a1, red, &out);
+    block_reduce_store<1>(a1, red, &out);
     __syncthreads();
     if (threadIdx.x == 0) partials[(long long)blockIdx.x * nv + v] = out;
 }
@@ -390,7 +402,7 @@ __global__ void __launch_bounds__(kReduceThreads) aar_update_kernel(int m, T *__
                                                                     const DevCtrl *ctrl) {
     __shared__ T s[LSG_MAX_M];
     if (solve_done(ctrl)) return;
-    if (threadIdx.x < m) s[threadIdx.x] = (T)ctrl->s[threadIdx.x];
+    if (threadIdx.x < m) s[threadIdx.x] = ctrl_s<T>(ctrl, threadIdx.x);
     __syncthreads();
     const long long stride = (long long)gridDim.x * blockDim.x;
     if constexpr (M > 0) {
@@ -445,9 +457,9 @@ __global__ void __launch_bounds__(kReduceThreads) proj_update_kernel(int m, T *_
                                                                      double *partials,
                                                                      const DevCtrl *ctrl) {
     __shared__ T s[LSG_MAX_M];
-    __shared__ double red[kReduceThreads / 32];
+    __shared__ double red[(kReduceThreads / 32) * AccWidth<T>::value];
     if (solve_done(ctrl)) return;
-    if (threadIdx.x < m) s[threadIdx.x] = (T)ctrl->s[threadIdx.x];
+    if (threadIdx.x < m) s[threadIdx.x] = ctrl_s<T>(ctrl, threadIdx.x);
     __syncthreads();
     Acc<T> acc;
     acc.zero();
@@ -466,7 +478,7 @@ __global__ void __launch_bounds__(kReduceThreads) proj_update_kernel(int m, T *_
         acc.add_prod(rn, rn);
     }
     Acc<T> a1[1] = {acc};
-    block_reduce_store<1, T>(a1, red, partials + blockIdx.x);
+    block_reduce_store<1>(a1, red, partials + blockIdx.x);
 }
 
 template <typename T>
@@ -477,7 +489,7 @@ __global__ void __launch_bounds__(kReduceThreads) cg_step_kernel(T *__restrict__
                                                                  long long n, int restart,
                                                                  double *partials,
                                                                  const DevCtrl *ctrl) {
-    __shared__ double red[kReduceThreads / 32];
+    __shared__ double red[(kReduceThreads / 32) * AccWidth<T>::value];
     if (solve_done(ctrl)) return;
     const T alpha = (T)ctrl->alpha;
     Acc<T> acc;
@@ -493,7 +505,7 @@ __global__ void __launch_bounds__(kReduceThreads) cg_step_kernel(T *__restrict__
     }
     if (!restart) {
         Acc<T> a1[1] = {acc};
-        block_reduce_store<1, T>(a1, red, partials + blockIdx.x);
+        block_reduce_store<1>(a1, red, partials + blockIdx.x);
     }
 }
 
@@ -501,7 +513,7 @@ template <typename T>
 __global__ void __launch_bounds__(kReduceThreads) norm2_kernel(const T *__restrict__ v, long long n,
                                                                double *partials,
                                                                const DevCtrl *ctrl) {
-    __shared__ double red[kReduceThreads / 32];
+    __shared__ double red[(kReduceThreads / 32) * AccWidth<T>::value];
     if (solve_done(ctrl)) return;
     Acc<T> acc;
     acc.zero();
@@ -511,7 +523,7 @@ __global__ void __launch_bounds__(kReduceThreads) norm2_kernel(const T *__restri
         acc.add_prod(a, a);
     }
     Acc<T> a1[1] = {acc};
-    block_reduce_store<1, T>(a1, red, partials + blockIdx.x);
+    block_reduce_store<1>(a1, red, partials + blockIdx.x * AccWidth<T>::value);
 }
 
 template <typename T>
@@ -525,19 +537,19 @@ __global__ void axpy_kernel(T *__restrict__ x, const T *__restrict__ y, T alpha,
 
 template <typename T>
 cudaError_t Kernels<T>::residual(const StencilLaunch &L, const Weights<T> &w, int mode,
-                                 const T *x, const T *b, T *r, T *df, T *hc, double cf, double hb,
+                                 const T *x, const T *b, T *r, T *df, T *hc, S cf, double hb,
                                  double *partials, const DevCtrl *ctrl) {
     switch (mode) {
     case RES_INIT: {
-        ResidualOp<T, RES_INIT> op{x, b, r, df, nullptr, (T)cf, T(0), partials, ctrl};
+        ResidualOp<T, RES_INIT> op{x, b, r, df, nullptr, (T)cf, T(0.0), partials, ctrl};
         return launch_stencil<T>(L, w, op);
     }
     case RES_ANDERSON: {
-        ResidualOp<T, RES_ANDERSON> op{x, b, r, df, hc, (T)cf, (T)hb, partials, ctrl};
+        ResidualOp<T, RES_ANDERSON> op{x, b, r, df, hc, (T)cf, T(hb), partials, ctrl};
         return launch_stencil<T>(L, w, op);
     }
     default: {
-        ResidualOp<T, RES_APPLY> op{x, b, r, df, nullptr, (T)cf, T(0), partials, ctrl};
+        ResidualOp<T, RES_APPLY> op{x, b, r, df, nullptr, (T)cf, T(0.0), partials, ctrl};
         return launch_stencil<T>(L, w, op);
     }
     }
@@ -546,29 +558,60 @@ cudaError_t Kernels<T>::residual(const StencilLaunch &L, const Weights<T> &w, in
 template <typename T>
 cudaError_t Kernels<T>::richardson(const StencilLaunch &L, const Weights<T> &w, int mode,
                                    const T *x, const T *r, const T *b, T *x2, T *r2, T *dx,
-                                   T *df, double c, double cf, double hb, const DevCtrl *ctrl) {
+                                   T *df, S c, S cf, double hb, const DevCtrl *ctrl) {
     if (mode == RICH_AAR) {
-        RichOp<T, RICH_AAR> op{x, r, b, x2, r2, dx, df, (T)c, (T)cf, (T)hb, nullptr, ctrl};
+        RichOp<T, RICH_AAR> op{x, r, b, x2, r2, dx, df, (T)c, (T)cf, T(hb), nullptr, ctrl};
         return launch_stencil<T>(L, w, op);
     }
-    RichOp<T, RICH_PGR> op{x, r, b, x2, r2, dx, df, (T)c, (T)cf, T(0), nullptr, ctrl};
+    RichOp<T, RICH_PGR> op{x, r, b, x2, r2, dx, df, (T)c, (T)cf, T(0.0), nullptr, ctrl};
     return launch_stencil<T>(L, w, op);
 }
 
 template <typename T>
 cudaError_t Kernels<T>::richardson_recur(const StencilLaunch &L, const Weights<T> &w, const T *r,
-                                         T *x, T *r2, T *dx, T *df, double c, double cf,
-                                         double hb, const DevCtrl *ctrl) {
-    RichRecurOp<T> op{r, x, r2, dx, df, (T)c, (T)cf, (T)hb, nullptr, ctrl};
+                                         T *x, T *r2, T *dx, T *df, S c, S cf, double hb,
+                                         const DevCtrl *ctrl) {
+    RichRecurOp<T> op{r, x, r2, dx, df, (T)c, (T)cf, T(hb), nullptr, ctrl};
     return launch_stencil<T>(L, w, op);
 }
 
 template <typename T>
 cudaError_t Kernels<T>::residual_recur(const StencilLaunch &L, const Weights<T> &w, const T *step,
-                                       T *r, T *df, T *hc, double cf, double hb,
-                                       double *partials, const DevCtrl *ctrl) {
-    ResRecurOp<T> op{step, r, df, hc, (T)cf, (T)hb, partials, ctrl};
+                                       T *r, T *df, T *hc, S cf, double hb, double *partials,
+                                       const DevCtrl *ctrl) {
+    ResRecurOp<T> op{step, r, df, hc, (T)cf, T(hb), partials, ctrl};
     return launch_stencil<T>(L, w, op);
+}
+
+// Hermitian Gram for complex vectors (PETSC_COMPLEX/AAR_Complex.c:213-216):
+// G(a,j) = DF_a^H DF_j (a <= j), h_j = DF_j^H r; M compile-time history depth.
+template <typename R, int M>
+__global__ void __launch_bounds__(kReduceThreads) gram_c_kernel(const cplx<R> *__restrict__ df,
+                                                                const cplx<R> *__restrict__ r,
+                                                                long long n, double *partials,
+                                                                const DevCtrl *ctrl) {
+    constexpr int NP = (M * (M + 1)) / 2;
+    constexpr int NV = NP + M;
+    __shared__ double red[2 * NV * (kReduceThreads / 32)];
+    if (solve_done(ctrl)) return;
+    Acc<cplx<R>> acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) acc[k].zero();
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        cplx<R> f[M];
+#pragma unroll
+        for (int j = 0; j < M; j++) f[j] = ldg(df + j * n + i);
+        const cplx<R> rv = ldg(r + i);
+        int k = 0;
+#pragma unroll
+        for (int j = 0; j < M; j++)
+#pragma unroll
+            for (int a = 0; a <= j; a++) { acc[k].add_prod(f[a], f[j]); k++; }
+#pragma unroll
+        for (int j = 0; j < M; j++) acc[NP + j].add_prod(f[j], rv);
+    }
+    block_reduce_store<NV>(acc, red, partials + (long long)blockIdx.x * 2 * NV);
 }
 
 template <typename T, int KIND>
@@ -596,7 +639,10 @@ template <typename T>
 int Kernels<T>::gram_grid(int kind, int m, long long n, int sms) {
     static int cache[2][LSG_MAX_M + 1];
     int &occ = cache[kind == GRAM_SYM ? 0 : 1][m];
-    if (occ == 0) {
+    if constexpr (IsCplx<T>::value) {
+        (void)kind;
+        if (occ == 0) occ = 1;
+    } else if (occ == 0) {
         int v = 0;
         cudaError_t e = cudaSuccess;
         switch (m) {
@@ -621,22 +667,41 @@ int Kernels<T>::gram_grid(int kind, int m, long long n, int sms) {
 template <typename T>
 cudaError_t Kernels<T>::gram(int kind, int m, const T *dx, const T *df, const T *r, long long n,
                              double *partials, int blocks, const DevCtrl *ctrl, cudaStream_t s) {
+    if constexpr (IsCplx<T>::value) {
+        using R = typename RealOf<T>::type;
+        (void)kind;
+        (void)dx;
+        switch (m) {
+#define LSG_GRAMC_CASE(MM) \
+    case MM: gram_c_kernel<R, MM><<<blocks, kReduceThreads, 0, s>>>(df, r, n, partials, ctrl); break;
+            LSG_GRAMC_CASE(1) LSG_GRAMC_CASE(2) LSG_GRAMC_CASE(3) LSG_GRAMC_CASE(4)
+            LSG_GRAMC_CASE(5) LSG_GRAMC_CASE(6) LSG_GRAMC_CASE(7) LSG_GRAMC_CASE(8)
+#undef LSG_GRAMC_CASE
+        default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    } else {
     if (kind == GRAM_SYM) return gram_dispatch<T, GRAM_SYM>(m, dx, df, r, n, partials, blocks, ctrl, s);
     return gram_dispatch<T, GRAM_GALERKIN>(m, dx, df, r, n, partials, blocks, ctrl, s);
+    }
 }
 
 template <typename T>
 cudaError_t Kernels<T>::aar_update(int m, T *x, const T *r, const T *h, T *step, double beta,
-                                   double cf, long long n, const DevCtrl *ctrl, cudaStream_t s) {
+                                   S cf, long long n, const DevCtrl *ctrl, cudaStream_t s) {
     const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 8);
-    const bool vec = n % Vec4<T>::N == 0;
-    switch (vec ? m : 0) {
+    if constexpr (IsCplx<T>::value) {
+        aar_update_kernel<T, 0><<<blocks, kReduceThreads, 0, s>>>(m, x, r, h, step, T(beta), (T)cf, n, ctrl);
+    } else {
+        const bool vec = n % Vec4<T>::N == 0;
+        switch (vec ? m : 0) {
 #define LSG_UPD_CASE(MM) \
     case MM: aar_update_kernel<T, MM><<<blocks, kReduceThreads, 0, s>>>(m, x, r, h, step, (T)beta, (T)cf, n, ctrl); break;
-        LSG_UPD_CASE(1) LSG_UPD_CASE(2) LSG_UPD_CASE(3) LSG_UPD_CASE(4)
-        LSG_UPD_CASE(5) LSG_UPD_CASE(6) LSG_UPD_CASE(7) LSG_UPD_CASE(8)
+            LSG_UPD_CASE(1) LSG_UPD_CASE(2) LSG_UPD_CASE(3) LSG_UPD_CASE(4)
+            LSG_UPD_CASE(5) LSG_UPD_CASE(6) LSG_UPD_CASE(7) LSG_UPD_CASE(8)
 #undef LSG_UPD_CASE
-    default: aar_update_kernel<T, 0><<<blocks, kReduceThreads, 0, s>>>(m, x, r, h, step, (T)beta, (T)cf, n, ctrl);
+        default: aar_update_kernel<T, 0><<<blocks, kReduceThreads, 0, s>>>(m, x, r, h, step, (T)beta, (T)cf, n, ctrl);
+        }
     }
     return cudaGetLastError();
 }
@@ -676,6 +741,30 @@ template <typename T>
 cudaError_t Kernels<T>::axpy(T *x, const T *y, double alpha, long long n, cudaStream_t s) {
     const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 8);
     axpy_kernel<T><<<blocks, kReduceThreads, 0, s>>>(x, y, (T)alpha, n);
+    return cudaGetLastError();
+}
+
+template <typename T64, typename T32>
+cudaError_t ir_residual(const StencilLaunch &L, const Weights<T64> &w, const T64 *x,
+                        const T64 *b, T32 *r32, double *partials, const DevCtrl *ctrl) {
+    IrResidualOp<T64, T32> op{x, b, r32, partials, ctrl};
+    return launch_stencil<T64>(L, w, op);
+}
+
+// x64 += e32; e32 = 0 (the correction is folded into x and restarts at zero).
+template <typename T64, typename T32>
+__global__ void ir_correct_kernel(T64 *__restrict__ x, T32 *__restrict__ e, long long n) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        x[i] += (T64)e[i];
+        e[i] = T32(0.0);
+    }
+}
+
+template <typename T64, typename T32>
+cudaError_t ir_correct(T64 *x, T32 *e, long long n, cudaStream_t s) {
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 8);
+    ir_correct_kernel<T64, T32><<<blocks, kReduceThreads, 0, s>>>(x, e, n);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,16 @@
+// complex128 instantiation of the AAR kernels (shifted Helmholtz), plus the
+// complex128 pieces of the mixed-precision solver.
+#include "lsg_kernels.cuh"
+
+namespace lsg {
+
+template struct Kernels<cplx<double>>;
+template cudaError_t ir_residual<cplx<double>, cplx<float>>(const StencilLaunch &,
+                                                            const Weights<cplx<double>> &,
+                                                            const cplx<double> *,
+                                                            const cplx<double> *, cplx<float> *,
+                                                            double *, const DevCtrl *);
+template cudaError_t ir_correct<cplx<double>, cplx<float>>(cplx<double> *, cplx<float> *, long long,
+                                                           cudaStream_t);
+
+}  // namespace lsg

@@ -48,10 +48,10 @@ __device__ double block_sum_partials(const double *partials, int nparts, int str
 }
 
 __global__ void finalize_norm_kernel(const double *partials, int nparts, DevCtrl *ctrl, int mode,
-                                     double tol, int iter) {
+                                     double tol, int iter, int width) {
     __shared__ double red[32];
     if (mode != NF_RHS && ctrl_done(ctrl)) return;
-    const double s = block_sum_partials(partials, nparts, 1, 0, red);
+    const double s = block_sum_partials(partials, nparts, width, 0, red);
     if (threadIdx.x != 0) return;
     const double v = sqrt(s);
     if (mode == NF_RHS) {
@@ -91,7 +91,7 @@ constexpr double kJacobiTol = 8 * kPinvEps;
 // x = V diag(1/w) V^T b from the converged G = A V (lane j of the warp owns
 // column j); shared by both Jacobi variants.  ld: leading dimension of G, V.
 __device__ void pinv_apply(const double *G, const double *V, int ld, const double *b, double *x,
-                           int m, double scale) {
+                           int m, double scale, double cut) {
     const int lane = threadIdx.x & 31;
     double w = 0.0;
     if (lane < m) {
@@ -101,7 +101,7 @@ __device__ void pinv_apply(const double *G, const double *V, int ld, const doubl
     double wmax = lane < m ? w : 0.0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) wmax = fmax(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
-    const double wmin = m * wmax * kPinvEps;
+    const double wmin = cut * wmax;
     double tj = 0.0;  // (V^T b)_j / w_j on lane j
     if (lane < m && w >= wmin && w > 0.0) {
         for (int i = 0; i < m; i++) tj = fma(V[i * ld + lane], b[i], tj);
@@ -118,7 +118,7 @@ __device__ void pinv_apply(const double *G, const double *V, int ld, const doubl
 // General case, m <= 32: one warp, lane k owns row k, column pairs visited
 // cyclically with the rotation computed in FP64.  Returns 0 on convergence,
 // LSG_SVD_NO_CONVERGENCE otherwise.
-__device__ int warp_pinv(double *G, double *V, const double *b, double *x, int m) {
+__device__ int warp_pinv(double *G, double *V, const double *b, double *x, int m, double cut) {
     const int lane = threadIdx.x & 31;
     for (int i = lane; i < m * m; i += 32) V[i] = (i / m == i % m) ? 1.0 : 0.0;
     __syncwarp();
@@ -156,7 +156,7 @@ __device__ int warp_pinv(double *G, double *V, const double *b, double *x, int m
             }
         }
     }
-    pinv_apply(G, V, m, b, x, m, 1.0);
+    pinv_apply(G, V, m, b, x, m, 1.0, cut);
     return rotated ? LSG_SVD_NO_CONVERGENCE : 0;
 }
 
@@ -170,7 +170,7 @@ __device__ int warp_pinv(double *G, double *V, const double *b, double *x, int m
 // slightly non-orthogonal is finished by the next sweep.  Pairs whose FP32
 // angle would underflow use the FP64 formula.  G, V: 8 x 8, row-major, ld 8,
 // rows and columns >= m zero.
-__device__ int warp_pinv8(double *G, double *V, const double *b, double *x, int m) {
+__device__ int warp_pinv8(double *G, double *V, const double *b, double *x, int m, double cut) {
     const int lane = threadIdx.x & 31;
     const int q = lane >> 3, row = lane & 7;
     const int M2 = m + (m & 1);
@@ -245,7 +245,7 @@ __device__ int warp_pinv8(double *G, double *V, const double *b, double *x, int 
         }
         any = __any_sync(0xffffffffu, rotated);
     }
-    pinv_apply(G, V, 8, b, x, m, ldexp(1.0, -e));
+    pinv_apply(G, V, 8, b, x, m, ldexp(1.0, -e), cut);
     return any ? LSG_SVD_NO_CONVERGENCE : 0;
 }
 
@@ -269,7 +269,7 @@ __device__ __forceinline__ double rcp_newton(double d) {
 // Jacobi SVD) when G is not of that kind.  G: m x m row-major (ld m) in shared
 // memory; Ls, Wi: m x m shared scratch; dd: m doubles.  One warp.
 __device__ bool warp_ldl_solve(const double *G, const double *h, double *x, int m, double *Ls,
-                               double *Wi, double *dd) {
+                               double *Wi, double *dd, double cut) {
     const int lane = threadIdx.x & 31;
     const unsigned full = 0xffffffffu;
     bool act = false, bad = false;
@@ -335,7 +335,7 @@ __device__ bool warp_ldl_solve(const double *G, const double *h, double *x, int 
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) tri += __shfl_xor_sync(full, tri, o);
-    if (!(trg * tri * (100.0 * m * kPinvEps) < 1.0)) return false;
+    if (!(trg * tri * (100.0 * cut) < 1.0)) return false;
     // Solve L z = h, z /= d, L^T x = z.
     double sv = (lane < m && act) ? h[lane] : 0.0;
     for (int t = 0; t < m; t++) {
@@ -356,7 +356,7 @@ __device__ bool warp_ldl_solve(const double *G, const double *h, double *x, int 
 // Dispatch on m; G (m x m row-major) is overwritten.  Gs / Vs: 8 x 8 staging
 // for the fast path.  Called by one full warp.
 __device__ int warp_pinv_any(double *G, double *V, const double *b, double *x, int m, double *Gs,
-                             double *Vs) {
+                             double *Vs, double cut) {
     const int lane = threadIdx.x & 31;
     if (m <= 8) {
         for (int k = lane; k < 64; k += 32) {
@@ -364,9 +364,9 @@ __device__ int warp_pinv_any(double *G, double *V, const double *b, double *x, i
             Gs[k] = (r < m && c < m) ? G[r * m + c] : 0.0;
         }
         __syncwarp();
-        return warp_pinv8(Gs, Vs, b, x, m);
+        return warp_pinv8(Gs, Vs, b, x, m, cut);
     }
-    return warp_pinv(G, V, b, x, m);
+    return warp_pinv(G, V, b, x, m, cut);
 }
 
 __global__ void finalize_gram_solve_kernel(const double *partials, int nparts, int kind, int m,
@@ -413,10 +413,11 @@ __global__ void finalize_gram_solve_kernel(const double *partials, int nparts, i
         int st = 0;
         if (!bad) {
             // symmetric PSD Gram: LDL^T when provably equal to the truncated pinv
-            const bool fast = kind == GRAM_SYM && warp_ldl_solve(G, h, s, m, V, Gs + 0, dd);
+            const double cut = m * kPinvEps;  // MPI_REAL/tools.c:331-335
+            const bool fast = kind == GRAM_SYM && warp_ldl_solve(G, h, s, m, V, Gs + 0, dd, cut);
             if (!fast) {
                 if (kind == GRAM_SYM && threadIdx.x == 0) ctrl->svd_fallbacks++;
-                st = warp_pinv_any(G, V, h, s, m, Gs, Vs);
+                st = warp_pinv_any(G, V, h, s, m, Gs, Vs, cut);
             }
         }
         __syncwarp();
@@ -424,6 +425,76 @@ __global__ void finalize_gram_solve_kernel(const double *partials, int nparts, i
         if (threadIdx.x == 0) {
             if (bad) { ctrl->status = LSG_NAN_DETECTED; ctrl->done = 1; }
             else if (st) ctrl->status = st;  // reported, the solve continues
+        }
+    }
+}
+
+// Complex Hermitian Gram: sums the (re, im) partials, builds the real 2m x 2m
+// representation [[A, -B], [B, A]] of G = A + iB (same singular values, each
+// twice) and right-hand side [Re h; Im h], and solves it with zgelsd's cutoff
+// sigma < eps * sigma_max (PETSC_COMPLEX/AAR_Complex.c:239, rcond = -1).
+__global__ void finalize_gram_solve_c_kernel(const double *partials, int nparts, int m, double hre,
+                                             double him, DevCtrl *ctrl) {
+    constexpr int M2MAX = LSG_MAX_M;
+    __shared__ double vals[2 * (LSG_MAX_M * LSG_MAX_M + LSG_MAX_M)];
+    __shared__ double G[M2MAX * M2MAX], V[M2MAX * M2MAX], W[M2MAX * M2MAX];
+    __shared__ double Gs[64], Vs[64];
+    __shared__ double h[M2MAX], s[M2MAX], dd[M2MAX];
+    __shared__ int bad;
+    if (ctrl_done(ctrl)) return;
+    const int np = (m * (m + 1)) / 2;
+    const int nvr = 2 * (np + m);  // reals per block partial
+    const int m2 = 2 * m;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int v = warp; v < nvr; v += nw) {
+            double t = 0.0;
+            for (int k = lane; k < nparts; k += 32) t += partials[(long long)k * nvr + v];
+            t = warp_sum(t);
+            if (lane == 0) {
+                vals[v] = t;
+                if (!isfinite(t)) bad = 1;
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        for (int k = threadIdx.x; k < np; k += 32) {
+            int j = 0;
+            while ((j + 1) * (j + 2) / 2 <= k) j++;
+            const int a = k - j * (j + 1) / 2;
+            const double re = vals[2 * k];  // G(a, j) = DF_a^H DF_j, real on the diagonal
+            const double im = a == j ? 0.0 : vals[2 * k + 1];
+            // A(a,j) = re, B(a,j) = im; A(j,a) = re, B(j,a) = -im
+            G[a * m2 + j] = re;           G[j * m2 + a] = re;
+            G[(a + m) * m2 + j + m] = re; G[(j + m) * m2 + a + m] = re;
+            G[a * m2 + j + m] = -im;      G[j * m2 + a + m] = im;
+            G[(a + m) * m2 + j] = im;     G[(j + m) * m2 + a] = -im;
+        }
+        for (int j = threadIdx.x; j < m; j += 32) {
+            const double re = vals[2 * (np + j)], im = vals[2 * (np + j) + 1];
+            h[j] = hre * re - him * im;
+            h[j + m] = hre * im + him * re;
+        }
+        __syncwarp();
+        int st = 0;
+        if (!bad) {
+            const double cut = kPinvEps;
+            if (!warp_ldl_solve(G, h, s, m2, V, W, dd, cut)) {
+                if (threadIdx.x == 0) ctrl->svd_fallbacks++;
+                st = warp_pinv_any(G, V, h, s, m2, Gs, Vs, cut);
+            }
+        }
+        __syncwarp();
+        for (int j = threadIdx.x; j < m; j += 32) {
+            ctrl->s[2 * j] = bad ? 0.0 : s[j];
+            ctrl->s[2 * j + 1] = bad ? 0.0 : s[j + m];
+        }
+        if (threadIdx.x == 0) {
+            if (bad) { ctrl->status = LSG_NAN_DETECTED; ctrl->done = 1; }
+            else if (st) ctrl->status = st;
         }
     }
 }
@@ -464,7 +535,7 @@ __global__ void pinv_kernel(const double *A, const double *b, double *x, int m, 
     for (int i = threadIdx.x; i < m * m; i += 32) G[i] = A[i];
     for (int i = threadIdx.x; i < m; i += 32) h[i] = b[i];
     __syncwarp();
-    const int st = warp_pinv_any(G, V, h, s, m, Gs, Vs);
+    const int st = warp_pinv_any(G, V, h, s, m, Gs, Vs, m * kPinvEps);
     __syncwarp();
     if (threadIdx.x < m) x[threadIdx.x] = s[threadIdx.x];
     if (threadIdx.x == 0 && status) *status = st;
@@ -473,14 +544,21 @@ __global__ void pinv_kernel(const double *A, const double *b, double *x, int m, 
 // ---------------------------------------------------------------- launchers
 
 cudaError_t finalize_norm(const double *partials, int nparts, DevCtrl *ctrl, int mode, double tol,
-                          int iter, cudaStream_t s) {
-    finalize_norm_kernel<<<1, kFinThreads, 0, s>>>(partials, nparts, ctrl, mode, tol, iter);
+                          int iter, cudaStream_t s, int width) {
+    finalize_norm_kernel<<<1, kFinThreads, 0, s>>>(partials, nparts, ctrl, mode, tol, iter, width);
     return cudaGetLastError();
 }
 
 cudaError_t finalize_gram_solve(const double *partials, int nparts, int kind, int m, double hscale,
                                 DevCtrl *ctrl, cudaStream_t s) {
     finalize_gram_solve_kernel<<<1, kFinThreads, 0, s>>>(partials, nparts, kind, m, hscale, ctrl);
+    return cudaGetLastError();
+}
+
+cudaError_t finalize_gram_solve_c(const double *partials, int nparts, int m, cplx<double> hscale,
+                                  DevCtrl *ctrl, cudaStream_t s) {
+    if (2 * m > LSG_MAX_M) return cudaErrorInvalidValue;
+    finalize_gram_solve_c_kernel<<<1, kFinThreads, 0, s>>>(partials, nparts, m, hscale.x, hscale.y, ctrl);
     return cudaGetLastError();
 }
 

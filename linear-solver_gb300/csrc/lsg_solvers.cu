@@ -77,10 +77,9 @@ static int sm_count() {
 // Resident stencil blocks on the device (one wave).
 template <typename T>
 static int stencil_slots(int sms) {
-    static int bpsm[2] = {0, 0};  // per element size, resolved on first use
-    int &v = bpsm[sizeof(T) == 8 ? 1 : 0];
-    if (v == 0) v = Kernels<T>::stencil_blocks_per_sm();
-    return sms * v;
+    static int bpsm = 0;  // per vector type, resolved on first use
+    if (bpsm == 0) bpsm = Kernels<T>::stencil_blocks_per_sm();
+    return sms * bpsm;
 }
 
 // ---------------------------------------------------------------- work arrays
@@ -150,6 +149,10 @@ static int get_workspace(size_t es, long long n, int m, bool mixed, const Geom &
     long long cap = partials_needed(n, m, sms);
     cap = std::max(cap, stencil_blocks<double>(g, choose_lz<double>(g, stencil_slots<double>(sms))));
     cap = std::max(cap, stencil_blocks<float>(g, choose_lz<float>(g, stencil_slots<float>(sms))));
+    if (es == sizeof(cplx<double>) || es == sizeof(cplx<float>)) {  // complex: (re, im) partials
+        cap = std::max(cap, 2 * stencil_blocks<cplx<double>>(g, choose_lz<cplx<double>>(g, stencil_slots<cplx<double>>(sms))));
+        cap = std::max(cap, 2 * stencil_blocks<cplx<float>>(g, choose_lz<cplx<float>>(g, stencil_slots<cplx<float>>(sms))));
+    }
     const size_t vec = align_up((size_t)n * es);
     size_t bytes = 0;
     const size_t o_xalt = bytes; bytes += vec;
@@ -158,9 +161,9 @@ static int get_workspace(size_t es, long long n, int m, bool mixed, const Geom &
     const size_t o_dx = bytes; bytes += align_up((size_t)n * es * (size_t)m);
     const size_t o_df = bytes; bytes += align_up((size_t)n * es * (size_t)m);
     size_t o_r32 = 0, o_e32 = 0;
-    if (mixed) {
-        o_r32 = bytes; bytes += align_up((size_t)n * 4);
-        o_e32 = bytes; bytes += align_up((size_t)n * 4);
+    if (mixed) {  // FP32 (or complex64) correction, half the outer element size
+        o_r32 = bytes; bytes += align_up((size_t)n * (es / 2));
+        o_e32 = bytes; bytes += align_up((size_t)n * (es / 2));
     }
     const size_t o_part = bytes; bytes += align_up((size_t)cap * 8);
     const size_t o_ctrl = bytes; bytes += align_up(sizeof(DevCtrl));
@@ -244,9 +247,28 @@ static Weights<T> make_weights(const lsg_operator *op) {
     Weights<T> w;
     memset(&w, 0, sizeof(w));
     w.radius = op->radius;
-    w.w[0] = (T)(op->a * 3.0 * op->coeff[0] + op->sigma);
-    for (int p = 1; p <= op->radius; p++) w.w[p] = (T)(op->a * op->coeff[p]);
+    if constexpr (IsCplx<T>::value) {
+        w.w[0] = T(op->a * 3.0 * op->coeff[0] + op->sigma, op->sigma_im);
+        for (int p = 1; p <= op->radius; p++) w.w[p] = T(op->a * op->coeff[p], 0.0);
+    } else {
+        w.w[0] = (T)(op->a * 3.0 * op->coeff[0] + op->sigma);
+        for (int p = 1; p <= op->radius; p++) w.w[p] = (T)(op->a * op->coeff[p]);
+    }
     return w;
+}
+
+// Jacobi factor cf = 1 / diag (or 1 without preconditioning), in the
+// vector type's host scalar: the complex shift makes it complex.
+template <typename T>
+static typename ScalarOf<T>::type jacobi_factor(const lsg_operator *op) {
+    if constexpr (IsCplx<T>::value) {
+        if (!op->precond) return cplx<double>(1.0, 0.0);
+        const double dr = op->a * (3 * op->coeff[0]) + op->sigma, di = op->sigma_im;
+        const double den = dr * dr + di * di;
+        return cplx<double>(dr / den, -di / den);
+    } else {
+        return op->precond ? 1.0 / jacobi_diag(op) : 1.0;
+    }
 }
 
 static int check_params(const lsg_params *prm, bool history) {
@@ -417,7 +439,9 @@ static long long richardson_count(int last, int p) {
 //   b is not read after the initial residual.
 template <typename T>
 struct AarLoop {
-    static constexpr bool recur = std::is_same<T, float>::value;
+    using S = typename ScalarOf<T>::type;
+    static constexpr bool recur = std::is_same<typename RealOf<T>::type, float>::value;
+    static constexpr int W = AccWidth<T>::value;
     Run &R;
     const lsg_params *prm;
     Workspace *ws;
@@ -425,7 +449,7 @@ struct AarLoop {
     long long n;
     int m, p;
     Weights<T> w;
-    double cf;
+    S cf;
     StencilLaunch L;
     int sb, rb, gb;
     T *X[2];
@@ -442,7 +466,7 @@ struct AarLoop {
         m = prm->m;
         p = prm->p;
         w = make_weights<T>(op);
-        cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
+        cf = jacobi_factor<T>(op);
         const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
         L = StencilLaunch{g, lz, R.s};
         sb = (int)stencil_blocks<T>(g, lz);
@@ -474,7 +498,10 @@ struct AarLoop {
         T *dxc = DX + (size_t)col * n, *dfc = DF + (size_t)col * n;
         if (is_anderson(it)) {
             LSG_KC(LSG_K_GRAM, Kernels<T>::gram(GRAM_SYM, m, DX, DF, Rv[rc], n, part, gb, ctrl, R.s));
-            LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, gb, GRAM_SYM, m, cf, ctrl, R.s));
+            if constexpr (IsCplx<T>::value)
+                LSG_KC(LSG_K_SMALL, finalize_gram_solve_c(part, gb, m, cf, ctrl, R.s));
+            else
+                LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, gb, GRAM_SYM, m, cf, ctrl, R.s));
             if (recur) {
                 // the step goes to the spare vector: the residual reads it as its stencil input
                 T *step = (T *)ws->xalt;
@@ -485,7 +512,7 @@ struct AarLoop {
                 LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_ANDERSON, X[xc], b, Rv[rc], dfc, dxc, cf,
                                                             prm->beta, part, ctrl));
             }
-            LSG_KC(LSG_K_SMALL, finalize_norm(part, sb, ctrl, NF_CHECK, prm->tol, it, R.s));
+            LSG_KC(LSG_K_SMALL, finalize_norm(part, sb, ctrl, NF_CHECK, prm->tol, it, R.s, W));
         } else if (recur) {
             LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson_recur(L, w, Rv[rc], X[0], Rv[rc ^ 1], dxc, dfc,
                                                                   prm->omega * cf, cf, prm->beta, ctrl));
@@ -517,7 +544,7 @@ int aar_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const 
     if (rc) return rc;
     // ||b|| and tol *= ||b|| (AAR.c:78-79); f = b - A x (AAR.c:80-82).
     LSG_KC(LSG_K_UPDATE, Kernels<T>::norm2(b, A.n, A.part, A.rb, A.ctrl, R.s));
-    LSG_KC(LSG_K_SMALL, finalize_norm(A.part, A.rb, A.ctrl, NF_RHS, prm->tol, 0, R.s));
+    LSG_KC(LSG_K_SMALL, finalize_norm(A.part, A.rb, A.ctrl, NF_RHS, prm->tol, 0, R.s, AarLoop<T>::W));
     LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(A.L, A.w, RES_INIT, x, b, A.Rv[0], nullptr, nullptr, A.cf, 0.0,
                                                 A.part, A.ctrl));
     rc = A.run(1);
@@ -653,15 +680,23 @@ static int solve_t(int solver, const lsg_operator *op, const lsg_params *prm, vo
     Workspace *ws = nullptr;
     std::unique_lock<std::mutex> lk;
     const int mh = solver == 3 ? 1 : prm->m;
+    if (IsCplx<T>::value && solver != 0)
+        return set_error(LSG_UNSUPPORTED, "complex vectors: only AAR is provided (PETSC_COMPLEX/AAR_Complex.c)");
+    if (IsCplx<T>::value && 2 * prm->m > LSG_MAX_M)
+        return set_error(LSG_BAD_ARG, "complex AAR: m = %d > %d", prm->m, LSG_MAX_M / 2);
     int rc = get_workspace(sizeof(T), g.n, mh, false, g, &ws, &lk);
     if (rc != LSG_OK) return rc;
     Run R(s, sm_count());
     DevCtrl c;
-    switch (solver) {
-    case 0: rc = aar_core<T>(R, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
-    case 1: rc = prich_core<T>(R, true, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
-    case 2: rc = prich_core<T>(R, false, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
-    default: rc = cg_core<T>(R, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
+    if constexpr (IsCplx<T>::value) {
+        rc = aar_core<T>(R, op, prm, (T *)d_x, (const T *)d_b, ws, &c);
+    } else {
+        switch (solver) {
+        case 0: rc = aar_core<T>(R, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
+        case 1: rc = prich_core<T>(R, true, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
+        case 2: rc = prich_core<T>(R, false, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
+        default: rc = cg_core<T>(R, op, prm, (T *)d_x, (const T *)d_b, ws, &c); break;
+        }
     }
     if (rc != LSG_OK) return rc;
     R.flush();
@@ -683,6 +718,8 @@ int solve(int solver, const lsg_operator *op, const lsg_params *prm, int dtype, 
     if (!d_x || !d_b) return set_error(LSG_BAD_ARG, "NULL vector");
     if (dtype == LSG_F64) return solve_t<double>(solver, op, prm, d_x, d_b, res, s);
     if (dtype == LSG_F32) return solve_t<float>(solver, op, prm, d_x, d_b, res, s);
+    if (dtype == LSG_C128) return solve_t<cplx<double>>(solver, op, prm, d_x, d_b, res, s);
+    if (dtype == LSG_C64) return solve_t<cplx<float>>(solver, op, prm, d_x, d_b, res, s);
     return set_error(LSG_BAD_ARG, "unknown dtype %d", dtype);
 }
 
@@ -697,49 +734,54 @@ int solve(int solver, const lsg_operator *op, const lsg_params *prm, int dtype, 
 // Anderson history intact, so no iterations are spent rebuilding it.  FP64
 // is used only for that residual, x64, the reductions and the m x m solve.
 // Convergence is decided on the FP64 residual.
-int solve_mixed(const lsg_operator *op, const lsg_params *prm, double *x, const double *b,
-                lsg_result *res, cudaStream_t s) {
+template <typename T64, typename T32>
+int solve_mixed_t(const lsg_operator *op, const lsg_params *prm, T64 *x, const T64 *b,
+                  lsg_result *res, cudaStream_t s) {
+    constexpr int W = AccWidth<T64>::value;
     const double t0 = now_s();
     int rc = check_operator(op);
     if (rc) return rc;
     rc = check_params(prm, true);
     if (rc) return rc;
+    if (IsCplx<T64>::value && 2 * prm->m > LSG_MAX_M)
+        return set_error(LSG_BAD_ARG, "complex AAR: m = %d > %d", prm->m, LSG_MAX_M / 2);
     if (!x || !b) return set_error(LSG_BAD_ARG, "NULL vector");
     const Geom g = make_geom(op->n);
     const long long n = g.n;
     Workspace *wo = nullptr, *wi = nullptr;
     std::unique_lock<std::mutex> lo, li;
-    rc = get_workspace(sizeof(double), n, 1, true, g, &wo, &lo);  // outer: e32, partials, ctrl
+    rc = get_workspace(sizeof(T64), n, 1, true, g, &wo, &lo);  // outer: e32, partials, ctrl
     if (rc) return rc;
-    rc = get_workspace(sizeof(float), n, prm->m, false, g, &wi, &li);  // FP32 AAR work arrays
+    rc = get_workspace(sizeof(T32), n, prm->m, false, g, &wi, &li);  // FP32 AAR work arrays
     if (rc) return rc;
     Run R(s, sm_count());
-    const Weights<double> w64 = make_weights<double>(op);
-    const int lz = choose_lz<double>(g, stencil_slots<double>(R.sms));
+    const Weights<T64> w64 = make_weights<T64>(op);
+    const int lz = choose_lz<T64>(g, stencil_slots<T64>(R.sms));
     const StencilLaunch L64{g, lz, s};
-    const int sb64 = (int)stencil_blocks<double>(g, lz);
+    const int sb64 = (int)stencil_blocks<T64>(g, lz);
     const int rb = reduce_blocks(n, R.sms);
     DevCtrl *octrl = wo->ctrl;
     double *opart = wo->partials;
     const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
     const double rho = prm->inner_tol > 0 ? prm->inner_tol : 3e-2;
-    AarLoop<float> A(R, op, prm, wo->e32, nullptr, wi);
+    T32 *e32 = (T32 *)wo->e32;
+    AarLoop<T32> A(R, op, prm, e32, nullptr, wi);
 
     wo->hctrl[0] = ctrl_init(prm->tol, 0);
     LSG_CUDA(cudaMemcpyAsync(octrl, wo->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, s));
-    LSG_CUDA(cudaMemsetAsync(wo->e32, 0, sizeof(float) * (size_t)n, s));
+    LSG_CUDA(cudaMemsetAsync(e32, 0, sizeof(T32) * (size_t)n, s));
     rc = A.reset_history();
     if (rc) return rc;
-    LSG_KC(LSG_K_UPDATE, Kernels<double>::norm2(b, n, opart, rb, octrl, s));
-    LSG_KC(LSG_K_SMALL, finalize_norm(opart, rb, octrl, NF_RHS, prm->tol, 0, s));
+    LSG_KC(LSG_K_UPDATE, Kernels<T64>::norm2(b, n, opart, rb, octrl, s));
+    LSG_KC(LSG_K_SMALL, finalize_norm(opart, rb, octrl, NF_RHS, prm->tol, 0, s, W));
 
     int status = LSG_NOT_CONVERGED, replacements = 0, it = 1, iters = 0;
     DevCtrl co, ci;
     for (;;) {
         // r = b - A x64 in FP64, stored as the FP32 residual the iteration continues from
         A.sync_parity(it - 1);
-        LSG_KC(LSG_K_REFINE, ir_residual(L64, w64, x, b, A.Rv[A.rc], opart, octrl));
-        LSG_KC(LSG_K_SMALL, finalize_norm(opart, sb64, octrl, NF_CHECK, prm->tol, it - 1, s));
+        LSG_KC(LSG_K_REFINE, (ir_residual<T64, T32>(L64, w64, x, b, A.Rv[A.rc], opart, octrl)));
+        LSG_KC(LSG_K_SMALL, finalize_norm(opart, sb64, octrl, NF_CHECK, prm->tol, it - 1, s, W));
         LSG_CUDA(cudaMemcpyAsync(&wo->hctrl[0], octrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost, s));
         LSG_CUDA(cudaStreamSynchronize(s));
         co = wo->hctrl[0];
@@ -765,7 +807,7 @@ int solve_mixed(const lsg_operator *op, const lsg_params *prm, double *x, const 
         if (ci.status == LSG_NAN_DETECTED) { status = LSG_NAN_DETECTED; break; }
         iters = ci.done ? ci.iters : prm->max_iter;
         // fold the correction into x64 (e = 0 afterwards) and replace the residual
-        LSG_KC(LSG_K_REFINE, ir_correct(x, wo->e32, n, s));
+        LSG_KC(LSG_K_REFINE, (ir_correct<T64, T32>(x, e32, n, s)));
         replacements++;
         it = iters + 1;
     }
@@ -785,6 +827,17 @@ int solve_mixed(const lsg_operator *op, const lsg_params *prm, double *x, const 
     return status;
 }
 
+int solve_mixed(const lsg_operator *op, const lsg_params *prm, double *x, const double *b,
+                lsg_result *res, cudaStream_t s) {
+    return solve_mixed_t<double, float>(op, prm, x, b, res, s);
+}
+
+int solve_mixed_c(const lsg_operator *op, const lsg_params *prm, void *x, const void *b,
+                  lsg_result *res, cudaStream_t s) {
+    return solve_mixed_t<cplx<double>, cplx<float>>(op, prm, (cplx<double> *)x, (const cplx<double> *)b,
+                                                    res, s);
+}
+
 int apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, cudaStream_t s) {
     int rc = check_operator(op);
     if (rc) return rc;
@@ -799,6 +852,16 @@ int apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, cudaStr
         const StencilLaunch L{g, choose_lz<float>(g, stencil_slots<float>(sms)), s};
         LSG_CUDA(Kernels<float>::residual(L, make_weights<float>(op), RES_APPLY, (const float *)d_x,
                                           nullptr, (float *)d_y, nullptr, nullptr, 1.0, 0.0, nullptr, nullptr));
+    } else if (dtype == LSG_C128) {
+        const StencilLaunch L{g, choose_lz<cplx<double>>(g, stencil_slots<cplx<double>>(sms)), s};
+        LSG_CUDA(Kernels<cplx<double>>::residual(L, make_weights<cplx<double>>(op), RES_APPLY,
+                                                 (const cplx<double> *)d_x, nullptr, (cplx<double> *)d_y,
+                                                 nullptr, nullptr, cplx<double>(1.0, 0.0), 0.0, nullptr, nullptr));
+    } else if (dtype == LSG_C64) {
+        const StencilLaunch L{g, choose_lz<cplx<float>>(g, stencil_slots<cplx<float>>(sms)), s};
+        LSG_CUDA(Kernels<cplx<float>>::residual(L, make_weights<cplx<float>>(op), RES_APPLY,
+                                                (const cplx<float> *)d_x, nullptr, (cplx<float> *)d_y,
+                                                nullptr, nullptr, cplx<double>(1.0, 0.0), 0.0, nullptr, nullptr));
     } else {
         return set_error(LSG_BAD_ARG, "unknown dtype %d", dtype);
     }
@@ -879,6 +942,10 @@ int lsg_cg(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, 
 int lsg_aar_mixed(const lsg_operator *op, const lsg_params *prm, double *d_x, const double *d_b,
                   lsg_result *res, void *stream) {
     return lsg::solve_mixed(op, prm, d_x, d_b, res, (cudaStream_t)stream);
+}
+int lsg_aar_mixed_c(const lsg_operator *op, const lsg_params *prm, void *d_x, const void *d_b,
+                    lsg_result *res, void *stream) {
+    return lsg::solve_mixed_c(op, prm, d_x, d_b, res, (cudaStream_t)stream);
 }
 int lsg_pinv_solve(const double *d_A, const double *d_b, double *d_x, int m, void *stream) {
     return lsg::pinv(d_A, d_b, d_x, m, (cudaStream_t)stream);

@@ -32,6 +32,7 @@
 
 #include "lsg_internal.cuh"
 #include "lsg_accum.cuh"
+#include "lsg_complex.cuh"
 
 namespace lsg {
 
@@ -197,9 +198,10 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
 
     if (Op::NACC > 0) {
         constexpr int NA = Op::NACC > 0 ? Op::NACC : 1;
-        __shared__ double red[NA * 32];
+        constexpr int W = AccWidth<T>::value;
+        __shared__ double red[NA * W * 32];
         const long long blk = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
-        block_reduce_store<NA, T>(acc, red, op.partials + blk * Op::NACC);
+        block_reduce_store<NA>(acc, red, op.partials + blk * Op::NACC * W);
     }
 }
 

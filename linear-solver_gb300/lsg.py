@@ -26,7 +26,7 @@ MAX_RADIUS = 8
 MAX_M = 32
 A_REF = -1.0 / (4.0 * math.pi)  # operator scale of MPI_REAL/main.c:68
 
-F64, F32 = 0, 1
+F64, F32, C128, C64 = 0, 1, 2, 3
 STATUS = {0: "ok", 1: "not converged", 2: "NaN/Inf detected", 3: "bad argument", 4: "CUDA error",
           5: "timeout", 6: "unsupported", 7: "out of memory", 8: "SVD sweep limit"}
 
@@ -37,7 +37,8 @@ class CudaLibraryError(RuntimeError):
 
 class _Operator(C.Structure):
     _fields_ = [("n", C.c_int * 3), ("radius", C.c_int), ("coeff", C.c_double * (MAX_RADIUS + 1)),
-                ("a", C.c_double), ("sigma", C.c_double), ("precond", C.c_int)]
+                ("a", C.c_double), ("sigma", C.c_double), ("precond", C.c_int),
+                ("sigma_im", C.c_double)]
 
 
 class _Params(C.Structure):
@@ -84,7 +85,8 @@ EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "ls
            "lsg_release_workspaces", "lsg_last_status", "lsg_last_error", "lsg_status_string",
            "lsg_version", "AAR", "PGR", "PL2R", "CG", "lsg_register_operator_callback",
            "lsg_register_precondition_callback", "lsg_set_verbose", "lsg_last_result",
-           "lsg_profile", "lsg_profile_read", "lsg_set_compat_mode"]
+           "lsg_profile", "lsg_profile_read", "lsg_set_compat_mode", "lsg_aar_mixed_c",
+           "lsg_pinv_solve_noalloc"]
 
 KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "unused"]
 
@@ -115,6 +117,8 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
                                       C.POINTER(_Result), vp]
         L.lsg_aar_mixed.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), vp, vp,
                                     C.POINTER(_Result), vp]
+        L.lsg_aar_mixed_c.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), vp, vp,
+                                      C.POINTER(_Result), vp]
         L.lsg_pinv_solve.argtypes = [vp, vp, vp, ip, vp]
         L.lsg_last_error.restype = C.c_char_p
         L.lsg_status_string.restype = C.c_char_p
@@ -161,17 +165,21 @@ def lap_coefficient(radius: int):
 
 
 class Operator:
-    """A = a * Lap_h + sigma * I on a periodic (nx, ny, nz) grid, FD half-width `radius`."""
+    """A = a * Lap_h + sigma * I on a periodic (nx, ny, nz) grid, FD half-width `radius`.
 
-    def __init__(self, n, radius: int = 6, a: float = A_REF, sigma: float = 0.0,
-                 precond: bool = True):
+    sigma may be complex (the shifted Helmholtz operator of the complex solver)."""
+
+    def __init__(self, n, radius: int = 6, a: float = A_REF, sigma=0.0, precond: bool = True):
         if isinstance(n, int):
             n = (n, n, n)
         self.n = tuple(int(v) for v in n)  # (nx, ny, nz)
-        self.radius, self.a, self.sigma, self.precond = int(radius), float(a), float(sigma), bool(precond)
+        sg = complex(sigma)
+        self.radius, self.a, self.precond = int(radius), float(a), bool(precond)
+        self.sigma = sg if sg.imag != 0 else sg.real
         self._s = _Operator()
-        _check(lib().lsg_operator_init(C.byref(self._s), *self.n, self.radius, self.a, self.sigma,
+        _check(lib().lsg_operator_init(C.byref(self._s), *self.n, self.radius, self.a, sg.real,
                                        int(self.precond)), "lsg_operator_init", allow=(0,))
+        self._s.sigma_im = sg.imag
 
     @property
     def shape(self):
@@ -208,10 +216,9 @@ def _stream_ptr(stream=None):
 
 def _dtype_code(t):
     import torch
-    if t.dtype == torch.float64:
-        return F64
-    if t.dtype == torch.float32:
-        return F32
+    codes = {torch.float64: F64, torch.float32: F32, torch.complex128: C128, torch.complex64: C64}
+    if t.dtype in codes:
+        return codes[t.dtype]
     raise TypeError(f"unsupported dtype {t.dtype}")
 
 
@@ -279,16 +286,19 @@ SOLVERS = {"aar": aar, "pgr": pgr, "pl2r": pl2r, "cg": cg}
 
 
 def aar_mixed(op, b, x0=None, stream=None, **kw):
-    """FP32 AAR with FP64 residual replacement (include/lsg.h); b and x are float64."""
+    """FP32 AAR with FP64 residual replacement (include/lsg.h).
+
+    b and x are float64, or complex128 (complex64 inner iteration)."""
     import torch
-    if b.dtype != torch.float64:
-        raise TypeError("aar_mixed takes float64 b / x")
+    if b.dtype not in (torch.float64, torch.complex128):
+        raise TypeError("aar_mixed takes float64 or complex128 b / x")
     _check_vec(b, op, "b")
     x = torch.zeros_like(b) if x0 is None else x0.clone()
     res = _Result()
     prm = _params(**kw)
-    rc = lib().lsg_aar_mixed(C.byref(op._s), C.byref(prm), C.c_void_p(x.data_ptr()),
-                             C.c_void_p(b.data_ptr()), C.byref(res), _stream_ptr(stream))
+    fn = lib().lsg_aar_mixed if b.dtype == torch.float64 else lib().lsg_aar_mixed_c
+    rc = fn(C.byref(op._s), C.byref(prm), C.c_void_p(x.data_ptr()), C.c_void_p(b.data_ptr()),
+            C.byref(res), _stream_ptr(stream))
     _check(rc, "lsg_aar_mixed")
     return x, _result(res)
 

@@ -19,8 +19,12 @@
  *   - PL2R + L2 step             MPI_REAL/PL2R.c:35-172, 180-218    lsgo_pl2r
  *   - Jacobi PCG                 MPI_REAL/CG.c:33-175               lsgo_cg
  *   - reference RHS              MPI_REAL/system.c:452-468          lsgo_reference_rhs
- * plus a real diagonal shift sigma (A = a*Lap + sigma*I) used by the shifted
- * configurations; sigma = 0 is exactly the reference operator.
+ *   - complex AAR              PETSC_COMPLEX/AAR_Complex.c:31-199, 207-246  lsgo_aar_c
+ * plus a diagonal shift sigma (A = a*Lap + sigma*I, complex for lsgo_aar_c)
+ * used by the shifted configurations; sigma = 0 is the reference operator.
+ * The complex path's reference needs PETSc and MKL (not buildable here); its
+ * restatement is checked against the exact FFT solve and against the real
+ * AAR, which it must reproduce for real sigma and b.
  *
  * Arithmetic is written in the reference's evaluation order and the file is
  * compiled with -ffp-contract=off, so the stencil, the vector updates and
@@ -35,6 +39,7 @@
  * point-wise loops for the timed CPU baseline; lsgo_set_threads(1) gives the
  * serial, reference-order reductions the parity tests use.
  */
+#include <complex.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -185,7 +190,15 @@ static void precondition(double diag, double *r, long n)
  * columns are mutually orthogonal; then w_j = ||G(:,j)|| and V holds the
  * right singular vectors.  Returns 0 on success, 2 if the sweep limit hit.
  */
+static int pinv_cut(const double *A, const double *b, double *x, int m, double cut);
+
 int lsgo_pinv_solve(const double *A, const double *b, double *x, int m)
+{
+    return pinv_cut(A, b, x, m, m * 2.22044605e-16);
+}
+
+/* As lsgo_pinv_solve with the cutoff w < cut * wmax. */
+static int pinv_cut(const double *A, const double *b, double *x, int m, double cut)
 {
     double G[LSGO_MAXM * LSGO_MAXM], V[LSGO_MAXM * LSGO_MAXM], w[LSGO_MAXM], t[LSGO_MAXM];
     int i, j, k, sweep, rotated = 1, status = 0;
@@ -232,7 +245,7 @@ int lsgo_pinv_solve(const double *A, const double *b, double *x, int m)
         w[j] = sqrt(s);
         if (w[j] > wmax) wmax = w[j];
     }
-    const double wmin = m * wmax * eps;
+    const double wmin = cut * wmax;
     for (j = 0; j < m; j++) {
         double s = 0;
         if (w[j] >= wmin && w[j] > 0) {
@@ -516,4 +529,124 @@ void lsgo_reference_rhs(int nx, int ny, int nz, double *rhs)
     }
     sum /= (double)n;
     for (g = 0; g < n; g++) rhs[g] -= sum;
+}
+
+/* ---------------------------------------------------------------- complex */
+
+/* y = (a*Lap + (sigma + i sigma_im)) x, complex vectors. */
+void lsgo_apply_c(const lsgo_op *op, double sigma_im, const double complex *x, double complex *y)
+{
+    const int nx = op->n[0], ny = op->n[1], nz = op->n[2], R = op->radius;
+    double w[LSGO_MAXR + 1];
+    const double complex shift = op->sigma + I * sigma_im;
+    long k;
+    for (int p = 0; p <= R; p++) w[p] = op->a * op->coeff[p];
+#pragma omp parallel for schedule(static)
+    for (k = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                const long c = i + (long)nx * (j + (long)ny * k);
+                double complex v = x[c] * 3 * w[0];
+                for (int p = 1; p <= R; p++) {
+                    const int im = (i - p + p * nx) % nx, ip = (i + p) % nx;
+                    const int jm = (j - p + p * ny) % ny, jp = (j + p) % ny;
+                    const int km = (int)((k - p + (long)p * nz) % nz), kp = (int)((k + p) % nz);
+                    v += (x[im + (long)nx * (j + (long)ny * k)] + x[ip + (long)nx * (j + (long)ny * k)]
+                          + x[i + (long)nx * (jm + (long)ny * k)] + x[i + (long)nx * (jp + (long)ny * k)]
+                          + x[i + (long)nx * (j + (long)ny * km)] + x[i + (long)nx * (j + (long)ny * kp)]) * w[p];
+                }
+                y[c] = v + shift * x[c];
+            }
+}
+
+static double complex zdot(const double complex *a, const double complex *b, long n) /* a^H b */
+{
+    double complex s = 0;
+    for (long k = 0; k < n; k++) s += conj(a[k]) * b[k];
+    return s;
+}
+
+/* PETSC_COMPLEX/AAR_Complex.c:31-199 with Anderson (:207-246): Jacobi on the
+ * complex diagonal 3 a c_0 + sigma; Gram G(i,j) = DF_i^H DF_j, rhs DF_i^H res;
+ * the m x m minimum-norm least-squares solve of LAPACKE_zgelsd with rcond -1
+ * (singular values below eps * sigma_max dropped), computed here through the
+ * real 2m x 2m representation of the Hermitian G. */
+int lsgo_aar_c(const lsgo_op *op, double sigma_im, int precond, double complex *x,
+               const double complex *b, double omega, double beta, int m, int p, int max_iter,
+               double tol, lsgo_result *res)
+{
+    const long np = (long)op->n[0] * op->n[1] * op->n[2];
+    const double complex diag = op->a * (3 * op->coeff[0]) + op->sigma + I * sigma_im;
+    double complex *r = calloc(np, sizeof(double complex)), *x_old = calloc(np, sizeof(double complex));
+    double complex *f_old = calloc(np, sizeof(double complex));
+    double complex *DX = calloc(np * m, sizeof(double complex)), *DF = calloc(np * m, sizeof(double complex));
+    double Gr[4 * LSGO_MAXM * LSGO_MAXM], hr[2 * LSGO_MAXM], sr[2 * LSGO_MAXM];
+    double b2 = 0, r2 = tol + 1, t0;
+    int iter = 1, status = 0;
+    long i;
+    if (!r || !x_old || !f_old || !DX || !DF) abort();
+    if (m > LSGO_MAXM / 2) m = LSGO_MAXM / 2;
+    for (i = 0; i < np; i++) b2 += creal(conj(b[i]) * b[i]);
+    b2 = sqrt(b2);
+    tol *= b2;
+    lsgo_apply_c(op, sigma_im, x, r);
+    for (i = 0; i < np; i++) r[i] = b[i] - r[i];
+    t0 = now_s();
+    while (r2 > tol && iter <= max_iter) {
+        if (precond)
+            for (i = 0; i < np; i++) r[i] /= diag;
+        if (iter > 1) {
+            const int k = (iter - 2) % m;
+            for (i = 0; i < np; i++) {
+                DX[k * np + i] = x[i] - x_old[i];
+                DF[k * np + i] = r[i] - f_old[i];
+            }
+        }
+        memcpy(x_old, x, sizeof(double complex) * np);
+        memcpy(f_old, r, sizeof(double complex) * np);
+        if (iter % p) {
+            for (i = 0; i < np; i++) x[i] += omega * r[i];
+        } else {
+            const int m2 = 2 * m;
+            for (int a = 0; a < m; a++)
+                for (int j = 0; j <= a; j++) {
+                    const double complex g = zdot(DF + a * np, DF + j * np, np); /* G(a,j) */
+                    const double gre = creal(g), gim = (a == j) ? 0.0 : cimag(g);
+                    /* real representation [[A, -B], [B, A]] of G = A + iB */
+                    Gr[a * m2 + j] = gre;           Gr[j * m2 + a] = gre;
+                    Gr[(a + m) * m2 + j + m] = gre; Gr[(j + m) * m2 + a + m] = gre;
+                    Gr[a * m2 + j + m] = -gim;      Gr[j * m2 + a + m] = gim;
+                    Gr[(a + m) * m2 + j] = gim;     Gr[(j + m) * m2 + a] = -gim;
+                }
+            for (int a = 0; a < m; a++) {
+                const double complex h = zdot(DF + a * np, r, np);
+                hr[a] = creal(h);
+                hr[a + m] = cimag(h);
+            }
+            if (pinv_cut(Gr, hr, sr, m2, 2.22044605e-16)) status = 2;
+            for (int a = 0; a < m; a++) {
+                const double complex sa = sr[a] + I * sr[a + m];
+                for (i = 0; i < np; i++) x[i] -= sa * (DX[a * np + i] + beta * DF[a * np + i]);
+            }
+            for (i = 0; i < np; i++) x[i] += beta * r[i];
+        }
+        lsgo_apply_c(op, sigma_im, x, r);
+        for (i = 0; i < np; i++) r[i] = b[i] - r[i];
+        if (iter % p == 0) {
+            r2 = 0;
+            for (i = 0; i < np; i++) r2 += creal(conj(r[i]) * r[i]);
+            r2 = sqrt(r2);
+        }
+        iter++;
+    }
+    if (res) {
+        res->seconds = now_s() - t0;
+        res->iters = iter - 1;
+        res->rhs_norm = b2;
+        res->relres = r2 / b2;
+        res->converged = r2 <= tol;
+        res->status = status ? status : (res->converged ? 0 : 1);
+    }
+    free(r); free(x_old); free(f_old); free(DX); free(DF);
+    return res ? res->status : 0;
 }

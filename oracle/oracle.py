@@ -81,6 +81,11 @@ def lib() -> C.CDLL:
         L.lsgo_cg.argtypes = [C.POINTER(OpStruct), C.c_int, _dp, _dp, C.c_int, C.c_double,
                               C.POINTER(ResultStruct)]
         L.lsgo_reference_rhs.argtypes = [C.c_int, C.c_int, C.c_int, _dp]
+        _cp = np.ctypeslib.ndpointer(dtype=np.complex128, flags="C_CONTIGUOUS")
+        L.lsgo_apply_c.argtypes = [C.POINTER(OpStruct), C.c_double, _cp, _cp]
+        L.lsgo_aar_c.argtypes = [C.POINTER(OpStruct), C.c_double, C.c_int, _cp, _cp, C.c_double,
+                                 C.c_double, C.c_int, C.c_int, C.c_int, C.c_double,
+                                 C.POINTER(ResultStruct)]
         L.lsgo_set_threads.argtypes = [C.c_int]
         L.lsgo_max_threads.restype = C.c_int
         L.lsgo_set_threads(1)
@@ -132,6 +137,32 @@ def apply(x: np.ndarray, radius=6, a=A_REF, sigma=0.0) -> np.ndarray:
     y = np.empty_like(x)
     lib().lsgo_apply(C.byref(op), x.reshape(-1), y.reshape(-1))
     return y
+
+
+def apply_c(x: np.ndarray, radius=6, a=A_REF, sigma=0.0):
+    """y = (a*Lap + sigma) x for complex x and complex sigma."""
+    x = np.ascontiguousarray(x, dtype=np.complex128)
+    nz, ny, nx = x.shape
+    sg = complex(sigma)
+    op = make_op((nx, ny, nz), radius, a, sg.real)
+    y = np.empty_like(x)
+    lib().lsgo_apply_c(C.byref(op), sg.imag, x.reshape(-1), y.reshape(-1))
+    return y
+
+
+def solve_c(b: np.ndarray, x0=None, *, radius=6, a=A_REF, sigma=0.0, precond=True, omega=0.6,
+            beta=0.6, m=7, p=6, max_iter=100000, tol=1e-8):
+    """Complex AAR (PETSC_COMPLEX/AAR_Complex.c restated); b shaped (nz, ny, nx)."""
+    b = np.ascontiguousarray(b, dtype=np.complex128)
+    nz, ny, nx = b.shape
+    sg = complex(sigma)
+    op = make_op((nx, ny, nz), radius, a, sg.real)
+    x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.complex128, copy=True)
+    res = ResultStruct()
+    lib().lsgo_aar_c(C.byref(op), sg.imag, int(precond), x.reshape(-1), b.reshape(-1), omega, beta,
+                     m, p, max_iter, tol, C.byref(res))
+    return x, dict(iters=res.iters, relres=res.relres, rhs_norm=res.rhs_norm,
+                   converged=bool(res.converged), status=res.status, seconds=res.seconds)
 
 
 def pinv_solve(A: np.ndarray, b: np.ndarray):

@@ -114,3 +114,19 @@ def test_fft_oracle_agrees_with_iterative_oracle(oracle):
     bs = workloads.uniform_rhs(12, 4)
     xs = oracle.fft_solve(bs, a=1.0, sigma=2.5)
     assert np.linalg.norm(oracle.apply(xs, a=1.0, sigma=2.5) - bs) < 1e-12 * np.linalg.norm(bs)
+
+
+def test_complex_restatement(oracle):
+    """Complex AAR: reduces to the pinned real AAR for real data; matches the FFT solve."""
+    import workloads
+    b = workloads.uniform_rhs(16, 3)
+    xr, rr = oracle.solve("aar", b, a=-256.0, sigma=2.0)
+    xc, rc = oracle.solve_c(b.astype(complex), a=-256.0, sigma=2.0)
+    assert rc["iters"] == rr["iters"]
+    assert np.abs(xc - xr).max() < 1e-12
+    rng = np.random.default_rng(0)
+    bc = rng.uniform(-.5, .5, (12, 12, 12)) + 1j * rng.uniform(-.5, .5, (12, 12, 12))
+    xc, rc = oracle.solve_c(bc, a=-144.0, sigma=20 + 15j, tol=1e-12)
+    xf = oracle.fft_solve(bc, a=-144.0, sigma=20 + 15j)
+    assert np.linalg.norm(xc - xf) <= 1e-10 * np.linalg.norm(xf)
+    assert np.linalg.norm(oracle.apply_c(xf, a=-144.0, sigma=20 + 15j) - bc) <= 1e-13 * np.linalg.norm(bc)
