@@ -126,6 +126,21 @@ int lsg_aar_mixed(const lsg_operator *op, const lsg_params *prm, double *d_x, co
 int lsg_aar_mixed_c(const lsg_operator *op, const lsg_params *prm, void *d_x, const void *d_b,
                     lsg_result *res, void *stream);
 
+/* Batched AAR: `count` independent solves, each with its own operator (grid
+ * size, shift, coefficients) and its own x / b (device pointers), sharing
+ * prm (omega, beta, m <= 8, p, tol, max_iter).  Every kernel launch covers
+ * all unfinished instances and one extrapolation cycle (p iterations) is
+ * replayed as a CUDA graph; each instance follows the single solve's
+ * iteration (MPI_REAL/AAR.c:37-177), its result in res[i] (res may be NULL).
+ * The reference has no batched entry point: its caller loops over AAR().
+ * lsg_aar_mixed_batched: dtype LSG_F64 (FP32 inner iteration) or LSG_C128
+ * (complex64 inner), the refinement of lsg_aar_mixed per instance.
+ * Returns LSG_OK when every instance converged, else the first failure. */
+int lsg_aar_batched(const lsg_operator *ops, int count, const lsg_params *prm, int dtype,
+                    void *const *d_x, const void *const *d_b, lsg_result *res, void *stream);
+int lsg_aar_mixed_batched(const lsg_operator *ops, int count, const lsg_params *prm, int dtype,
+                          void *const *d_x, const void *const *d_b, lsg_result *res, void *stream);
+
 /* m x m pseudo-inverse solve with the reference's semantics
  * (x = V diag(1/w) V^T b, w < m*wmax*2.22044605e-16 dropped; MPI_REAL/tools.c:52-105),
  * computed on the device by one warp.  A row-major, device pointers. */

@@ -1,0 +1,359 @@
+// lsg_batch.cuh — batched kernels: one launch per pass covers every active
+// instance of a batch (instances may differ in grid size, shift and
+// coefficients).  Instantiated per vector type by lsg_batch_{f64,f32,c128,c64}.cu.
+//
+// A batched stencil launch is a 1-D grid: block b serves instance map[b],
+// tile (b - sblk0) of that instance's (tx, ty, z-chunk) tile grid, with the
+// same z-marching driver, functors and per-block partial sums as a single
+// solve.  Point-local passes (Gram, extrapolation update, norms) give each
+// instance `ublocks` grid-stride blocks.  The iteration number, the history
+// column ((it-1) % m) and the residual ping-pong parity are computed on the
+// device from the batch clock, so one captured cycle replays unchanged.
+#pragma once
+
+#include "lsg_kernels.cuh"
+
+namespace lsg {
+
+__device__ __forceinline__ int batch_iter(const BArgs &a) { return a.clk->it0 + a.k + 1; }
+
+template <typename T>
+__device__ __forceinline__ T *rbuf(const BInst<T> &I, int par) { return par ? I.r1 : I.r0; }
+
+template <typename T>
+struct IsRecur { static constexpr bool value = std::is_same<typename RealOf<T>::type, float>::value; };
+
+// Refinement passes act on instances whose FP32 iteration paused (gate 0), or
+// on every unfinished one (gate 1, the final pass after max_iter).
+__device__ __forceinline__ bool replace_gate(const BCtl &C, const BArgs &a) {
+    if (solve_done(C.octrl)) return false;
+    return a.gate == 1 || solve_done(C.ctrl);
+}
+
+// ---------------------------------------------------------------- passes
+// make(): the functor of one instance for this launch, or false when the
+// instance has nothing to do in it.
+
+template <typename T>
+struct PassRichRecur {  // AAR.c:93-107,134-139 in residual-recurrence form
+    using TS = T;
+    using Op = RichRecurOp<T>;
+    static constexpr int MINB = TileOf<T>::MINB;
+    __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &a, Op &op) {
+        const int it = batch_iter(a);
+        if (it > a.max_iter) return false;
+        const int rc = richardson_parity(it - 1, a.p);
+        const long long off = (long long)((it - 1) % a.m) * I.g.n;
+        op = Op{rbuf(I, rc), I.x, rbuf(I, rc ^ 1), I.dx + off, I.df + off, I.c, I.cf, T(a.beta), nullptr, C.ctrl};
+        return true;
+    }
+    __device__ static Weights<TS> weights(const BInst<T> &I) { return I.w; }
+};
+
+template <typename T>
+struct PassRich {  // AAR.c:93-107,134-139, x and r ping-pong
+    using TS = T;
+    using Op = RichOp<T, RICH_AAR>;
+    static constexpr int MINB = TileOf<T>::MINB;
+    __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &a, Op &op) {
+        const int it = batch_iter(a);
+        if (it > a.max_iter) return false;
+        const int rc = richardson_parity(it - 1, a.p);
+        const long long off = (long long)((it - 1) % a.m) * I.g.n;
+        T *xo = rc ? I.xalt : I.x, *xn = rc ? I.x : I.xalt;
+        op = Op{xo, rbuf(I, rc), I.b, xn, rbuf(I, rc ^ 1), I.dx + off, I.df + off, I.c, I.cf, T(a.beta),
+                nullptr, C.ctrl};
+        return true;
+    }
+    __device__ static Weights<TS> weights(const BInst<T> &I) { return I.w; }
+};
+
+template <typename T>
+struct PassResInit {  // AAR.c:80-82
+    using TS = T;
+    using Op = ResidualOp<T, RES_INIT>;
+    static constexpr int MINB = TileOf<T>::MINB;
+    __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &, Op &op) {
+        op = Op{I.x, I.b, I.r0, nullptr, nullptr, I.cf, T(0.0), C.part, C.ctrl};
+        return true;
+    }
+    __device__ static Weights<TS> weights(const BInst<T> &I) { return I.w; }
+};
+
+template <typename T>
+struct PassResAnderson {  // AAR.c:116-123, reference form
+    using TS = T;
+    using Op = ResidualOp<T, RES_ANDERSON>;
+    static constexpr int MINB = TileOf<T>::MINB;
+    __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &a, Op &op) {
+        const int it = batch_iter(a);
+        if (it > a.max_iter) return false;
+        const int rc = richardson_parity(it - 1, a.p);
+        const long long off = (long long)((it - 1) % a.m) * I.g.n;
+        op = Op{rc ? I.xalt : I.x, I.b, rbuf(I, rc), I.df + off, I.dx + off, I.cf, T(a.beta), C.part, C.ctrl};
+        return true;
+    }
+    __device__ static Weights<TS> weights(const BInst<T> &I) { return I.w; }
+};
+
+template <typename T>
+struct PassResRecur {  // AAR.c:116-123, residual recurrence on the step in xalt
+    using TS = T;
+    using Op = ResRecurOp<T>;
+    static constexpr int MINB = TileOf<T>::MINB;
+    __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &a, Op &op) {
+        const int it = batch_iter(a);
+        if (it > a.max_iter) return false;
+        const int rc = richardson_parity(it - 1, a.p);
+        const long long off = (long long)((it - 1) % a.m) * I.g.n;
+        op = Op{I.xalt, rbuf(I, rc), I.df + off, I.dx + off, I.cf, T(a.beta), C.part, C.ctrl};
+        return true;
+    }
+    __device__ static Weights<TS> weights(const BInst<T> &I) { return I.w; }
+};
+
+template <typename T>
+struct PassIrResidual {  // r = float(b64 - A x64) after iteration it (mixed solves)
+    using TS = typename WideOf<T>::type;
+    using Op = IrResidualOp<TS, T>;
+    static constexpr int MINB = 1;
+    __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &a, Op &op) {
+        if (!replace_gate(C, a)) return false;
+        const int it = batch_iter(a);
+        op = Op{I.x64, I.b64, rbuf(I, richardson_parity(it, a.p)), C.part, nullptr};
+        return true;
+    }
+    __device__ static Weights<TS> weights(const BInst<T> &I) { return I.w64; }
+};
+
+// ---------------------------------------------------------------- kernels
+
+template <typename T, int RQ, int BY, int NY, int MINB, bool GENERIC, class Pass>
+__global__ void __launch_bounds__(32 * BY, MINB) batch_stencil_kernel(const BInst<T> *tab, BArgs a) {
+    using TS = typename Pass::TS;
+    constexpr int FX = 32 + 2 * RQ;
+    constexpr int FY = BY * NY + 2 * RQ;
+    __shared__ TS smem[2][FX * FY];
+    const int i = a.map[blockIdx.x];
+    const BCtl &C = a.ctl[i];
+    const BInst<T> &I = tab[i];
+    typename Pass::Op op;
+    if (!Pass::make(I, C, a, op)) return;
+    if (op.skip()) return;
+    op.init();
+    const int lb = blockIdx.x - C.sblk0;
+    const int t = lb / I.tx;
+    const Weights<TS> w = Pass::weights(I);
+    stencil_march<TS, RQ, BY, NY, GENERIC>(I.g, w, I.lz, op, smem[0], smem[1], lb - t * I.tx, t % I.ty,
+                                           t / I.ty, lb);
+}
+
+// Batched stencil tile: the vector type's tile; the generic-radius path uses
+// one row per thread (NY = 1) so the widest staged plane stays in 48 KB.
+template <typename T, bool GENERIC>
+struct BTile {
+    static constexpr int BY = TileOf<T>::BY;
+    static constexpr int NY = GENERIC ? 1 : TileOf<T>::NY;
+};
+
+template <typename T, class Pass>
+cudaError_t launch_batch_stencil(const BInst<T> *tab, const BArgs &a, int grid, bool generic,
+                                 cudaStream_t s) {
+    if (grid <= 0) return cudaSuccess;
+    if (!generic) {
+        using Tl = BTile<T, false>;
+        batch_stencil_kernel<T, 6, Tl::BY, Tl::NY, Pass::MINB, false, Pass>
+            <<<grid, dim3(32, Tl::BY), 0, s>>>(tab, a);
+    } else {
+        using Tl = BTile<T, true>;
+        batch_stencil_kernel<T, LSG_MAX_RADIUS, Tl::BY, Tl::NY, 1, true, Pass>
+            <<<grid, dim3(32, Tl::BY), 0, s>>>(tab, a);
+    }
+    return cudaGetLastError();
+}
+
+template <typename T, int M>
+__global__ void __launch_bounds__(kReduceThreads) batch_gram_kernel(const BInst<T> *tab, BArgs a) {
+    constexpr int NV = (M * (M + 1)) / 2 + M;
+    const int i = a.map[blockIdx.x];
+    const BCtl &C = a.ctl[i];
+    const int it = batch_iter(a);
+    if (it > a.max_iter || solve_done(C.ctrl)) return;
+    const BInst<T> &I = tab[i];
+    const T *r = rbuf(I, richardson_parity(it - 1, a.p));
+    const long long lb = blockIdx.x - C.ublk0;
+    if constexpr (IsCplx<T>::value) {
+        gram_c_block<typename RealOf<T>::type, M>(I.df, r, I.g.n, C.part + lb * 2 * NV, lb, C.ublocks);
+    } else {
+        if (I.vec) gram_block<T, GRAM_SYM, M, true>(I.dx, I.df, r, I.g.n, C.part + lb * NV, lb, C.ublocks);
+        else gram_block<T, GRAM_SYM, M, false>(I.dx, I.df, r, I.g.n, C.part + lb * NV, lb, C.ublocks);
+    }
+}
+
+template <typename T, int M>
+__global__ void __launch_bounds__(kReduceThreads) batch_update_kernel(const BInst<T> *tab, BArgs a) {
+    const int i = a.map[blockIdx.x];
+    const BCtl &C = a.ctl[i];
+    const int it = batch_iter(a);
+    if (it > a.max_iter || solve_done(C.ctrl)) return;
+    const BInst<T> &I = tab[i];
+    const int rc = richardson_parity(it - 1, a.p);
+    T *x, *step;
+    if (IsRecur<T>::value) {
+        x = I.x;
+        step = I.xalt;  // the residual pass reads the step as its stencil input
+    } else {
+        x = rc ? I.xalt : I.x;
+        step = I.dx + (long long)((it - 1) % a.m) * I.g.n;  // completed by the residual pass
+    }
+    const long long lb = blockIdx.x - C.ublk0;
+    if constexpr (!IsCplx<T>::value) {
+        if (I.vec) {
+            aar_update_block<T, M, true>(a.m, x, rbuf(I, rc), I.dx, step, T(a.beta), I.cf, I.g.n, C.ctrl, lb,
+                                         C.ublocks);
+            return;
+        }
+    }
+    aar_update_block<T, M, false>(a.m, x, rbuf(I, rc), I.dx, step, T(a.beta), I.cf, I.g.n, C.ctrl, lb,
+                                  C.ublocks);
+}
+
+template <typename T, bool WIDE>
+__global__ void __launch_bounds__(kReduceThreads) batch_norm2_kernel(const BInst<T> *tab, BArgs a) {
+    using TV = typename std::conditional<WIDE, typename WideOf<T>::type, T>::type;
+    constexpr int W = AccWidth<TV>::value;
+    __shared__ double red[(kReduceThreads / 32) * W];
+    const int i = a.map[blockIdx.x];
+    const BCtl &C = a.ctl[i];
+    const BInst<T> &I = tab[i];
+    const TV *v;
+    if constexpr (WIDE) v = I.b64;
+    else v = I.b;
+    const long long lb = blockIdx.x - C.ublk0;
+    Acc<TV> acc;
+    acc.zero();
+    const long long stride = (long long)C.ublocks * blockDim.x;
+    for (long long j = lb * blockDim.x + threadIdx.x; j < I.g.n; j += stride) {
+        const TV u = ldg(v + j);
+        acc.add_prod(u, u);
+    }
+    Acc<TV> a1[1] = {acc};
+    block_reduce_store<1>(a1, red, C.part + lb * W);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) batch_ir_correct_kernel(const BInst<T> *tab, BArgs a) {
+    using TW = typename WideOf<T>::type;
+    const int i = a.map[blockIdx.x];
+    const BCtl &C = a.ctl[i];
+    if (!replace_gate(C, a)) return;
+    const BInst<T> &I = tab[i];
+    const long long lb = blockIdx.x - C.ublk0;
+    const long long stride = (long long)C.ublocks * blockDim.x;
+    TW *x = I.x64;
+    T *e = I.x;
+    for (long long j = lb * blockDim.x + threadIdx.x; j < I.g.n; j += stride) {
+        x[j] += (TW)e[j];
+        e[j] = T(0.0);
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+
+template <typename T>
+int BatchKernels<T>::tile_y(bool generic) {
+    return generic ? BTile<T, true>::BY * BTile<T, true>::NY : BTile<T, false>::BY * BTile<T, false>::NY;
+}
+
+template <typename T>
+int BatchKernels<T>::stencil_blocks_per_sm(bool generic) {
+    int n = 0;
+    cudaError_t e;
+    using P = typename std::conditional<IsRecur<T>::value, PassRichRecur<T>, PassRich<T>>::type;
+    if (!generic) {
+        using Tl = BTile<T, false>;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &n, batch_stencil_kernel<T, 6, Tl::BY, Tl::NY, P::MINB, false, P>, 32 * Tl::BY, 0);
+    } else {
+        using Tl = BTile<T, true>;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &n, batch_stencil_kernel<T, LSG_MAX_RADIUS, Tl::BY, Tl::NY, 1, true, P>, 32 * Tl::BY, 0);
+    }
+    if (e != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        n = 1;
+    }
+    return n;
+}
+
+template <typename T>
+cudaError_t BatchKernels<T>::richardson(const BInst<T> *tab, const BArgs &a, int grid, bool generic,
+                                        cudaStream_t s) {
+    if constexpr (IsRecur<T>::value) return launch_batch_stencil<T, PassRichRecur<T>>(tab, a, grid, generic, s);
+    else return launch_batch_stencil<T, PassRich<T>>(tab, a, grid, generic, s);
+}
+
+template <typename T>
+cudaError_t BatchKernels<T>::residual_init(const BInst<T> *tab, const BArgs &a, int grid, bool generic,
+                                           cudaStream_t s) {
+    return launch_batch_stencil<T, PassResInit<T>>(tab, a, grid, generic, s);
+}
+
+template <typename T>
+cudaError_t BatchKernels<T>::residual_anderson(const BInst<T> *tab, const BArgs &a, int grid, bool generic,
+                                               cudaStream_t s) {
+    if constexpr (IsRecur<T>::value) return launch_batch_stencil<T, PassResRecur<T>>(tab, a, grid, generic, s);
+    else return launch_batch_stencil<T, PassResAnderson<T>>(tab, a, grid, generic, s);
+}
+
+template <typename T>
+cudaError_t BatchKernels<T>::ir_residual(const BInst<T> *tab, const BArgs &a, int grid, bool generic,
+                                         cudaStream_t s) {
+    if constexpr (IsRecur<T>::value) return launch_batch_stencil<T, PassIrResidual<T>>(tab, a, grid, generic, s);
+    else return cudaErrorInvalidValue;
+}
+
+template <typename T>
+cudaError_t BatchKernels<T>::gram(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s) {
+    if (grid <= 0) return cudaSuccess;
+    switch (a.m) {
+#define LSG_BGRAM(MM) case MM: batch_gram_kernel<T, MM><<<grid, kReduceThreads, 0, s>>>(tab, a); break;
+        LSG_BGRAM(1) LSG_BGRAM(2) LSG_BGRAM(3) LSG_BGRAM(4) LSG_BGRAM(5) LSG_BGRAM(6) LSG_BGRAM(7) LSG_BGRAM(8)
+#undef LSG_BGRAM
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t BatchKernels<T>::update(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s) {
+    if (grid <= 0) return cudaSuccess;
+    switch (a.m) {
+#define LSG_BUPD(MM) case MM: batch_update_kernel<T, MM><<<grid, kReduceThreads, 0, s>>>(tab, a); break;
+        LSG_BUPD(1) LSG_BUPD(2) LSG_BUPD(3) LSG_BUPD(4) LSG_BUPD(5) LSG_BUPD(6) LSG_BUPD(7) LSG_BUPD(8)
+#undef LSG_BUPD
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t BatchKernels<T>::norm2_rhs(const BInst<T> *tab, const BArgs &a, int grid, bool wide, cudaStream_t s) {
+    if (grid <= 0) return cudaSuccess;
+    if (wide) batch_norm2_kernel<T, true><<<grid, kReduceThreads, 0, s>>>(tab, a);
+    else batch_norm2_kernel<T, false><<<grid, kReduceThreads, 0, s>>>(tab, a);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t BatchKernels<T>::ir_correct(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s) {
+    if (grid <= 0) return cudaSuccess;
+    if constexpr (IsRecur<T>::value) {
+        batch_ir_correct_kernel<T><<<grid, kReduceThreads, 0, s>>>(tab, a);
+        return cudaGetLastError();
+    } else {
+        return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace lsg

@@ -16,7 +16,7 @@ namespace lsg {
 template <typename R>
 struct alignas(2 * sizeof(R)) cplx {
     R x, y;
-    __host__ __device__ cplx() = default;
+    cplx() = default;
     __host__ __device__ constexpr cplx(R re, R im = R(0)) : x(re), y(im) {}
     template <typename S>
     __host__ __device__ explicit cplx(const cplx<S> &o) : x((R)o.x), y((R)o.y) {}

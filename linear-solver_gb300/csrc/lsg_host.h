@@ -27,5 +27,11 @@ int solve_mixed_c(const lsg_operator *op, const lsg_params *prm, void *x, const 
 int apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, cudaStream_t s);
 int pinv(const double *A, const double *b, double *x, int m, cudaStream_t s);
 int release_workspaces();
+// Batched AAR (lsg_batch.cu).
+int solve_batched(const lsg_operator *ops, int count, const lsg_params *prm, int dtype, void *const *xs,
+                  const void *const *bs, lsg_result *res, cudaStream_t s);
+int solve_mixed_batched(const lsg_operator *ops, int count, const lsg_params *prm, int dtype, void *const *xs,
+                        const void *const *bs, lsg_result *res, cudaStream_t s);
+int release_batch_workspaces();
 
 }  // namespace lsg

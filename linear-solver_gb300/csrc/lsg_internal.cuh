@@ -6,6 +6,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "../../include/lsg.h"
 #include "lsg_complex.cuh"
@@ -21,7 +22,7 @@ struct DevCtrl {
     int done;         // 1: converged, failed or stopped -> later kernels are no-ops
     int status;       // lsg_status raised on the device (NaN, SVD sweep limit)
     int iters;        // reference iteration count at exit (AAR.c:153 reports iter-1)
-    int pad0;
+    int restarts;     // mixed solves: FP32 runs started (outer control block only)
     double rhs_norm;  // ||b||
     double tol_abs;   // tol * ||b||  (AAR.c:79)
     double relres;    // last computed ||r|| (absolute)
@@ -64,6 +65,42 @@ struct Weights {
     T w[LSG_MAX_RADIUS + 1];
     int radius;
 };
+
+// Host: weights and Jacobi factor of an operator in a vector type.
+template <typename T>
+inline Weights<T> make_weights(const lsg_operator *op) {
+    Weights<T> w;
+    memset(&w, 0, sizeof(w));
+    w.radius = op->radius;
+    if constexpr (IsCplx<T>::value) {
+        w.w[0] = T(op->a * 3.0 * op->coeff[0] + op->sigma, op->sigma_im);
+        for (int p = 1; p <= op->radius; p++) w.w[p] = T(op->a * op->coeff[p], 0.0);
+    } else {
+        w.w[0] = (T)(op->a * 3.0 * op->coeff[0] + op->sigma);
+        for (int p = 1; p <= op->radius; p++) w.w[p] = (T)(op->a * op->coeff[p]);
+    }
+    return w;
+}
+
+// Jacobi factor cf = 1 / diag (or 1 without preconditioning), in the
+// vector type's host scalar: the complex shift makes it complex.
+template <typename T>
+inline typename ScalarOf<T>::type jacobi_factor(const lsg_operator *op) {
+    if constexpr (IsCplx<T>::value) {
+        if (!op->precond) return cplx<double>(1.0, 0.0);
+        const double dr = op->a * (3 * op->coeff[0]) + op->sigma, di = op->sigma_im;
+        const double den = dr * dr + di * di;
+        return cplx<double>(dr / den, -di / den);
+    } else {
+        return op->precond ? 1.0 / (op->a * (3 * op->coeff[0]) + op->sigma) : 1.0;
+    }
+}
+
+// Host helpers of lsg_solvers.cu.
+int sm_count();
+int check_params(const lsg_params *prm, bool history);
+// Initial control block: relres = tol + 1 (AAR.c:76), stall rule off (0) or on.
+DevCtrl ctrl_init(double tol, int stall_limit);
 
 // ----------------------------------------------------------------------------
 // Reductions.  Every reducing kernel writes one partial per block (FP64) to a
@@ -257,6 +294,107 @@ cudaError_t finalize_cg(const double *partials, int nparts, DevCtrl *ctrl, int m
                         int precond, int iter, int max_iter, cudaStream_t s);
 cudaError_t pinv_solve_dev(const double *A, const double *b, double *x, int m, int *status,
                            cudaStream_t s);
+
+// ----------------------------------------------------------------------------
+// Batched solves (lsg_batch.cu).  All instances of a batch advance in
+// lockstep through the same iteration numbers; every launch covers all active
+// instances.  A block finds its instance through a block -> instance map and
+// its share of the instance's work through the first-block / block-count
+// fields of that instance's BCtl.  Finished instances are skipped through
+// their DevCtrl flags, exactly as single solves skip queued work.
+
+template <typename T> struct WideOf { using type = T; };
+template <> struct WideOf<float> { using type = double; };
+template <> struct WideOf<cplx<float>> { using type = cplx<double>; };
+
+// Parity of the residual ping-pong after iterations 1..last (the Richardson
+// iterations among them flip it; iteration 1 is one even when p = 1).
+__host__ __device__ inline int richardson_parity(int last, int p) {
+    if (last < 1) return 0;
+    return (last - last / p + (p == 1 ? 1 : 0)) & 1;
+}
+
+struct BClock {
+    int it0;     // iterations covered by the cycles already run
+    int ndone;   // finished instances (written by the cycle's last kernel)
+    int pad[2];
+};
+
+// Type-independent part of an instance record.
+struct BCtl {
+    DevCtrl *ctrl;       // the AAR iteration (the FP32 one of a mixed solve)
+    DevCtrl *octrl;      // mixed solves: the FP64 refinement; else nullptr
+    double *part;        // this instance's partial sums
+    long long n;
+    int sblk0, sblocks;  // its share of the batched stencil launches
+    int ublk0, ublocks;  // its share of the batched point-local launches
+    double hre, him;     // scale of the Gram right-hand side (the Jacobi factor)
+};
+
+template <typename T>
+struct BInst {
+    Geom g;
+    int tx, ty, lz;      // stencil tiles along x and y; z planes per block
+    int vec;             // n is a multiple of the 16-byte vector width
+    Weights<T> w;
+    Weights<typename WideOf<T>::type> w64;
+    T cf, c;             // Jacobi factor, omega * cf
+    T *x, *xalt, *r0, *r1, *dx, *df;
+    const T *b;
+    typename WideOf<T>::type *x64;        // mixed: the FP64 iterate and rhs
+    const typename WideOf<T>::type *b64;
+};
+
+struct BArgs {
+    const BCtl *ctl;
+    const int *map;      // block -> instance
+    const BClock *clk;
+    int k;               // position in the cycle: iteration it = clk->it0 + k + 1
+    int m, p, max_iter;
+    double beta;
+    int gate;            // refinement passes: 0 = paused instances, 1 = every unfinished one
+};
+
+template <typename T>
+struct BatchKernels {
+    // Resident blocks per SM of the batched Richardson pass.
+    static int stencil_blocks_per_sm(bool generic);
+    // Tile height of the batched stencil passes.
+    static int tile_y(bool generic);
+    // Richardson iteration k of the cycle (residual-recurrence form for FP32
+    // vectors, the reference form for FP64 ones).
+    static cudaError_t richardson(const BInst<T> *tab, const BArgs &a, int grid, bool generic, cudaStream_t s);
+    // r0 = b - A x, ||r0||^2 partials.
+    static cudaError_t residual_init(const BInst<T> *tab, const BArgs &a, int grid, bool generic, cudaStream_t s);
+    // The extrapolation iteration's residual, history column and ||r||^2.
+    static cudaError_t residual_anderson(const BInst<T> *tab, const BArgs &a, int grid, bool generic, cudaStream_t s);
+    static cudaError_t gram(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s);
+    static cudaError_t update(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s);
+    // ||b||^2 partials (wide: the FP64 rhs of a mixed solve).
+    static cudaError_t norm2_rhs(const BInst<T> *tab, const BArgs &a, int grid, bool wide, cudaStream_t s);
+    // Mixed solves: r = float(b64 - A x64) into the current residual buffer.
+    static cudaError_t ir_residual(const BInst<T> *tab, const BArgs &a, int grid, bool generic, cudaStream_t s);
+    // Mixed solves: x64 += e; e = 0.
+    static cudaError_t ir_correct(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s);
+};
+
+// Batched finalize kernels (lsg_small.cu): one block per active instance.
+enum BatchFinal {
+    BF_RHS = 0,          // ctrl: rhs norm from point-local partials
+    BF_RHS_OUTER = 1,    // octrl: rhs norm from point-local partials
+    BF_CHECK = 2,        // ctrl: convergence test after the extrapolation iteration
+    BF_REPLACE = 3,      // octrl: FP64 residual norm of a refinement (gated)
+};
+cudaError_t batch_finalize_norm(const BArgs &a, const int *amap, int nact, int kind, double tol,
+                                int width, cudaStream_t s);
+cudaError_t batch_finalize_gram(const BArgs &a, const int *amap, int nact, bool complex_gram,
+                                cudaStream_t s);
+// Mixed solves: resume paused FP32 iterations (gated) with their next target.
+cudaError_t batch_resume(const BArgs &a, const int *amap, int nact, double rho, int max_outer,
+                         cudaStream_t s);
+// it0 += p; ndone = finished instances; the int after the BClock of
+// instance i = 1 if it finished.
+cudaError_t batch_tick(BClock *clk, const BCtl *ctl, int count, int p, bool mixed, cudaStream_t s);
 
 // Number of Gram values per block for a kind and history depth.
 __host__ __device__ inline int gram_values(int kind, int m) {

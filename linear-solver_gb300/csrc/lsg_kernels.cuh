@@ -284,7 +284,7 @@ template <typename T> struct Vec4;
 template <> struct Vec4<float> { using type = float4; static constexpr int N = 4; };
 template <> struct Vec4<double> { using type = double2; static constexpr int N = 2; };
 
-template <typename V> __device__ __forceinline__ V ldv(const V *p) { return __ldg(p); }
+template <typename V> __device__ __forceinline__ V ldv(const V *p) { return ldg(p); }
 
 __device__ __forceinline__ float dotv(const float4 &a, const float4 &b) {
     float p = a.x * b.x;
@@ -298,27 +298,33 @@ __device__ __forceinline__ void accv(Acc<double> &acc, const double2 &a, const d
     acc.add_prod(a.y, b.y);
 }
 
-template <typename T, int KIND, int M>
-__global__ void __launch_bounds__(kReduceThreads) gram_kernel(const T *__restrict__ dx,
-                                                              const T *__restrict__ df,
-                                                              const T *__restrict__ r, long long n,
-                                                              double *partials,
-                                                              const DevCtrl *ctrl) {
-    using V = typename Vec4<T>::type;
-    constexpr int VN = Vec4<T>::N;
+__device__ __forceinline__ void accv(Acc<float> &acc, float a, float b) { acc.add_prod(a, b); }
+__device__ __forceinline__ void accv(Acc<double> &acc, double a, double b) { acc.add_prod(a, b); }
+
+// Loads of VN consecutive values (VEC) or of one value.
+template <typename T, bool VEC> struct VecLoad { using type = T; static constexpr int N = 1; };
+template <typename T> struct VecLoad<T, true> { using type = typename Vec4<T>::type; static constexpr int N = Vec4<T>::N; };
+
+// One block's share of the Gram sums: block `blk` of `nblk` covering points
+// 0..n-1 of the history (grid-stride), NV sums written to out[0..NV).
+template <typename T, int KIND, int M, bool VEC>
+__device__ __forceinline__ void gram_block(const T *__restrict__ dx, const T *__restrict__ df,
+                                           const T *__restrict__ r, long long n, double *out,
+                                           long long blk, long long nblk) {
+    using V = typename VecLoad<T, VEC>::type;
+    constexpr int VN = VecLoad<T, VEC>::N;
     constexpr int NP = (KIND == GRAM_SYM) ? (M * (M + 1)) / 2 : M * M;
     constexpr int NV = NP + M;
     __shared__ double red[NV * (kReduceThreads / 32)];
-    if (solve_done(ctrl)) return;
     Acc<T> acc[NV];
 #pragma unroll
     for (int k = 0; k < NV; k++) acc[k].zero();
-    const long long nv = n / VN;  // caller guarantees n % VN == 0
+    const long long nv = n / VN;  // VEC: caller guarantees n % VN == 0
     const V *dfv = reinterpret_cast<const V *>(df);
     const V *dxv = reinterpret_cast<const V *>(dx);
     const V *rvv = reinterpret_cast<const V *>(r);
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride) {
+    const long long stride = nblk * blockDim.x;
+    for (long long i = blk * blockDim.x + threadIdx.x; i < nv; i += stride) {
         V f[M], xv[KIND == GRAM_SYM ? 1 : M];
 #pragma unroll
         for (int j = 0; j < M; j++) f[j] = ldv(dfv + j * nv + i);
@@ -344,7 +350,18 @@ __global__ void __launch_bounds__(kReduceThreads) gram_kernel(const T *__restric
             for (int j = 0; j < M; j++) accv(acc[NP + j], xv[j], rv);
         }
     }
-    block_reduce_store<NV>(acc, red, partials + (long long)blockIdx.x * NV);
+    block_reduce_store<NV>(acc, red, out);
+}
+
+template <typename T, int KIND, int M>
+__global__ void __launch_bounds__(kReduceThreads) gram_kernel(const T *__restrict__ dx,
+                                                              const T *__restrict__ df,
+                                                              const T *__restrict__ r, long long n,
+                                                              double *partials,
+                                                              const DevCtrl *ctrl) {
+    constexpr int NV = ((KIND == GRAM_SYM) ? (M * (M + 1)) / 2 : M * M) + M;
+    if (solve_done(ctrl)) return;
+    gram_block<T, KIND, M, true>(dx, df, r, n, partials + (long long)blockIdx.x * NV, blockIdx.x, gridDim.x);
 }
 
 // Generic Gram (any m <= LSG_MAX_M): one value per (block, thread-slot), the
@@ -393,22 +410,20 @@ __global__ void __launch_bounds__(kReduceThreads) gram_generic_kernel(int kind, 
 // M: history depth known at compile time (all m loads in flight at once),
 // VN points per thread and step through 16-byte vectors; M = 0 is the
 // generic path (runtime m, scalar).
-template <typename T, int M>
-__global__ void __launch_bounds__(kReduceThreads) aar_update_kernel(int m, T *__restrict__ x,
-                                                                    const T *__restrict__ r,
-                                                                    const T *__restrict__ h,
-                                                                    T *__restrict__ step, T beta,
-                                                                    T cf, long long n,
-                                                                    const DevCtrl *ctrl) {
+template <typename T, int M, bool VEC>
+__device__ __forceinline__ void aar_update_block(int m, T *__restrict__ x, const T *__restrict__ r,
+                                                 const T *__restrict__ h, T *__restrict__ step,
+                                                 T beta, T cf, long long n, const DevCtrl *ctrl,
+                                                 long long blk, long long nblk) {
     __shared__ T s[LSG_MAX_M];
-    if (solve_done(ctrl)) return;
     if (threadIdx.x < m) s[threadIdx.x] = ctrl_s<T>(ctrl, threadIdx.x);
     __syncthreads();
-    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long stride = nblk * blockDim.x;
+    const long long t0 = blk * blockDim.x + threadIdx.x;
     if constexpr (M > 0) {
-        using V = typename Vec4<T>::type;
-        constexpr int VN = Vec4<T>::N;
-        const long long nv = n / VN;  // caller guarantees n % VN == 0
+        using V = typename VecLoad<T, VEC>::type;
+        constexpr int VN = VecLoad<T, VEC>::N;
+        const long long nv = n / VN;  // VEC: caller guarantees n % VN == 0
         const V *hv = reinterpret_cast<const V *>(h);
         V *xv = reinterpret_cast<V *>(x);
         const V *rv = reinterpret_cast<const V *>(r);
@@ -416,12 +431,12 @@ __global__ void __launch_bounds__(kReduceThreads) aar_update_kernel(int m, T *__
         T sj[M];
 #pragma unroll
         for (int j = 0; j < M; j++) sj[j] = s[j];
-        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride) {
+        for (long long i = t0; i < nv; i += stride) {
             V hj[M];
 #pragma unroll
             for (int j = 0; j < M; j++) hj[j] = ldv(hv + j * nv + i);
             const V xo = xv[i], ro = rv[i];
-            T *xs = (T *)&xo;
+            const T *xs = (const T *)&xo;
             const T *rs = (const T *)&ro;
             V xn, st;
             T *xns = (T *)&xn, *sts = (T *)&st;
@@ -437,7 +452,7 @@ __global__ void __launch_bounds__(kReduceThreads) aar_update_kernel(int m, T *__
             sv[i] = st;
         }
     } else {
-        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        for (long long i = t0; i < n; i += stride) {
             T am = T(0);
             for (int j = 0; j < m; j++) am = fma(ldg(h + j * n + i), s[j], am);
             const T xo = x[i];
@@ -446,6 +461,22 @@ __global__ void __launch_bounds__(kReduceThreads) aar_update_kernel(int m, T *__
             step[i] = xn - xo;
         }
     }
+}
+
+// x_new = x + beta cf r - sum_j H_j s_j with H_j = DX_j + beta DF_j
+// (AAR.c:116-117, 225-231); the step x_new - x_old goes to `step`.
+// M: history depth known at compile time (all m loads in flight at once),
+// VN points per thread and step through 16-byte vectors; M = 0 is the
+// generic path (runtime m, scalar).
+template <typename T, int M>
+__global__ void __launch_bounds__(kReduceThreads) aar_update_kernel(int m, T *__restrict__ x,
+                                                                    const T *__restrict__ r,
+                                                                    const T *__restrict__ h,
+                                                                    T *__restrict__ step, T beta,
+                                                                    T cf, long long n,
+                                                                    const DevCtrl *ctrl) {
+    if (solve_done(ctrl)) return;
+    aar_update_block<T, M, (M > 0)>(m, x, r, h, step, beta, cf, n, ctrl, blockIdx.x, gridDim.x);
 }
 
 template <typename T>
@@ -583,22 +614,19 @@ cudaError_t Kernels<T>::residual_recur(const StencilLaunch &L, const Weights<T> 
     return launch_stencil<T>(L, w, op);
 }
 
-// Hermitian Gram for complex vectors (PETSC_COMPLEX/AAR_Complex.c:213-216):
-// G(a,j) = DF_a^H DF_j (a <= j), h_j = DF_j^H r; M compile-time history depth.
+// One block's share of the Hermitian Gram sums (2 reals per value).
 template <typename R, int M>
-__global__ void __launch_bounds__(kReduceThreads) gram_c_kernel(const cplx<R> *__restrict__ df,
-                                                                const cplx<R> *__restrict__ r,
-                                                                long long n, double *partials,
-                                                                const DevCtrl *ctrl) {
+__device__ __forceinline__ void gram_c_block(const cplx<R> *__restrict__ df,
+                                             const cplx<R> *__restrict__ r, long long n,
+                                             double *out, long long blk, long long nblk) {
     constexpr int NP = (M * (M + 1)) / 2;
     constexpr int NV = NP + M;
     __shared__ double red[2 * NV * (kReduceThreads / 32)];
-    if (solve_done(ctrl)) return;
     Acc<cplx<R>> acc[NV];
 #pragma unroll
     for (int k = 0; k < NV; k++) acc[k].zero();
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const long long stride = nblk * blockDim.x;
+    for (long long i = blk * blockDim.x + threadIdx.x; i < n; i += stride) {
         cplx<R> f[M];
 #pragma unroll
         for (int j = 0; j < M; j++) f[j] = ldg(df + j * n + i);
@@ -611,7 +639,19 @@ __global__ void __launch_bounds__(kReduceThreads) gram_c_kernel(const cplx<R> *_
 #pragma unroll
         for (int j = 0; j < M; j++) acc[NP + j].add_prod(f[j], rv);
     }
-    block_reduce_store<NV>(acc, red, partials + (long long)blockIdx.x * 2 * NV);
+    block_reduce_store<NV>(acc, red, out);
+}
+
+// Hermitian Gram for complex vectors (PETSC_COMPLEX/AAR_Complex.c:213-216):
+// G(a,j) = DF_a^H DF_j (a <= j), h_j = DF_j^H r; M compile-time history depth.
+template <typename R, int M>
+__global__ void __launch_bounds__(kReduceThreads) gram_c_kernel(const cplx<R> *__restrict__ df,
+                                                                const cplx<R> *__restrict__ r,
+                                                                long long n, double *partials,
+                                                                const DevCtrl *ctrl) {
+    constexpr int NV = (M * (M + 1)) / 2 + M;
+    if (solve_done(ctrl)) return;
+    gram_c_block<R, M>(df, r, n, partials + (long long)blockIdx.x * 2 * NV, blockIdx.x, gridDim.x);
 }
 
 template <typename T, int KIND>

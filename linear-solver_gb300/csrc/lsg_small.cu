@@ -47,10 +47,9 @@ __device__ double block_sum_partials(const double *partials, int nparts, int str
     return t;  // valid in warp 0
 }
 
-__global__ void finalize_norm_kernel(const double *partials, int nparts, DevCtrl *ctrl, int mode,
-                                     double tol, int iter, int width) {
+__device__ void finalize_norm_body(const double *partials, int nparts, DevCtrl *ctrl, int mode,
+                                   double tol, int iter, int width) {
     __shared__ double red[32];
-    if (mode != NF_RHS && ctrl_done(ctrl)) return;
     const double s = block_sum_partials(partials, nparts, width, 0, red);
     if (threadIdx.x != 0) return;
     const double v = sqrt(s);
@@ -80,6 +79,12 @@ __global__ void finalize_norm_kernel(const double *partials, int nparts, DevCtrl
             }
         }
     }
+}
+
+__global__ void finalize_norm_kernel(const double *partials, int nparts, DevCtrl *ctrl, int mode,
+                                     double tol, int iter, int width) {
+    if (mode != NF_RHS && ctrl_done(ctrl)) return;
+    finalize_norm_body(partials, nparts, ctrl, mode, tol, iter, width);
 }
 
 // ---------------------------------------------------------------- m x m solve
@@ -369,14 +374,13 @@ __device__ int warp_pinv_any(double *G, double *V, const double *b, double *x, i
     return warp_pinv(G, V, b, x, m, cut);
 }
 
-__global__ void finalize_gram_solve_kernel(const double *partials, int nparts, int kind, int m,
-                                           double hscale, DevCtrl *ctrl) {
+__device__ void gram_solve_body(const double *partials, int nparts, int kind, int m, double hscale,
+                                DevCtrl *ctrl) {
     __shared__ double vals[LSG_MAX_M * LSG_MAX_M + LSG_MAX_M];
     __shared__ double G[LSG_MAX_M * LSG_MAX_M], V[LSG_MAX_M * LSG_MAX_M];
     __shared__ double Gs[LSG_MAX_M * LSG_MAX_M], Vs[64];
     __shared__ double h[LSG_MAX_M], s[LSG_MAX_M], dd[LSG_MAX_M];
     __shared__ int bad;
-    if (ctrl_done(ctrl)) return;
     const int nv = gram_values(kind, m);
     const int np = nv - m;
     if (threadIdx.x == 0) bad = 0;
@@ -429,19 +433,24 @@ __global__ void finalize_gram_solve_kernel(const double *partials, int nparts, i
     }
 }
 
+__global__ void finalize_gram_solve_kernel(const double *partials, int nparts, int kind, int m,
+                                           double hscale, DevCtrl *ctrl) {
+    if (ctrl_done(ctrl)) return;
+    gram_solve_body(partials, nparts, kind, m, hscale, ctrl);
+}
+
 // Complex Hermitian Gram: sums the (re, im) partials, builds the real 2m x 2m
 // representation [[A, -B], [B, A]] of G = A + iB (same singular values, each
 // twice) and right-hand side [Re h; Im h], and solves it with zgelsd's cutoff
 // sigma < eps * sigma_max (PETSC_COMPLEX/AAR_Complex.c:239, rcond = -1).
-__global__ void finalize_gram_solve_c_kernel(const double *partials, int nparts, int m, double hre,
-                                             double him, DevCtrl *ctrl) {
+__device__ void gram_solve_c_body(const double *partials, int nparts, int m, double hre, double him,
+                                  DevCtrl *ctrl) {
     constexpr int M2MAX = LSG_MAX_M;
     __shared__ double vals[2 * (LSG_MAX_M * LSG_MAX_M + LSG_MAX_M)];
     __shared__ double G[M2MAX * M2MAX], V[M2MAX * M2MAX], W[M2MAX * M2MAX];
     __shared__ double Gs[64], Vs[64];
     __shared__ double h[M2MAX], s[M2MAX], dd[M2MAX];
     __shared__ int bad;
-    if (ctrl_done(ctrl)) return;
     const int np = (m * (m + 1)) / 2;
     const int nvr = 2 * (np + m);  // reals per block partial
     const int m2 = 2 * m;
@@ -496,6 +505,100 @@ __global__ void finalize_gram_solve_c_kernel(const double *partials, int nparts,
             if (bad) { ctrl->status = LSG_NAN_DETECTED; ctrl->done = 1; }
             else if (st) ctrl->status = st;
         }
+    }
+}
+
+__global__ void finalize_gram_solve_c_kernel(const double *partials, int nparts, int m, double hre,
+                                             double him, DevCtrl *ctrl) {
+    if (ctrl_done(ctrl)) return;
+    gram_solve_c_body(partials, nparts, m, hre, him, ctrl);
+}
+
+// ---------------------------------------------------------------- batched finalize
+// One block per active instance (amap[blockIdx.x]); the iteration number comes
+// from the batch clock as in the batched stencil passes.
+
+__global__ void batch_finalize_norm_kernel(BArgs a, const int *amap, int kind, double tol, int width) {
+    const int i = amap[blockIdx.x];
+    const BCtl &C = a.ctl[i];
+    const int it = a.clk->it0 + a.k + 1;
+    switch (kind) {
+    case BF_RHS:
+        finalize_norm_body(C.part, C.ublocks, C.ctrl, NF_RHS, tol, 0, width);
+        break;
+    case BF_RHS_OUTER:
+        finalize_norm_body(C.part, C.ublocks, C.octrl, NF_RHS, tol, 0, width);
+        break;
+    case BF_CHECK:
+        if (it > a.max_iter || ctrl_done(C.ctrl)) return;
+        finalize_norm_body(C.part, C.sblocks, C.ctrl, NF_CHECK, tol, it, width);
+        break;
+    default:  // BF_REPLACE
+        if (ctrl_done(C.octrl) || !(a.gate == 1 || ctrl_done(C.ctrl))) return;
+        finalize_norm_body(C.part, C.sblocks, C.octrl, NF_CHECK, tol, it, width);
+    }
+}
+
+__global__ void batch_finalize_gram_kernel(BArgs a, const int *amap, int cplx_gram) {
+    const int i = amap[blockIdx.x];
+    const BCtl &C = a.ctl[i];
+    const int it = a.clk->it0 + a.k + 1;
+    if (it > a.max_iter || ctrl_done(C.ctrl)) return;
+    if (cplx_gram) gram_solve_c_body(C.part, C.ublocks, a.m, C.hre, C.him, C.ctrl);
+    else gram_solve_body(C.part, C.ublocks, GRAM_SYM, a.m, C.hre, C.ctrl);
+}
+
+// Thread per active instance.  A paused FP32 iteration whose FP64 residual
+// did not meet tol resumes with the target max(tol_abs, rho * relres) and a
+// fresh stall record -- or the instance stops: NaN in the FP32 iteration, or
+// max_outer runs used.
+__global__ void batch_resume_kernel(BArgs a, const int *amap, int nact, double rho, int max_outer) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nact) return;
+    const BCtl &C = a.ctl[amap[t]];
+    DevCtrl *in = C.ctrl, *out = C.octrl;
+    if (out->done || !in->done) return;
+    const int it = a.clk->it0 + a.k + 1;
+    if (in->status == LSG_NAN_DETECTED) {
+        out->status = LSG_NAN_DETECTED;
+        out->done = 1;
+        out->iters = it;
+        return;
+    }
+    if (out->restarts >= max_outer) {
+        out->done = 1;
+        out->iters = it;
+        return;
+    }
+    out->restarts++;
+    in->stall = 0;
+    in->stalled = 0;
+    in->best = __longlong_as_double(0x7ff0000000000000LL);  // +inf
+    in->tol_abs = fmax(out->tol_abs, rho * out->relres);
+    in->rhs_norm = out->rhs_norm;
+    __threadfence();
+    in->done = 0;
+}
+
+__global__ void batch_tick_kernel(BClock *clk, const BCtl *ctl, int count, int p, int mixed) {
+    __shared__ int red[32];
+    int *flags = reinterpret_cast<int *>(clk + 1);
+    int c = 0;
+    for (int i = threadIdx.x; i < count; i += blockDim.x) {
+        const DevCtrl *d = mixed ? ctl[i].octrl : ctl[i].ctrl;
+        const int f = ctrl_done(d) ? 1 : 0;
+        flags[i] = f;
+        c += f;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int tot = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += red[w];
+        clk->ndone = tot;
+        clk->it0 += p;
     }
 }
 
@@ -565,6 +668,33 @@ cudaError_t finalize_gram_solve_c(const double *partials, int nparts, int m, cpl
 cudaError_t finalize_cg(const double *partials, int nparts, DevCtrl *ctrl, int mode, double cf,
                         int precond, int iter, int max_iter, cudaStream_t s) {
     finalize_cg_kernel<<<1, kFinThreads, 0, s>>>(partials, nparts, ctrl, mode, cf, precond, iter, max_iter);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_finalize_norm(const BArgs &a, const int *amap, int nact, int kind, double tol,
+                                int width, cudaStream_t s) {
+    if (nact <= 0) return cudaSuccess;
+    batch_finalize_norm_kernel<<<nact, kFinThreads, 0, s>>>(a, amap, kind, tol, width);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_finalize_gram(const BArgs &a, const int *amap, int nact, bool complex_gram,
+                                cudaStream_t s) {
+    if (nact <= 0) return cudaSuccess;
+    if (complex_gram && 2 * a.m > LSG_MAX_M) return cudaErrorInvalidValue;
+    batch_finalize_gram_kernel<<<nact, kFinThreads, 0, s>>>(a, amap, complex_gram ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_resume(const BArgs &a, const int *amap, int nact, double rho, int max_outer,
+                         cudaStream_t s) {
+    if (nact <= 0) return cudaSuccess;
+    batch_resume_kernel<<<(nact + 127) / 128, 128, 0, s>>>(a, amap, nact, rho, max_outer);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_tick(BClock *clk, const BCtl *ctl, int count, int p, bool mixed, cudaStream_t s) {
+    batch_tick_kernel<<<1, 256, 0, s>>>(clk, ctl, count, p, mixed ? 1 : 0);
     return cudaGetLastError();
 }
 

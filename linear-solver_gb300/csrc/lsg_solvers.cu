@@ -60,7 +60,7 @@ const char *last_error() { return t_last_error; }
 
 // ---------------------------------------------------------------- device info
 
-static int sm_count() {
+int sm_count() {
     static std::mutex mu;
     static std::map<int, int> cache;
     int dev = 0;
@@ -206,9 +206,11 @@ static int get_workspace(size_t es, long long n, int m, bool mixed, const Geom &
 
 int release_workspaces() {
     cudaDeviceSynchronize();
-    std::lock_guard<std::mutex> gl(g_ws_mu);
-    g_ws.clear();
-    return LSG_OK;
+    {
+        std::lock_guard<std::mutex> gl(g_ws_mu);
+        g_ws.clear();
+    }
+    return release_batch_workspaces();
 }
 
 // ---------------------------------------------------------------- operator
@@ -242,36 +244,7 @@ int check_operator(const lsg_operator *op) {
 
 double jacobi_diag(const lsg_operator *op) { return op->a * (3 * op->coeff[0]) + op->sigma; }
 
-template <typename T>
-static Weights<T> make_weights(const lsg_operator *op) {
-    Weights<T> w;
-    memset(&w, 0, sizeof(w));
-    w.radius = op->radius;
-    if constexpr (IsCplx<T>::value) {
-        w.w[0] = T(op->a * 3.0 * op->coeff[0] + op->sigma, op->sigma_im);
-        for (int p = 1; p <= op->radius; p++) w.w[p] = T(op->a * op->coeff[p], 0.0);
-    } else {
-        w.w[0] = (T)(op->a * 3.0 * op->coeff[0] + op->sigma);
-        for (int p = 1; p <= op->radius; p++) w.w[p] = (T)(op->a * op->coeff[p]);
-    }
-    return w;
-}
-
-// Jacobi factor cf = 1 / diag (or 1 without preconditioning), in the
-// vector type's host scalar: the complex shift makes it complex.
-template <typename T>
-static typename ScalarOf<T>::type jacobi_factor(const lsg_operator *op) {
-    if constexpr (IsCplx<T>::value) {
-        if (!op->precond) return cplx<double>(1.0, 0.0);
-        const double dr = op->a * (3 * op->coeff[0]) + op->sigma, di = op->sigma_im;
-        const double den = dr * dr + di * di;
-        return cplx<double>(dr / den, -di / den);
-    } else {
-        return op->precond ? 1.0 / jacobi_diag(op) : 1.0;
-    }
-}
-
-static int check_params(const lsg_params *prm, bool history) {
+int check_params(const lsg_params *prm, bool history) {
     if (!prm) return set_error(LSG_BAD_ARG, "params is NULL");
     if (prm->max_iter < 0) return set_error(LSG_BAD_ARG, "max_iter %d < 0", prm->max_iter);
     if (!(prm->tol >= 0)) return set_error(LSG_BAD_ARG, "tol must be >= 0");
@@ -359,7 +332,7 @@ static int reduce_blocks(long long n, int sms) {
 
 // Initial DevCtrl contents.  relres starts at tol + 1 as in AAR.c:76, so a
 // solve stopped before its first check reports the reference's value.
-static DevCtrl ctrl_init(double tol, int stall_limit) {
+DevCtrl ctrl_init(double tol, int stall_limit) {
     DevCtrl c;
     memset(&c, 0, sizeof(c));
     c.relres = tol + 1.0;

@@ -55,9 +55,11 @@ __device__ __forceinline__ bool unrolled_steps(F &f) {
 
 // RQ: radius the storage is sized for; the arithmetic uses `radius` (== RQ on
 // the specialised path, <= RQ on the generic path).
+// (bx, by, bz): the block's tile (x, y) and z chunk; blk: where its partial sums go.
 template <typename T, int RQ, int BY, int NY, bool GENERIC, class Op>
 __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w, int lz, Op &op,
-                                              T *smem0, T *smem1) {
+                                              T *smem0, T *smem1, int bx, int by, int bz,
+                                              long long blk) {
     using Raw = typename Op::Raw;
     using Ctr = typename Op::Ctr;
     constexpr int TX = 32;
@@ -71,8 +73,8 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
     const int radius = GENERIC ? w.radius : RQ;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * 32 + tx;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-    const int z0 = blockIdx.z * lz;
+    const int x0 = bx * TX, y0 = by * TY;
+    const int z0 = bz * lz;
     const int z1 = min(z0 + lz, g.nz);
 
     // Owned columns (periodically wrapped, so partial tiles still hold valid data).
@@ -200,7 +202,6 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
         constexpr int NA = Op::NACC > 0 ? Op::NACC : 1;
         constexpr int W = AccWidth<T>::value;
         __shared__ double red[NA * W * 32];
-        const long long blk = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
         block_reduce_store<NA>(acc, red, op.partials + blk * Op::NACC * W);
     }
 }
@@ -212,7 +213,9 @@ __global__ void __launch_bounds__(32 * BY, MINB) stencil_kernel(Geom g, Weights<
     __shared__ T smem[2][FX * FY];
     if (op.skip()) return;
     op.init();
-    stencil_march<T, RQ, BY, NY, GENERIC>(g, w, lz, op, smem[0], smem[1]);
+    const long long blk = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+    stencil_march<T, RQ, BY, NY, GENERIC>(g, w, lz, op, smem[0], smem[1], blockIdx.x, blockIdx.y,
+                                          blockIdx.z, blk);
 }
 
 }  // namespace lsg

@@ -86,7 +86,7 @@ EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "ls
            "lsg_version", "AAR", "PGR", "PL2R", "CG", "lsg_register_operator_callback",
            "lsg_register_precondition_callback", "lsg_set_verbose", "lsg_last_result",
            "lsg_profile", "lsg_profile_read", "lsg_set_compat_mode", "lsg_aar_mixed_c",
-           "lsg_pinv_solve_noalloc"]
+           "lsg_pinv_solve_noalloc", "lsg_aar_batched", "lsg_aar_mixed_batched"]
 
 KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "unused"]
 
@@ -120,6 +120,9 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
         L.lsg_aar_mixed_c.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), vp, vp,
                                       C.POINTER(_Result), vp]
         L.lsg_pinv_solve.argtypes = [vp, vp, vp, ip, vp]
+        for f in ("lsg_aar_batched", "lsg_aar_mixed_batched"):
+            getattr(L, f).argtypes = [C.POINTER(_Operator), ip, C.POINTER(_Params), ip,
+                                      C.POINTER(vp), C.POINTER(vp), C.POINTER(_Result), vp]
         L.lsg_last_error.restype = C.c_char_p
         L.lsg_status_string.restype = C.c_char_p
         L.lsg_version.restype = C.c_char_p
@@ -301,6 +304,37 @@ def aar_mixed(op, b, x0=None, stream=None, **kw):
             C.byref(res), _stream_ptr(stream))
     _check(rc, "lsg_aar_mixed")
     return x, _result(res)
+
+
+def aar_batched(ops, bs, x0s=None, mixed=False, stream=None, **kw):
+    """Batched AAR: solve ops[i] x_i = bs[i] for every i in lockstep.
+
+    Each launch covers all unfinished instances and one extrapolation cycle
+    is replayed as a CUDA graph (include/lsg.h, lsg_aar_batched).  bs: CUDA
+    tensors of one dtype (float64 / float32 / complex128 / complex64; with
+    mixed=True float64 or complex128).  Returns (list of x, list of result dicts).
+    """
+    import torch
+    if len(ops) != len(bs) or not ops:
+        raise ValueError("ops and bs must be non-empty lists of equal length")
+    dt = bs[0].dtype
+    for i, (op, b) in enumerate(zip(ops, bs)):
+        _check_vec(b, op, f"bs[{i}]")
+        if b.dtype != dt:
+            raise TypeError("all right-hand sides must share one dtype")
+    if mixed and dt not in (torch.float64, torch.complex128):
+        raise TypeError("mixed batched AAR takes float64 or complex128 vectors")
+    xs = [torch.zeros_like(b) if x0s is None else x0s[i].clone() for i, b in enumerate(bs)]
+    count = len(ops)
+    arr = (_Operator * count)(*[op._s for op in ops])
+    xp = (C.c_void_p * count)(*[x.data_ptr() for x in xs])
+    bp = (C.c_void_p * count)(*[b.data_ptr() for b in bs])
+    res = (_Result * count)()
+    prm = _params(**kw)
+    fn = lib().lsg_aar_mixed_batched if mixed else lib().lsg_aar_batched
+    rc = fn(arr, count, C.byref(prm), _dtype_code(bs[0]), xp, bp, res, _stream_ptr(stream))
+    _check(rc, "lsg_aar_mixed_batched" if mixed else "lsg_aar_batched")
+    return xs, [_result(r) for r in res]
 
 
 def pinv_solve(A, b, stream=None):
