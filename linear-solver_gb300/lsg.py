@@ -458,52 +458,114 @@ def compat_solve(solver: str, x, rhs, *, n=None, fdn=6, a=A_REF, precond=True, o
 
 def _solve_for(precision: str, op: Operator, rhs, kw: dict):
     import torch
+    cplx = rhs.is_complex() or isinstance(op.sigma, complex)
+    hi, lo = (torch.complex128, torch.complex64) if cplx else (torch.float64, torch.float32)
     if precision == "mixed":
-        return aar_mixed(op, rhs.to(torch.float64).contiguous(), **kw)
+        return aar_mixed(op, rhs.to(hi).contiguous(), **kw)
     if precision == "fp64":
-        return aar(op, rhs.to(torch.float64).contiguous(), **kw)
+        return aar(op, rhs.to(hi).contiguous(), **kw)
     if precision == "fp32":
-        return aar(op, rhs.to(torch.float32).contiguous(), **kw)
+        return aar(op, rhs.to(lo).contiguous(), **kw)
     raise ValueError(precision)
 
 
-class _ShiftedSolve:
-    """x = A(sigma)^-1 b with A = a * Lap_h + sigma * I (real, symmetric).
+def _solve_batch_for(precision: str, ops, rhs, kw: dict):
+    """Batched solves of ops[i] x_i = rhs[i]; rhs (B, nz, ny, nx); returns (B, ...) and results."""
+    import torch
+    cplx = rhs.is_complex() or any(isinstance(op.sigma, complex) for op in ops)
+    hi, lo = (torch.complex128, torch.complex64) if cplx else (torch.float64, torch.float32)
+    if precision not in ("mixed", "fp64", "fp32"):
+        raise ValueError(precision)
+    dt = lo if precision == "fp32" else hi
+    bs = [rhs[i].to(dt).contiguous() for i in range(rhs.shape[0])]
+    xs, rs = aar_batched(ops, bs, mixed=(precision == "mixed"), **kw)
+    return torch.stack(xs), rs
 
-    Backward is the adjoint solve on the same kernels: A^T = A, so
-    lambda = A^-1 (dL/dx), dL/db = lambda and dL/dsigma = -lambda . x.
+
+def _raise_failed(what, infos):
+    bad = [(i, r) for i, r in enumerate(infos) if r["status"] != 0]
+    if bad:
+        i, r = bad[0]
+        raise CudaLibraryError(f"{what}: instance {i}: {r['status_name']} ({r})")
+
+
+class _ShiftedSolve:
+    """x = A(sigma)^-1 b with A = a * Lap_h + sigma * I.
+
+    A is symmetric (complex symmetric for complex sigma), so A^H is the same
+    stencil with conj(sigma).  Backward is the adjoint solve on the same
+    kernels: lambda = A^-H (dL/dx), dL/db = lambda, dL/dsigma = -sum conj(x) lambda
+    (real case: -lambda . x).  A leading batch dimension of b (with one sigma
+    per instance) runs the forward and adjoint solves as one batched solve.
     """
 
     @staticmethod
     def build():
         import torch
 
+        def conj_op(op):
+            return Operator(op.n, radius=op.radius, a=op.a, sigma=complex(op.sigma).conjugate()
+                            if isinstance(op.sigma, complex) else op.sigma, precond=op.precond)
+
         class Fn(torch.autograd.Function):
             @staticmethod
             def forward(ctx, b, sigma, grid, radius, a, precision, kw):
-                s = float(sigma.detach().cpu()) if torch.is_tensor(sigma) else float(sigma)
-                op = Operator(grid, radius=radius, a=a, sigma=s)
-                x, info = _solve_for(precision, op, b.detach(), kw)
-                if info["status"] != 0:
-                    raise CudaLibraryError(f"forward solve: {info['status_name']} ({info})")
-                x = x.to(b.dtype)
-                ctx.op, ctx.precision, ctx.kw = op, precision, kw
+                batched = b.dim() == 4
+                if torch.is_tensor(sigma):
+                    raw = sigma.detach().cpu().reshape(-1).tolist()
+                elif isinstance(sigma, (list, tuple)):
+                    raw = list(sigma)
+                else:
+                    raw = [sigma]
+                svals = [v if isinstance(v, complex) else float(v) for v in raw]
+                if batched and len(svals) == 1:
+                    svals = svals * b.shape[0]
+                ops = [Operator(grid, radius=radius, a=a, sigma=s) for s in svals]
+                if batched:
+                    x, infos = _solve_batch_for(precision, ops, b.detach(), kw)
+                else:
+                    x, info = _solve_for(precision, ops[0], b.detach(), kw)
+                    infos = [info]
+                _raise_failed("forward solve", infos)
+                out_dt = b.dtype if not (isinstance(svals[0], complex) and not b.is_complex()) else (
+                    torch.complex128 if b.dtype == torch.float64 else torch.complex64)
+                x = x.to(out_dt)
+                ctx.ops, ctx.precision, ctx.kw, ctx.batched = ops, precision, kw, batched
                 ctx.sigma_is_tensor = torch.is_tensor(sigma)
+                ctx.sigma_shape = sigma.shape if torch.is_tensor(sigma) else None
                 ctx.sigma_dtype = sigma.dtype if torch.is_tensor(sigma) else torch.float64
+                ctx.b_dtype = b.dtype
                 ctx.save_for_backward(x)
                 return x
 
             @staticmethod
             def backward(ctx, gx):
                 (x,) = ctx.saved_tensors
-                lam, info = _solve_for(ctx.precision, ctx.op, gx.contiguous(), ctx.kw)
-                if info["status"] != 0:
-                    raise CudaLibraryError(f"adjoint solve: {info['status_name']} ({info})")
+                aops = [conj_op(op) for op in ctx.ops]
+                if ctx.batched:
+                    lam, infos = _solve_batch_for(ctx.precision, aops, gx.contiguous(), ctx.kw)
+                else:
+                    lam, info = _solve_for(ctx.precision, aops[0], gx.contiguous(), ctx.kw)
+                    infos = [info]
+                _raise_failed("adjoint solve", infos)
                 lam = lam.to(x.dtype)
                 gsig = None
                 if ctx.sigma_is_tensor and ctx.needs_input_grad[1]:
-                    gsig = -(lam.double() * x.double()).sum().to(ctx.sigma_dtype)
-                gb = lam if ctx.needs_input_grad[0] else None
+                    hp = torch.complex128 if x.is_complex() else torch.float64
+                    prod = -(x.to(hp).conj() * lam.to(hp))
+                    g = prod.reshape(prod.shape[0], -1).sum(1) if ctx.batched else prod.sum()
+                    if not ctx.sigma_dtype.is_complex:
+                        g = g.real
+                    nsig = 1
+                    for d in ctx.sigma_shape:
+                        nsig *= d
+                    if g.numel() != nsig:  # one sigma shared by the whole batch
+                        g = g.sum()
+                    gsig = g.to(ctx.sigma_dtype).reshape(ctx.sigma_shape)
+                gb = None
+                if ctx.needs_input_grad[0]:
+                    gb = lam if ctx.b_dtype.is_complex else lam.real if lam.is_complex() else lam
+                    gb = gb.to(ctx.b_dtype)
                 return gb, gsig, None, None, None, None, None
 
         return Fn
@@ -515,12 +577,14 @@ _Fn = None
 def solve_shifted(b, sigma, *, a=A_REF, radius=6, precision="mixed", **kw):
     """Differentiable x = (a Lap_h + sigma I)^-1 b on the periodic grid of b.
 
-    b: CUDA tensor (nz, ny, nx); sigma: float or 0-dim tensor (may require
-    grad).  precision: "mixed" (FP32 AAR + FP64 residual replacement), "fp64"
-    or "fp32" AAR.  kw: solver parameters (tol, m, p, omega, beta, ...).
+    b: CUDA tensor (nz, ny, nx), or (B, nz, ny, nx) for a batch solved by one
+    batched solve; real or complex.  sigma: float / complex or a tensor (0-dim,
+    or (B,) for a batch; may require grad).  precision: "mixed" (FP32 /
+    complex64 AAR + FP64 residual replacement), "fp64" or "fp32" AAR.
+    kw: solver parameters (tol, m, p, omega, beta, ...).
     """
     global _Fn
     if _Fn is None:
         _Fn = _ShiftedSolve.build()
-    nz, ny, nx = b.shape
+    nz, ny, nx = b.shape[-3:]
     return _Fn.apply(b, sigma, (nx, ny, nz), radius, a, precision, dict(kw))
