@@ -141,6 +141,30 @@ int lsg_aar_batched(const lsg_operator *ops, int count, const lsg_params *prm, i
 int lsg_aar_mixed_batched(const lsg_operator *ops, int count, const lsg_params *prm, int dtype,
                           void *const *d_x, const void *const *d_b, lsg_result *res, void *stream);
 
+/* Autotuner of the Richardson stencil pass (no counterpart in the reference,
+ * whose operator is a fixed host loop, MPI_REAL/system.c:189-204).  Times
+ * every candidate launch shape -- xy tile variant (threads_y x
+ * rows_per_thread rows of 32 columns) and z planes per block -- for the grid
+ * of `op` and vector type `dtype` on the device, caches the fastest, and
+ * reports it.  Solves on that grid then use the cached shape.  Radius 6. */
+typedef struct lsg_tune_info {
+    int tile;             /* tile variant index */
+    int threads_y;        /* block = 32 x threads_y threads */
+    int rows_per_thread;  /* tile = 32 x (threads_y * rows_per_thread) columns */
+    int lz;               /* z planes per block */
+    double us_best;       /* measured time per launch of the chosen shape */
+    double us_default;    /* measured time of the default shape */
+    int candidates;       /* shapes timed */
+} lsg_tune_info;
+int lsg_autotune(const lsg_operator *op, int dtype, lsg_tune_info *info, void *stream);
+/* 0: default shapes; 1: use cached shapes (the default); 2: also tune every
+ * (dtype, grid) a solve meets for the first time.  LSG_AUTOTUNE=<mode> in the
+ * environment sets the initial mode. */
+int lsg_set_autotune(int mode);
+/* Text cache of tuned shapes; load adds the file's entries (count: entries read, may be NULL). */
+int lsg_autotune_save(const char *path);
+int lsg_autotune_load(const char *path, int *count);
+
 /* m x m pseudo-inverse solve with the reference's semantics
  * (x = V diag(1/w) V^T b, w < m*wmax*2.22044605e-16 dropped; MPI_REAL/tools.c:52-105),
  * computed on the device by one warp.  A row-major, device pointers. */

@@ -47,6 +47,7 @@ static size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
 // Launch plan of the active instances.
 struct BPlan {
     std::vector<int> act;     // active instances
+    int var = 0;              // tile variant of the stencil passes
     int sgrid = 0, ugrid = 0;
     long long points = 0;     // grid points of the active instances
 };
@@ -70,6 +71,9 @@ struct BatchWs {
     std::vector<char *> vec;      // per instance: xalt r0 r1 dx[m] df[m] (e)
     std::vector<double *> part;
     std::vector<long long> part_cap;
+    int tuned = 0;               // 1: tile variant and z-depth scale measured for this batch
+    int tvar = 0;
+    double tscale = 1.0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
     cudaEvent_t join = nullptr;
@@ -131,7 +135,8 @@ static int batch_ws_get(const std::vector<Geom> &geo, int m, bool mixed, bool ge
     if (ws->base) { *out = ws; return LSG_OK; }
 
     const int sms = sm_count();
-    const int ty = BatchKernels<T>::tile_y(generic);
+    int ty = BatchKernels<T>::tile_y(generic, 0);  // fewest rows over the variants: most blocks
+    for (int v = 1; v < kTileVariants && !generic; v++) ty = std::min(ty, BatchKernels<T>::tile_y(false, v));
     const int W = AccWidth<T>::value;
     const long long nvmax = (long long)(m * (m + 1)) / 2 + m;
     const long long ucap = (long long)kUcapPerSm * sms;
@@ -228,8 +233,8 @@ static const int *clk_flags(const BClock *c) { return (const int *)(c + 1); }
 // (a partial second wave would double the time of its blocks).
 template <typename T>
 static void make_plan(BatchWs *ws, const std::vector<Geom> &geo, const std::vector<int> &act, bool generic,
-                      int slots, BPlan *plan) {
-    const int ty = BatchKernels<T>::tile_y(generic);
+                      int var, int slots, double lscale, BPlan *plan) {
+    const int ty = BatchKernels<T>::tile_y(generic, var);
     const int sms = sm_count();
     BInst<T> *hi = (BInst<T> *)ws->h_inst;
     plan->act = act;
@@ -255,7 +260,9 @@ static void make_plan(BatchWs *ws, const std::vector<Geom> &geo, const std::vect
             return b;
         };
         while (L < maxnz && blocks_at(L) > slots) L++;
+        L = std::max(8, std::min(maxnz, (int)(L * lscale + 0.5)));
     }
+    plan->var = var;
     int sb0 = 0;
     for (int i : act) {
         const int lz = std::min(L, geo[i].nz);
@@ -338,13 +345,13 @@ struct BatchRun {
         cudaStream_t s = ws->stream;
         const int W = AccWidth<T>::value;
         LSG_BL(BatchKernels<T>::ir_correct(tab(), args(ws->d_umap, k, gate), plan.ugrid, s));
-        LSG_BL(BatchKernels<T>::ir_residual(tab(), args(ws->d_smap, k, gate), plan.sgrid, generic, s));
+        LSG_BL(BatchKernels<T>::ir_residual(tab(), args(ws->d_smap, k, gate), plan.sgrid, generic, plan.var, s));
         LSG_BL(batch_finalize_norm(args(nullptr, k, gate), ws->d_amap, nact(), BF_REPLACE, prm->tol, W, s));
         if (gate == 0) LSG_BL(batch_resume(args(nullptr, k, 0), ws->d_amap, nact(), rho, max_outer, s));
         return LSG_OK;
     }
     int richardson(int k) {
-        LSG_BL(BatchKernels<T>::richardson(tab(), args(ws->d_smap, k), plan.sgrid, generic, ws->stream));
+        LSG_BL(BatchKernels<T>::richardson(tab(), args(ws->d_smap, k), plan.sgrid, generic, plan.var, ws->stream));
         return LSG_OK;
     }
     // One extrapolation cycle (iterations it0+1 .. it0+p) and the clock tick.
@@ -359,7 +366,7 @@ struct BatchRun {
         LSG_BL(BatchKernels<T>::gram(tab(), args(ws->d_umap, k), plan.ugrid, s));
         LSG_BL(batch_finalize_gram(args(nullptr, k), ws->d_amap, nact(), IsCplx<T>::value, s));
         LSG_BL(BatchKernels<T>::update(tab(), args(ws->d_umap, k), plan.ugrid, s));
-        LSG_BL(BatchKernels<T>::residual_anderson(tab(), args(ws->d_smap, k), plan.sgrid, generic, s));
+        LSG_BL(BatchKernels<T>::residual_anderson(tab(), args(ws->d_smap, k), plan.sgrid, generic, plan.var, s));
         LSG_BL(batch_finalize_norm(args(nullptr, k), ws->d_amap, nact(), BF_CHECK, prm->tol, W, s));
         if (mixed) {
             int rc = refine(k, 0);
@@ -395,6 +402,65 @@ struct BatchRun {
     }
     long long per_cycle() const { return (prm->p - 1) + 5 + (mixed ? 4 : 0) + 1; }
 };
+
+// Batch autotuner: times the batched Richardson pass (every instance active)
+// for each tile variant at the one-wave z depth, half and twice it, and keeps
+// the fastest for this batch shape.  Runs before the solve state exists: the
+// control blocks are set to "running", and the FP32 plain form (x updated in
+// place) writes its iterate to the spare vector instead of the caller's x.
+template <typename T>
+static int tune_batch(BatchWs *ws, const std::vector<Geom> &geo, const std::vector<int> &act,
+                      const lsg_params *prm, bool mixed) {
+    const int count = ws->count;
+    cudaStream_t s = ws->stream;
+    BInst<T> *hi = (BInst<T> *)ws->h_inst;
+    std::vector<T *> xsave(count);
+    const bool redirect = !mixed && std::is_same<typename RealOf<T>::type, float>::value;
+    for (int i = 0; i < count; i++) {
+        xsave[i] = hi[i].x;
+        if (redirect) hi[i].x = hi[i].xalt;
+    }
+    std::vector<DevCtrl> run(2 * count, ctrl_init(prm->tol, 0));
+    LSG_BCUDA(cudaMemcpyAsync(ws->d_ctrl, run.data(), sizeof(DevCtrl) * 2 * count, cudaMemcpyHostToDevice, s));
+    LSG_BCUDA(cudaMemsetAsync(ws->d_clk, 0, ws->clk_bytes, s));
+    cudaEvent_t e0, e1;
+    LSG_BCUDA(cudaEventCreate(&e0));
+    LSG_BCUDA(cudaEventCreate(&e1));
+    BatchRun<T> B{ws, prm, mixed, false, 0.0, 0, BPlan(), 0};
+    float best = 1e30f;
+    int rc = LSG_OK;
+    static const double scales[3] = {1.0, 0.5, 2.0};
+    for (int var = 0; var < kTileVariants && rc == LSG_OK; var++) {
+        const int slots = sm_count() * BatchKernels<T>::stencil_blocks_per_sm(false, var);
+        for (double sc : scales) {
+            make_plan<T>(ws, geo, act, false, var, slots, sc, &B.plan);
+            rc = upload_tables<T>(ws, B.plan);
+            if (rc) break;
+            for (int k = 0; k < 2 && rc == LSG_OK; k++) rc = B.richardson(0);
+            if (rc) break;
+            cudaEventRecord(e0, s);
+            for (int k = 0; k < 5 && rc == LSG_OK; k++) rc = B.richardson(0);
+            cudaEventRecord(e1, s);
+            if (rc) break;
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                rc = set_error(LSG_CUDA_ERROR, "batch autotune: %s", cudaGetErrorString(cudaGetLastError()));
+                break;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+                best = ms;
+                ws->tvar = var;
+                ws->tscale = sc;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (int i = 0; i < count; i++) hi[i].x = xsave[i];
+    if (rc == LSG_OK) ws->tuned = 1;
+    return rc;
+}
 
 template <typename T>
 static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm, bool mixed, void *const *xs,
@@ -469,6 +535,12 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
     cudaStream_t s = ws->stream;
     LSG_BCUDA(cudaEventRecord(ws->join, us));
     LSG_BCUDA(cudaStreamWaitEvent(s, ws->join, 0));
+    std::vector<int> act(count);
+    for (int i = 0; i < count; i++) act[i] = i;
+    if (!generic && !ws->tuned && tune_mode() == 2) {
+        rc = tune_batch<T>(ws, geo, act, prm, mixed);
+        if (rc) return rc;
+    }
     LSG_BCUDA(cudaMemcpyAsync(ws->d_ctrl, ws->h_ctrl, sizeof(DevCtrl) * 2 * count, cudaMemcpyHostToDevice, s));
     LSG_BCUDA(cudaMemsetAsync(ws->d_clk, 0, ws->clk_bytes, s));
     for (int i = 0; i < count; i++) {
@@ -476,12 +548,12 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
         LSG_BCUDA(cudaMemsetAsync(hi[i].dx, 0, 2 * (size_t)m * vb, s));  // dx, df contiguous
         if (mixed) LSG_BCUDA(cudaMemsetAsync(hi[i].x, 0, vb, s));
     }
-    const int slots = sm_count() * BatchKernels<T>::stencil_blocks_per_sm(generic);
+    const int var = generic ? 0 : ws->tvar;
+    const double lscale = generic ? 1.0 : ws->tscale;
+    const int slots = sm_count() * BatchKernels<T>::stencil_blocks_per_sm(generic, var);
     BatchRun<T> B{ws, prm, mixed, generic, prm->inner_tol > 0 ? prm->inner_tol : 3e-2,
                   prm->max_outer > 0 ? prm->max_outer : 50, BPlan(), 0};
-    std::vector<int> act(count);
-    for (int i = 0; i < count; i++) act[i] = i;
-    make_plan<T>(ws, geo, act, generic, slots, &B.plan);
+    make_plan<T>(ws, geo, act, generic, var, slots, lscale, &B.plan);
     rc = upload_tables<T>(ws, B.plan);
     if (rc) return rc;
     const int W = AccWidth<T>::value;
@@ -502,7 +574,7 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
         if (e == cudaSuccess)
             e = batch_finalize_norm(B.args(nullptr, -1), ws->d_amap, B.nact(), BF_RHS, prm->tol, W, s);
         if (e == cudaSuccess)
-            e = BatchKernels<T>::residual_init(B.tab(), B.args(ws->d_smap, -1), B.plan.sgrid, generic, s);
+            e = BatchKernels<T>::residual_init(B.tab(), B.args(ws->d_smap, -1), B.plan.sgrid, generic, B.plan.var, s);
         if (e != cudaSuccess) return set_error(LSG_CUDA_ERROR, "batched initial residual: %s", cudaGetErrorString(e));
         B.launches += 3;
     }
@@ -551,7 +623,7 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
                     if (a2.empty()) {
                         stop = true;
                     } else {
-                        make_plan<T>(ws, geo, a2, generic, slots, &B.plan);
+                        make_plan<T>(ws, geo, a2, generic, var, slots, lscale, &B.plan);
                         rc = upload_tables<T>(ws, B.plan);
                         if (rc) return rc;
                         rc = B.capture();

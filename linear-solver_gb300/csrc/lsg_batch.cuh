@@ -38,7 +38,7 @@ template <typename T>
 struct PassRichRecur {  // AAR.c:93-107,134-139 in residual-recurrence form
     using TS = T;
     using Op = RichRecurOp<T>;
-    static constexpr int MINB = TileOf<T>::MINB;
+    static constexpr int MINB = 0;  // the tile variant's
     __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &a, Op &op) {
         const int it = batch_iter(a);
         if (it > a.max_iter) return false;
@@ -54,7 +54,7 @@ template <typename T>
 struct PassRich {  // AAR.c:93-107,134-139, x and r ping-pong
     using TS = T;
     using Op = RichOp<T, RICH_AAR>;
-    static constexpr int MINB = TileOf<T>::MINB;
+    static constexpr int MINB = 0;  // the tile variant's
     __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &a, Op &op) {
         const int it = batch_iter(a);
         if (it > a.max_iter) return false;
@@ -72,7 +72,7 @@ template <typename T>
 struct PassResInit {  // AAR.c:80-82
     using TS = T;
     using Op = ResidualOp<T, RES_INIT>;
-    static constexpr int MINB = TileOf<T>::MINB;
+    static constexpr int MINB = 0;  // the tile variant's
     __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &, Op &op) {
         op = Op{I.x, I.b, I.r0, nullptr, nullptr, I.cf, T(0.0), C.part, C.ctrl};
         return true;
@@ -84,7 +84,7 @@ template <typename T>
 struct PassResAnderson {  // AAR.c:116-123, reference form
     using TS = T;
     using Op = ResidualOp<T, RES_ANDERSON>;
-    static constexpr int MINB = TileOf<T>::MINB;
+    static constexpr int MINB = 0;  // the tile variant's
     __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &a, Op &op) {
         const int it = batch_iter(a);
         if (it > a.max_iter) return false;
@@ -100,7 +100,7 @@ template <typename T>
 struct PassResRecur {  // AAR.c:116-123, residual recurrence on the step in xalt
     using TS = T;
     using Op = ResRecurOp<T>;
-    static constexpr int MINB = TileOf<T>::MINB;
+    static constexpr int MINB = 0;  // the tile variant's
     __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &a, Op &op) {
         const int it = batch_iter(a);
         if (it > a.max_iter) return false;
@@ -148,27 +148,35 @@ __global__ void __launch_bounds__(32 * BY, MINB) batch_stencil_kernel(const BIns
                                            t / I.ty, lb);
 }
 
-// Batched stencil tile: the vector type's tile; the generic-radius path uses
-// one row per thread (NY = 1) so the widest staged plane stays in 48 KB.
-template <typename T, bool GENERIC>
+// Batched stencil tile: tile variant V of the vector type (the refinement
+// pass keeps its own launch bounds); the generic-radius path uses variant 0
+// with one row per thread (NY = 1) so the widest staged plane stays in 48 KB.
+template <typename T, int V, bool GENERIC>
 struct BTile {
-    static constexpr int BY = TileOf<T>::BY;
-    static constexpr int NY = GENERIC ? 1 : TileOf<T>::NY;
+    static constexpr int BY = GENERIC ? TileVar<T, 0>::BY : TileVar<T, V>::BY;
+    static constexpr int NY = GENERIC ? 1 : TileVar<T, V>::NY;
+    static constexpr int MINB = GENERIC ? 1 : TileVar<T, V>::MINB;
 };
 
+template <typename T, int V, class Pass>
+cudaError_t launch_batch_var(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s) {
+    using Tl = BTile<T, V, false>;
+    constexpr int MB = Pass::MINB == 0 ? Tl::MINB : Pass::MINB;
+    batch_stencil_kernel<T, 6, Tl::BY, Tl::NY, MB, false, Pass><<<grid, dim3(32, Tl::BY), 0, s>>>(tab, a);
+    return cudaGetLastError();
+}
+
 template <typename T, class Pass>
-cudaError_t launch_batch_stencil(const BInst<T> *tab, const BArgs &a, int grid, bool generic,
+cudaError_t launch_batch_stencil(const BInst<T> *tab, const BArgs &a, int grid, bool generic, int var,
                                  cudaStream_t s) {
     if (grid <= 0) return cudaSuccess;
     if (!generic) {
-        using Tl = BTile<T, false>;
-        batch_stencil_kernel<T, 6, Tl::BY, Tl::NY, Pass::MINB, false, Pass>
-            <<<grid, dim3(32, Tl::BY), 0, s>>>(tab, a);
-    } else {
-        using Tl = BTile<T, true>;
-        batch_stencil_kernel<T, LSG_MAX_RADIUS, Tl::BY, Tl::NY, 1, true, Pass>
-            <<<grid, dim3(32, Tl::BY), 0, s>>>(tab, a);
+        if (var == 1) return launch_batch_var<T, 1, Pass>(tab, a, grid, s);
+        if (var == 2) return launch_batch_var<T, 2, Pass>(tab, a, grid, s);
+        return launch_batch_var<T, 0, Pass>(tab, a, grid, s);
     }
+    using Tl = BTile<T, 0, true>;
+    batch_stencil_kernel<T, LSG_MAX_RADIUS, Tl::BY, Tl::NY, 1, true, Pass><<<grid, dim3(32, Tl::BY), 0, s>>>(tab, a);
     return cudaGetLastError();
 }
 
@@ -261,24 +269,19 @@ __global__ void __launch_bounds__(kReduceThreads) batch_ir_correct_kernel(const 
 // ---------------------------------------------------------------- launchers
 
 template <typename T>
-int BatchKernels<T>::tile_y(bool generic) {
-    return generic ? BTile<T, true>::BY * BTile<T, true>::NY : BTile<T, false>::BY * BTile<T, false>::NY;
+int BatchKernels<T>::tile_y(bool generic, int var) {
+    if (generic) return BTile<T, 0, true>::BY * BTile<T, 0, true>::NY;
+    return tile_var_rows<T>(var);
 }
 
-template <typename T>
-int BatchKernels<T>::stencil_blocks_per_sm(bool generic) {
-    int n = 0;
-    cudaError_t e;
+template <typename T, int V, bool GENERIC>
+static int batch_rich_occupancy() {
     using P = typename std::conditional<IsRecur<T>::value, PassRichRecur<T>, PassRich<T>>::type;
-    if (!generic) {
-        using Tl = BTile<T, false>;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &n, batch_stencil_kernel<T, 6, Tl::BY, Tl::NY, P::MINB, false, P>, 32 * Tl::BY, 0);
-    } else {
-        using Tl = BTile<T, true>;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &n, batch_stencil_kernel<T, LSG_MAX_RADIUS, Tl::BY, Tl::NY, 1, true, P>, 32 * Tl::BY, 0);
-    }
+    using Tl = BTile<T, V, GENERIC>;
+    int n = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &n, batch_stencil_kernel<T, GENERIC ? LSG_MAX_RADIUS : 6, Tl::BY, Tl::NY, Tl::MINB, GENERIC, P>,
+        32 * Tl::BY, 0);
     if (e != cudaSuccess || n < 1) {
         cudaGetLastError();
         n = 1;
@@ -287,29 +290,38 @@ int BatchKernels<T>::stencil_blocks_per_sm(bool generic) {
 }
 
 template <typename T>
-cudaError_t BatchKernels<T>::richardson(const BInst<T> *tab, const BArgs &a, int grid, bool generic,
-                                        cudaStream_t s) {
-    if constexpr (IsRecur<T>::value) return launch_batch_stencil<T, PassRichRecur<T>>(tab, a, grid, generic, s);
-    else return launch_batch_stencil<T, PassRich<T>>(tab, a, grid, generic, s);
+int BatchKernels<T>::stencil_blocks_per_sm(bool generic, int var) {
+    if (generic) return batch_rich_occupancy<T, 0, true>();
+    if (var == 1) return batch_rich_occupancy<T, 1, false>();
+    if (var == 2) return batch_rich_occupancy<T, 2, false>();
+    return batch_rich_occupancy<T, 0, false>();
 }
 
 template <typename T>
-cudaError_t BatchKernels<T>::residual_init(const BInst<T> *tab, const BArgs &a, int grid, bool generic,
+cudaError_t BatchKernels<T>::richardson(const BInst<T> *tab, const BArgs &a, int grid, bool generic, int var,
+                                        cudaStream_t s) {
+    if constexpr (IsRecur<T>::value) return launch_batch_stencil<T, PassRichRecur<T>>(tab, a, grid, generic, var, s);
+    else return launch_batch_stencil<T, PassRich<T>>(tab, a, grid, generic, var, s);
+}
+
+template <typename T>
+cudaError_t BatchKernels<T>::residual_init(const BInst<T> *tab, const BArgs &a, int grid, bool generic, int var,
                                            cudaStream_t s) {
-    return launch_batch_stencil<T, PassResInit<T>>(tab, a, grid, generic, s);
+    return launch_batch_stencil<T, PassResInit<T>>(tab, a, grid, generic, var, s);
 }
 
 template <typename T>
 cudaError_t BatchKernels<T>::residual_anderson(const BInst<T> *tab, const BArgs &a, int grid, bool generic,
-                                               cudaStream_t s) {
-    if constexpr (IsRecur<T>::value) return launch_batch_stencil<T, PassResRecur<T>>(tab, a, grid, generic, s);
-    else return launch_batch_stencil<T, PassResAnderson<T>>(tab, a, grid, generic, s);
+                                               int var, cudaStream_t s) {
+    if constexpr (IsRecur<T>::value) return launch_batch_stencil<T, PassResRecur<T>>(tab, a, grid, generic, var, s);
+    else return launch_batch_stencil<T, PassResAnderson<T>>(tab, a, grid, generic, var, s);
 }
 
 template <typename T>
-cudaError_t BatchKernels<T>::ir_residual(const BInst<T> *tab, const BArgs &a, int grid, bool generic,
+cudaError_t BatchKernels<T>::ir_residual(const BInst<T> *tab, const BArgs &a, int grid, bool generic, int var,
                                          cudaStream_t s) {
-    if constexpr (IsRecur<T>::value) return launch_batch_stencil<T, PassIrResidual<T>>(tab, a, grid, generic, s);
+    if constexpr (IsRecur<T>::value)
+        return launch_batch_stencil<T, PassIrResidual<T>>(tab, a, grid, generic, var, s);
     else return cudaErrorInvalidValue;
 }
 

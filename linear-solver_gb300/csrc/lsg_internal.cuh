@@ -96,6 +96,19 @@ inline typename ScalarOf<T>::type jacobi_factor(const lsg_operator *op) {
     }
 }
 
+// Autotuned Richardson launch shape (lsg_tune.cu).
+struct TuneEntry {
+    int tile;          // tile variant
+    int lz;            // z planes per block
+    double us;         // measured time per launch
+    double us_default; // the default shape's time
+};
+int tune_mode();
+bool tune_lookup(int dtype, const Geom &g, TuneEntry *e);
+struct StencilLaunch;
+template <typename T>
+StencilLaunch rich_launch(const lsg_operator *op, const StencilLaunch &L);
+
 // Host helpers of lsg_solvers.cu.
 int sm_count();
 int check_params(const lsg_params *prm, bool history);
@@ -167,6 +180,7 @@ struct StencilLaunch {
     Geom g;
     int lz;           // z planes per block
     cudaStream_t stream;
+    int tile = 0;     // tile variant (passes without partial sums only)
 };
 
 // Tile shape per vector type: FP64 is ALU-bound (narrower tile, fewer live
@@ -177,6 +191,34 @@ template <> struct TileOf<double> { static constexpr int BY = 8, NY = 2, MINB = 
 template <> struct TileOf<float> { static constexpr int BY = 4, NY = 4, MINB = 4; };
 template <> struct TileOf<cplx<double>> { static constexpr int BY = 8, NY = 1, MINB = 1; };
 template <> struct TileOf<cplx<float>> { static constexpr int BY = 8, NY = 2, MINB = 2; };
+
+// Tile variants the autotuner chooses from for the Richardson pass of single
+// solves and for every stencil pass of a batch: (BY, NY, resident blocks the
+// launch bounds ask for).  Variant 0 is TileOf<T>.
+constexpr int kTileVariants = 3;
+template <typename T, int V> struct TileVar;
+template <> struct TileVar<double, 0> { static constexpr int BY = 8, NY = 2, MINB = 1; };
+template <> struct TileVar<double, 1> { static constexpr int BY = 4, NY = 4, MINB = 1; };
+template <> struct TileVar<double, 2> { static constexpr int BY = 8, NY = 1, MINB = 2; };
+template <> struct TileVar<float, 0> { static constexpr int BY = 4, NY = 4, MINB = 4; };
+template <> struct TileVar<float, 1> { static constexpr int BY = 8, NY = 2, MINB = 2; };
+template <> struct TileVar<float, 2> { static constexpr int BY = 4, NY = 2, MINB = 4; };
+template <> struct TileVar<cplx<double>, 0> { static constexpr int BY = 8, NY = 1, MINB = 1; };
+template <> struct TileVar<cplx<double>, 1> { static constexpr int BY = 4, NY = 2, MINB = 1; };
+template <> struct TileVar<cplx<double>, 2> { static constexpr int BY = 4, NY = 1, MINB = 2; };
+template <> struct TileVar<cplx<float>, 0> { static constexpr int BY = 8, NY = 2, MINB = 2; };
+template <> struct TileVar<cplx<float>, 1> { static constexpr int BY = 4, NY = 4, MINB = 2; };
+template <> struct TileVar<cplx<float>, 2> { static constexpr int BY = 8, NY = 1, MINB = 2; };
+
+// Rows (TY) of a tile variant.
+template <typename T>
+inline int tile_var_rows(int v) {
+    switch (v) {
+    case 1: return TileVar<T, 1>::BY * TileVar<T, 1>::NY;
+    case 2: return TileVar<T, 2>::BY * TileVar<T, 2>::NY;
+    default: return TileVar<T, 0>::BY * TileVar<T, 0>::NY;
+    }
+}
 
 inline dim3 stencil_grid(const Geom &g, int ty, int lz) {
     return dim3((unsigned)((g.nx + 31) / 32), (unsigned)((g.ny + ty - 1) / ty),
@@ -199,6 +241,17 @@ inline int choose_lz(const Geom &g, int slots) {
     return lz;
 }
 
+// One-wave z depth for a tile of `ty` rows (choose_lz for any tile).
+inline int one_wave_lz(const Geom &g, int ty, int slots) {
+    const long long bxy = (long long)((g.nx + 31) / 32) * ((g.ny + ty - 1) / ty);
+    long long chunks = bxy >= slots ? 1 : slots / bxy;
+    if (chunks < 1) chunks = 1;
+    int lz = (int)((g.nz + chunks - 1) / chunks);
+    if (lz < 8) lz = 8;
+    if (lz > g.nz) lz = g.nz;
+    return lz;
+}
+
 // Blocks (and so partial sums) of one stencil launch.
 template <typename T>
 inline long long stencil_blocks(const Geom &g, int lz) {
@@ -209,8 +262,8 @@ inline long long stencil_blocks(const Geom &g, int lz) {
 template <typename T>
 struct Kernels {
     using S = typename ScalarOf<T>::type;
-    // Resident blocks per SM of the fused Richardson stencil kernel.
-    static int stencil_blocks_per_sm();
+    // Resident blocks per SM of the fused Richardson stencil kernel (tile variant var).
+    static int stencil_blocks_per_sm(int var = 0);
     // y / r update driven by one stencil pass over x.  RES_ANDERSON also
     // completes the history column hc (holding x_new - x_old) with hb * DF_col.
     static cudaError_t residual(const StencilLaunch &L, const Weights<T> &w, int mode,
@@ -357,23 +410,27 @@ struct BArgs {
 
 template <typename T>
 struct BatchKernels {
-    // Resident blocks per SM of the batched Richardson pass.
-    static int stencil_blocks_per_sm(bool generic);
-    // Tile height of the batched stencil passes.
-    static int tile_y(bool generic);
+    // Resident blocks per SM of the batched Richardson pass in tile variant var.
+    static int stencil_blocks_per_sm(bool generic, int var);
+    // Tile height of the batched stencil passes in tile variant var.
+    static int tile_y(bool generic, int var);
     // Richardson iteration k of the cycle (residual-recurrence form for FP32
     // vectors, the reference form for FP64 ones).
-    static cudaError_t richardson(const BInst<T> *tab, const BArgs &a, int grid, bool generic, cudaStream_t s);
+    static cudaError_t richardson(const BInst<T> *tab, const BArgs &a, int grid, bool generic, int var,
+                                  cudaStream_t s);
     // r0 = b - A x, ||r0||^2 partials.
-    static cudaError_t residual_init(const BInst<T> *tab, const BArgs &a, int grid, bool generic, cudaStream_t s);
+    static cudaError_t residual_init(const BInst<T> *tab, const BArgs &a, int grid, bool generic, int var,
+                                     cudaStream_t s);
     // The extrapolation iteration's residual, history column and ||r||^2.
-    static cudaError_t residual_anderson(const BInst<T> *tab, const BArgs &a, int grid, bool generic, cudaStream_t s);
+    static cudaError_t residual_anderson(const BInst<T> *tab, const BArgs &a, int grid, bool generic, int var,
+                                         cudaStream_t s);
     static cudaError_t gram(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s);
     static cudaError_t update(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s);
     // ||b||^2 partials (wide: the FP64 rhs of a mixed solve).
     static cudaError_t norm2_rhs(const BInst<T> *tab, const BArgs &a, int grid, bool wide, cudaStream_t s);
     // Mixed solves: r = float(b64 - A x64) into the current residual buffer.
-    static cudaError_t ir_residual(const BInst<T> *tab, const BArgs &a, int grid, bool generic, cudaStream_t s);
+    static cudaError_t ir_residual(const BInst<T> *tab, const BArgs &a, int grid, bool generic, int var,
+                                   cudaStream_t s);
     // Mixed solves: x64 += e; e = 0.
     static cudaError_t ir_correct(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s);
 };

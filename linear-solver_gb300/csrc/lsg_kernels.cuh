@@ -244,34 +244,52 @@ struct IrResidualOp {
 
 // ---------------------------------------------------------------- stencil dispatch
 
-template <typename T, class Op>
-cudaError_t launch_stencil(const StencilLaunch &L, const Weights<T> &w, const Op &op) {
-    constexpr int BY = TileOf<T>::BY, NY = TileOf<T>::NY, MB = TileOf<T>::MINB;
+template <typename T, int V, class Op>
+cudaError_t launch_stencil_var(const StencilLaunch &L, const Weights<T> &w, const Op &op) {
+    constexpr int BY = TileVar<T, V>::BY, NY = TileVar<T, V>::NY, MB = TileVar<T, V>::MINB;
     const dim3 grid = stencil_grid(L.g, BY * NY, L.lz);
-    const dim3 block(32, BY);
-    if (w.radius == 6)
-        stencil_kernel<T, 6, BY, NY, MB, false, Op><<<grid, block, 0, L.stream>>>(L.g, w, L.lz, op);
-    else
-        stencil_kernel<T, LSG_MAX_RADIUS, BY, NY, 1, true, Op><<<grid, block, 0, L.stream>>>(L.g, w, L.lz, op);
+    stencil_kernel<T, 6, BY, NY, MB, false, Op><<<grid, dim3(32, BY), 0, L.stream>>>(L.g, w, L.lz, op);
     return cudaGetLastError();
 }
 
-template <typename T>
-int Kernels<T>::stencil_blocks_per_sm() {
+// Passes that write partial sums keep the default tile (their block count
+// sizes the partials); the others may run any tuned variant.
+template <typename T, class Op>
+cudaError_t launch_stencil(const StencilLaunch &L, const Weights<T> &w, const Op &op) {
     constexpr int BY = TileOf<T>::BY, NY = TileOf<T>::NY;
+    if (w.radius == 6) {
+        if constexpr (Op::NACC == 0) {
+            if (L.tile == 1) return launch_stencil_var<T, 1>(L, w, op);
+            if (L.tile == 2) return launch_stencil_var<T, 2>(L, w, op);
+        }
+        return launch_stencil_var<T, 0>(L, w, op);
+    }
+    const dim3 grid = stencil_grid(L.g, BY * NY, L.lz);
+    stencil_kernel<T, LSG_MAX_RADIUS, BY, NY, 1, true, Op><<<grid, dim3(32, BY), 0, L.stream>>>(L.g, w, L.lz, op);
+    return cudaGetLastError();
+}
+
+// Resident blocks per SM of the Richardson pass in tile variant V.
+template <typename T, int V>
+static int rich_blocks_per_sm() {
+    using Tl = TileVar<T, V>;
+    using Op = typename std::conditional<std::is_same<typename RealOf<T>::type, float>::value, RichRecurOp<T>,
+                                         RichOp<T, RICH_AAR>>::type;
     int n = 0;
-    cudaError_t e;
-    if (std::is_same<T, float>::value)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &n, stencil_kernel<T, 6, BY, NY, TileOf<T>::MINB, false, RichRecurOp<T>>, 32 * BY, 0);
-    else
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &n, stencil_kernel<T, 6, BY, NY, TileOf<T>::MINB, false, RichOp<T, RICH_AAR>>, 32 * BY, 0);
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &n, stencil_kernel<T, 6, Tl::BY, Tl::NY, Tl::MINB, false, Op>, 32 * Tl::BY, 0);
     if (e != cudaSuccess || n < 1) {
         cudaGetLastError();
-        n = 2;
+        n = 1;
     }
     return n;
+}
+
+template <typename T>
+int Kernels<T>::stencil_blocks_per_sm(int var) {
+    if (var == 1) return rich_blocks_per_sm<T, 1>();
+    if (var == 2) return rich_blocks_per_sm<T, 2>();
+    return rich_blocks_per_sm<T, 0>();
 }
 
 // ---------------------------------------------------------------- point-local kernels

@@ -423,7 +423,8 @@ struct AarLoop {
     int m, p;
     Weights<T> w;
     S cf;
-    StencilLaunch L;
+    StencilLaunch L;   // residual passes
+    StencilLaunch Lr;  // Richardson passes (autotuned shape when cached)
     int sb, rb, gb;
     T *X[2];
     T *Rv[2];
@@ -442,6 +443,7 @@ struct AarLoop {
         cf = jacobi_factor<T>(op);
         const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
         L = StencilLaunch{g, lz, R.s};
+        Lr = rich_launch<T>(op, L);
         sb = (int)stencil_blocks<T>(g, lz);
         rb = reduce_blocks(n, R.sms);
         gb = Kernels<T>::gram_grid(GRAM_SYM, m, n, R.sms);
@@ -487,11 +489,11 @@ struct AarLoop {
             }
             LSG_KC(LSG_K_SMALL, finalize_norm(part, sb, ctrl, NF_CHECK, prm->tol, it, R.s, W));
         } else if (recur) {
-            LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson_recur(L, w, Rv[rc], X[0], Rv[rc ^ 1], dxc, dfc,
+            LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson_recur(Lr, w, Rv[rc], X[0], Rv[rc ^ 1], dxc, dfc,
                                                                   prm->omega * cf, cf, prm->beta, ctrl));
             rc ^= 1;
         } else {
-            LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson(L, w, RICH_AAR, X[xc], Rv[rc], b, X[xc ^ 1], Rv[rc ^ 1],
+            LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson(Lr, w, RICH_AAR, X[xc], Rv[rc], b, X[xc ^ 1], Rv[rc ^ 1],
                                                             dxc, dfc, prm->omega * cf, cf, prm->beta, ctrl));
             xc ^= 1;
             rc ^= 1;
@@ -545,6 +547,7 @@ int prich_core(Run &R, bool galerkin, const lsg_operator *op, const lsg_params *
     const double cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
     const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
     const StencilLaunch L{g, lz, R.s};
+    const StencilLaunch Lr = rich_launch<T>(op, L);
     const int rb = reduce_blocks(n, R.sms);
     T *X[2] = {x, (T *)ws->xalt};
     T *Rv[2] = {(T *)ws->r0, (T *)ws->r1};
@@ -566,7 +569,7 @@ int prich_core(Run &R, bool galerkin, const lsg_operator *op, const lsg_params *
     auto is_proj = [p](int it) { return it % p == 0; };
     auto enqueue = [&](int it) -> int {
         const int col = (it - 2 + m) % m;
-        LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson(L, w, RICH_PGR, X[cur], Rv[cur], b, X[cur ^ 1], Rv[cur ^ 1],
+        LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson(Lr, w, RICH_PGR, X[cur], Rv[cur], b, X[cur ^ 1], Rv[cur ^ 1],
                                       DX + (size_t)col * n, DF + (size_t)col * n, prm->omega * cf,
                                       cf, 0.0, ctrl));
         cur ^= 1;

@@ -57,6 +57,11 @@ class _KernelStats(C.Structure):
     _fields_ = [("launches", C.c_longlong * 8), ("ms", C.c_double * 8)]
 
 
+class _TuneInfo(C.Structure):
+    _fields_ = [("tile", C.c_int), ("threads_y", C.c_int), ("rows_per_thread", C.c_int), ("lz", C.c_int),
+                ("us_best", C.c_double), ("us_default", C.c_double), ("candidates", C.c_int)]
+
+
 class POISSON(C.Structure):
     """Leading fields of MPI_REAL/system.h:26-63 (all the library reads)."""
     _fields_ = [("FDn", C.c_int), ("ssize", C.c_int * 3), ("psize", C.c_int * 3),
@@ -86,7 +91,8 @@ EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "ls
            "lsg_version", "AAR", "PGR", "PL2R", "CG", "lsg_register_operator_callback",
            "lsg_register_precondition_callback", "lsg_set_verbose", "lsg_last_result",
            "lsg_profile", "lsg_profile_read", "lsg_set_compat_mode", "lsg_aar_mixed_c",
-           "lsg_pinv_solve_noalloc", "lsg_aar_batched", "lsg_aar_mixed_batched"]
+           "lsg_pinv_solve_noalloc", "lsg_aar_batched", "lsg_aar_mixed_batched", "lsg_autotune",
+           "lsg_set_autotune", "lsg_autotune_save", "lsg_autotune_load"]
 
 KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "unused"]
 
@@ -120,6 +126,10 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
         L.lsg_aar_mixed_c.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), vp, vp,
                                       C.POINTER(_Result), vp]
         L.lsg_pinv_solve.argtypes = [vp, vp, vp, ip, vp]
+        L.lsg_autotune.argtypes = [C.POINTER(_Operator), ip, C.POINTER(_TuneInfo), vp]
+        L.lsg_set_autotune.argtypes = [ip]
+        L.lsg_autotune_save.argtypes = [C.c_char_p]
+        L.lsg_autotune_load.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
         for f in ("lsg_aar_batched", "lsg_aar_mixed_batched"):
             getattr(L, f).argtypes = [C.POINTER(_Operator), ip, C.POINTER(_Params), ip,
                                       C.POINTER(vp), C.POINTER(vp), C.POINTER(_Result), vp]
@@ -335,6 +345,36 @@ def aar_batched(ops, bs, x0s=None, mixed=False, stream=None, **kw):
     rc = fn(arr, count, C.byref(prm), _dtype_code(bs[0]), xp, bp, res, _stream_ptr(stream))
     _check(rc, "lsg_aar_mixed_batched" if mixed else "lsg_aar_batched")
     return xs, [_result(r) for r in res]
+
+
+def autotune(op: Operator, dtype, stream=None) -> dict:
+    """Times the Richardson pass's launch shapes for op's grid and dtype; caches the fastest.
+
+    dtype: a torch dtype or one of F64 / F32 / C128 / C64."""
+    import torch
+    code = dtype if isinstance(dtype, int) else {torch.float64: F64, torch.float32: F32,
+                                                 torch.complex128: C128, torch.complex64: C64}[dtype]
+    info = _TuneInfo()
+    _check(lib().lsg_autotune(C.byref(op._s), code, C.byref(info), _stream_ptr(stream)), "lsg_autotune",
+           allow=(0,))
+    return dict(tile=info.tile, threads_y=info.threads_y, rows_per_thread=info.rows_per_thread, lz=info.lz,
+                us_best=info.us_best, us_default=info.us_default, candidates=info.candidates)
+
+
+def set_autotune(mode: int):
+    """0: default launch shapes; 1: cached tuned shapes (default); 2: tune each new grid / batch."""
+    _check(lib().lsg_set_autotune(int(mode)), "lsg_set_autotune", allow=(0,))
+
+
+def autotune_save(path: str):
+    _check(lib().lsg_autotune_save(path.encode()), "lsg_autotune_save", allow=(0,))
+
+
+def autotune_load(path: str) -> int:
+    """Adds the tuned shapes of a file written by autotune_save; returns the entries read."""
+    n = C.c_int(0)
+    _check(lib().lsg_autotune_load(path.encode(), C.byref(n)), "lsg_autotune_load", allow=(0,))
+    return n.value
 
 
 def pinv_solve(A, b, stream=None):
