@@ -128,11 +128,13 @@ def _dist():
 
 
 def _max_over_ranks(v: float, ws: int) -> float:
+    """The slowest rank's time (every rank gets it)."""
     if ws == 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -226,7 +228,9 @@ def run_lsg(args):
     def solve_fp64():
         return lsg.aar(op, b, **SOLVER_KW)
 
-    # ---- warm-up (also builds the work arrays)
+    # ---- launch-shape autotuning (Richardson pass of both precisions), then
+    # warm-up (also builds the work arrays); both outside the timed region
+    tuned = {"f32": lsg.autotune(op, torch.float32), "f64": lsg.autotune(op, torch.float64)}
     for _ in range(args.warmup):
         x, info = solve_mixed()
     torch.cuda.synchronize()
@@ -308,6 +312,8 @@ def run_lsg(args):
                          f"workload on {threads} threads, extrapolated by the iteration count",
                "seconds_per_iter": per_iter}
 
+    extra = other_workloads(dev) if (rank == 0 and not args.no_extra) else None
+
     launches = sum(i["launches"] for i in infos)
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": ws, "steps": args.steps,
@@ -315,7 +321,10 @@ def run_lsg(args):
         "vs_baseline": None, "dtype": "f32 inner / f64 refinement", "data": "synthetic",
         "config": {"workload": WORKLOAD, "n": n, "solver": "AAR mixed (lsg_aar_mixed)",
                    "l2": "no flush: each solve streams ~17 vectors of 67-134 MB (> 129 MB L2)",
-                   "parallelism": f"replicas x{ws}"},
+                   "parallelism": f"replicas x{ws}",
+                   "autotuned_richardson": {k: {kk: v[kk] for kk in ("threads_y", "rows_per_thread", "lz",
+                                                                       "us_best", "us_default")}
+                                            for k, v in tuned.items()}},
         "mixed": {"inner_iters": infos[-1]["inner_iters"], "outer_iters": infos[-1]["outer_iters"],
                   "relres": infos[-1]["relres"], "true_relres_fp64": true_res},
         "fp64": {"seconds": fp64_s, "iters": i64["iters"], "relres": i64["relres"],
@@ -335,6 +344,7 @@ def run_lsg(args):
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "other_workloads": extra,
     }
     if rank == 0:
         print(json.dumps(line))
@@ -342,6 +352,64 @@ def run_lsg(args):
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def other_workloads(dev):
+    """One timed run each of the other measured workloads (inputs resident,
+    one warm-up run first): 384^3 mixed AAR to 1e-10 on the 64-blob rhs; 48
+    batched complex shifted-Helmholtz solves (sides 32..160, complex64 inner
+    / complex128 refinement, tol 1e-8); the differentiable batch of 16 real
+    128^3 solves (mixed forward to 1e-9 + adjoint backward)."""
+    import torch
+
+    import lsg
+    import workloads
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3, out
+
+    res = {}
+    n = 384
+    op = lsg.Operator(n)
+    b = torch.from_numpy(workloads.blob_rhs(n, 3)).to(dev)
+    secs, (x, r) = timed(lambda: lsg.aar_mixed(op, b, tol=1e-10))
+    res["blobs_384_mixed_1e-10"] = {"seconds": secs, "inner_iters": r["inner_iters"],
+                                    "outer_iters": r["outer_iters"], "relres": r["relres"],
+                                    "updates_per_s": n ** 3 * r["inner_iters"] / secs}
+    del b, x
+    batch = workloads.helmholtz_batch(2024)
+    ops = [lsg.Operator(m, a=-float(m * m), sigma=s) for m, s, _ in batch]
+    bs = [torch.from_numpy(v).to(dev) for _, _, v in batch]
+    secs, (xs, rs) = timed(lambda: lsg.aar_batched(ops, bs, mixed=True, tol=1e-8))
+    pts = sum(m ** 3 * r["iters"] for (m, _, _), r in zip(batch, rs))
+    res["helmholtz_48_batched"] = {"seconds": secs, "instances": len(batch),
+                                   "converged": sum(r["status"] == 0 for r in rs),
+                                   "iters_min": min(r["iters"] for r in rs),
+                                   "iters_max": max(r["iters"] for r in rs),
+                                   "updates_per_s": pts / secs, "launches": rs[0]["launches"]}
+    del bs, xs
+    probs = workloads.differentiable_batch(5)
+    bb = torch.stack([torch.from_numpy(v[1]) for v in probs]).to(dev)
+    xstar = torch.stack([torch.from_numpy(v[2]) for v in probs]).to(dev)
+    sig = torch.tensor([v[0] for v in probs], dtype=torch.float64, device=dev)
+
+    def fwd_bwd():
+        bq = bb.clone().requires_grad_(True)
+        sq = sig.clone().requires_grad_(True)
+        x = lsg.solve_shifted(bq, sq, a=-128.0 * 128.0, precision="mixed", tol=1e-9)
+        (0.5 * ((x - xstar) ** 2).sum()).backward()
+        return sq.grad
+
+    secs, _ = timed(fwd_bwd)
+    res["differentiable_16x128_fwd_bwd"] = {"seconds": secs}
+    return res
 
 
 def run_case(case: str):
@@ -381,6 +449,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="lsg", choices=["lsg", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-extra", action="store_true", help="skip the other measured workloads")
     ap.add_argument("--case", choices=["rich32", "rich64", "mixed", "fp64"],
                     help="run one short fixed invocation for a profiler and exit")
     args = ap.parse_args()
