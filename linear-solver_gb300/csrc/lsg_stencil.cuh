@@ -2,7 +2,8 @@
 //
 // Replaces the sequential operator of MPI_REAL/system.c:189-204 (and the MPI
 // halo exchange of :106-188, which one GPU does not need): each thread block
-// owns a 32 x TY column tile of the xy plane and a range of lz planes along z.
+// owns a 32 x TY column tile of the xy plane (NY adjacent rows per thread) and a
+// range of lz planes along z.
 // For every plane it
 //   * keeps, per owned column, the 2R+1 values u(z-R .. z+R) in a register
 //     queue (one new plane value loaded per step: the z neighbours),
@@ -83,7 +84,7 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
     bool valid[NY];
 #pragma unroll
     for (int k = 0; k < NY; k++) {
-        const int yy = y0 + ty + BY * k;
+        const int yy = y0 + ty * NY + k;  // a thread owns NY adjacent rows
         col[k] = gx + wrap_index(yy, g.ny) * g.nx;
         valid[k] = (x0 + tx < g.nx) && (yy < g.ny);
     }
@@ -157,7 +158,7 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
 #pragma unroll
         for (int k = 0; k < NY; k++) {
             q[k][HEAD] = op.value(qn[k]);
-            sm[(RQ + ty + BY * k) * FX + RQ + tx] = q[k][CEN];
+            sm[(RQ + ty * NY + k) * FX + RQ + tx] = q[k][CEN];
         }
 #pragma unroll
         for (int s = 0; s < NH; s++)
@@ -178,14 +179,26 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
             zl = (zl + 1 == nz) ? 0u : zl + 1;
         }
         __syncthreads();  // plane z staged; the other buffer is no longer read
+        // y neighbours of the thread's NY adjacent rows, rows r0-RQ .. r0+NY-1+RQ:
+        // loaded from the staged plane once for all NY points (its own rows
+        // are the queue centres), so a point costs 2 RQ + 2 RQ / NY shared loads.
+        const T *col0 = sm + (RQ + ty * NY) * FX + RQ + tx;
+        T yv[NY + 2 * RQ];
+#pragma unroll
+        for (int j = 0; j < RQ; j++) {
+            yv[j] = col0[(j - RQ) * FX];
+            yv[RQ + NY + j] = col0[(NY + j) * FX];
+        }
+#pragma unroll
+        for (int k = 0; k < NY; k++) yv[RQ + k] = q[k][CEN];
 #pragma unroll
         for (int k = 0; k < NY; k++) {
-            const T *row = sm + (RQ + ty + BY * k) * FX + RQ + tx;
+            const T *row = col0 + k * FX;
             T au = w.w[0] * q[k][CEN];
 #pragma unroll
             for (int p = 1; p <= RQ; p++) {
                 if (GENERIC && p > radius) break;
-                const T sxy = (row[-p] + row[p]) + (row[-p * FX] + row[p * FX]);
+                const T sxy = (row[-p] + row[p]) + (yv[RQ + k - p] + yv[RQ + k + p]);
                 const T sz = q[k][(CEN + Q - p) % Q] + q[k][(CEN + p) % Q];
                 au = fma(w.w[p], sxy + sz, au);
             }
