@@ -359,7 +359,8 @@ def other_workloads(dev):
     one warm-up run first): 384^3 mixed AAR to 1e-10 on the 64-blob rhs; 48
     batched complex shifted-Helmholtz solves (sides 32..160, complex64 inner
     / complex128 refinement, tol 1e-8); the differentiable batch of 16 real
-    128^3 solves (mixed forward to 1e-9 + adjoint backward)."""
+    128^3 solves (mixed forward to 1e-9 + adjoint backward); GMRES(30), CG
+    and AAR on the 256^3 workload at 1e-6."""
     import torch
 
     import lsg
@@ -409,6 +410,19 @@ def other_workloads(dev):
 
     secs, _ = timed(fwd_bwd)
     res["differentiable_16x128_fwd_bwd"] = {"seconds": secs}
+    del bb, xstar
+    # the reference's KSP comparison (PETSC_REAL/main.c:84-184): GMRES(30) and CG
+    # against AAR at PETSc's tolerance 1e-6, FP64, the 256^3 workload
+    op = lsg.Operator(N_GRID)
+    b = torch.from_numpy(workloads.uniform_rhs(N_GRID, SEED)).to(dev)
+    cmp = {}
+    for name, fn in (("gmres30", lambda: lsg.gmres(op, b, restart=30, tol=1e-6, max_iter=20000)),
+                     ("cg", lambda: lsg.cg(op, b, tol=1e-6)),
+                     ("aar_fp64", lambda: lsg.aar(op, b, tol=1e-6)),
+                     ("aar_mixed", lambda: lsg.aar_mixed(op, b, tol=1e-6))):
+        secs, (x, r) = timed(fn)
+        cmp[name] = {"seconds": secs, "iters": r["iters"], "relres": r["relres"], "status": r["status_name"]}
+    res["krylov_comparison_256_1e-6"] = cmp
     return res
 
 

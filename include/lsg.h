@@ -113,6 +113,15 @@ int lsg_pl2r(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x
 int lsg_cg(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
            const void *d_b, lsg_result *res, void *stream);    /* MPI_REAL/CG.c:33 */
 
+/* Restarted GMRES(m), prm->m = restart length (the reference's comparator:
+ * PETSc KSPGMRES, PETSC_REAL/main.c:84-122; PETSc's default restart is 30).
+ * Left Jacobi preconditioning, classical Gram-Schmidt; stops when the GMRES
+ * residual estimate reaches tol * ||M^-1 b|| and the true residual of the
+ * restarted x confirms ||b - A x|| <= tol ||b||.  res->iters counts Arnoldi
+ * steps.  dtype LSG_F64 or LSG_F32; omega, beta and p are unused. */
+int lsg_gmres(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
+              const void *d_b, lsg_result *res, void *stream);
+
 /* Mixed precision: FP64 x and b (lsg_aar_mixed_c: complex128 x and b with a
  * complex64 inner iteration).  One FP32 AAR (FP32 vectors, history and
  * stencil; FP64-class reductions and m x m solve) runs on the correction;

@@ -33,5 +33,9 @@ int solve_batched(const lsg_operator *ops, int count, const lsg_params *prm, int
 int solve_mixed_batched(const lsg_operator *ops, int count, const lsg_params *prm, int dtype, void *const *xs,
                         const void *const *bs, lsg_result *res, cudaStream_t s);
 int release_batch_workspaces();
+// Restarted GMRES (lsg_krylov.cu).
+int gmres(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, const void *d_b, lsg_result *res,
+          cudaStream_t s);
+int release_gmres_workspaces();
 
 }  // namespace lsg

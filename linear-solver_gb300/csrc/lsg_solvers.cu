@@ -210,6 +210,7 @@ int release_workspaces() {
         std::lock_guard<std::mutex> gl(g_ws_mu);
         g_ws.clear();
     }
+    release_gmres_workspaces();
     return release_batch_workspaces();
 }
 

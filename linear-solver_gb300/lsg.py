@@ -92,7 +92,7 @@ EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "ls
            "lsg_register_precondition_callback", "lsg_set_verbose", "lsg_last_result",
            "lsg_profile", "lsg_profile_read", "lsg_set_compat_mode", "lsg_aar_mixed_c",
            "lsg_pinv_solve_noalloc", "lsg_aar_batched", "lsg_aar_mixed_batched", "lsg_autotune",
-           "lsg_set_autotune", "lsg_autotune_save", "lsg_autotune_load"]
+           "lsg_set_autotune", "lsg_autotune_save", "lsg_autotune_load", "lsg_gmres"]
 
 KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "unused"]
 
@@ -118,7 +118,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
         L.lsg_params_default.argtypes = [C.POINTER(_Params)]
         L.lsg_params_default.restype = None
         L.lsg_apply.argtypes = [C.POINTER(_Operator), ip, vp, vp, vp]
-        for f in ("lsg_aar", "lsg_pgr", "lsg_pl2r", "lsg_cg"):
+        for f in ("lsg_aar", "lsg_pgr", "lsg_pl2r", "lsg_cg", "lsg_gmres"):
             getattr(L, f).argtypes = [C.POINTER(_Operator), C.POINTER(_Params), ip, vp, vp,
                                       C.POINTER(_Result), vp]
         L.lsg_aar_mixed.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), vp, vp,
@@ -295,7 +295,14 @@ def cg(op, b, x0=None, **kw):
     return _solve("lsg_cg", op, b, x0, **kw)
 
 
-SOLVERS = {"aar": aar, "pgr": pgr, "pl2r": pl2r, "cg": cg}
+def gmres(op, b, x0=None, restart=30, **kw):
+    """Restarted GMRES(restart), the reference's PETSc comparator (PETSC_REAL/main.c:84-122)."""
+    kw = dict(kw)
+    kw["m"] = restart
+    return _solve("lsg_gmres", op, b, x0, **kw)
+
+
+SOLVERS = {"aar": aar, "pgr": pgr, "pl2r": pl2r, "cg": cg, "gmres": gmres}
 
 
 def aar_mixed(op, b, x0=None, stream=None, **kw):

@@ -271,3 +271,64 @@ def fft_solve(b: np.ndarray, radius=6, a=A_REF, sigma=0.0, zero_mean=True):
     if np.isrealobj(b) and np.isrealobj(np.asarray(sigma)):
         return x.real
     return x
+
+
+# ----------------------------------------------------------------------------- GMRES(m)
+
+def gmres(b: np.ndarray, x0=None, *, restart=30, tol=1e-8, max_iter=2000, radius=6, a=A_REF,
+          sigma=0.0, precond=True):
+    """Restarted GMRES(restart), left Jacobi preconditioning, classical
+    Gram-Schmidt: the steps of liblsg's lsg_gmres in numpy (test
+    infrastructure).  The reference's comparator is PETSc's KSPGMRES
+    (PETSC_REAL/main.c:84-122), which is not available here; this restates
+    Saad & Schultz's algorithm with the same stopping rules.  Returns (x, dict)."""
+    b = np.asarray(b, dtype=np.float64)
+    x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
+    c = coefficients(radius)
+    diag = a * 3.0 * c[0] + sigma
+    cf = 1.0 / diag if precond else 1.0
+    A = lambda v: apply(v, radius, a, sigma)
+    bnorm = np.linalg.norm(b)
+    tol_abs = tol * bnorm
+    m = restart
+    iters = 0
+    while True:
+        r = b - A(x)
+        nr = np.linalg.norm(r)
+        if not nr > tol_abs or iters >= max_iter:
+            return x, dict(iters=iters, relres=nr / bnorm if bnorm > 0 else nr,
+                           converged=bool(not nr > tol_abs))
+        W = [r]
+        s = [np.sign(cf) / nr if cf != 0 else 0.0]
+        g = np.zeros(m + 1)
+        g[0] = abs(cf) * nr
+        H = np.zeros((m + 1, m))
+        cs, sn = np.zeros(m), np.zeros(m)
+        k = 0
+        for j in range(m):
+            z = cf * A(s[j] * W[j])
+            h = np.array([s[i] * np.dot(W[i].ravel(), z.ravel()) for i in range(j + 1)])
+            H[:j + 1, j] = h
+            z = z - sum((h[i] * s[i]) * W[i] for i in range(j + 1))
+            eta = np.linalg.norm(z)
+            H[j + 1, j] = eta
+            W.append(z)
+            s.append(1.0 / eta if eta > 0 else 0.0)
+            for i in range(j):
+                t = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
+                H[i + 1, j] = -sn[i] * H[i, j] + cs[i] * H[i + 1, j]
+                H[i, j] = t
+            rr = np.hypot(H[j, j], eta)
+            cs[j], sn[j] = (H[j, j] / rr, eta / rr) if rr > 0 else (1.0, 0.0)
+            H[j, j] = rr
+            H[j + 1, j] = 0.0
+            g[j + 1] = -sn[j] * g[j]
+            g[j] = cs[j] * g[j]
+            k = j + 1
+            iters += 1
+            if abs(g[j + 1]) <= tol_abs * abs(cf) or iters >= max_iter or not eta > 0:
+                break
+        y = np.zeros(k)
+        for i in range(k - 1, -1, -1):
+            y[i] = (g[i] - H[i, i + 1:k] @ y[i + 1:k]) / H[i, i] if H[i, i] != 0 else 0.0
+        x = x + sum((y[i] * s[i]) * W[i] for i in range(k))
