@@ -113,6 +113,27 @@ int lsg_pl2r(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x
 int lsg_cg(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
            const void *d_b, lsg_result *res, void *stream);    /* MPI_REAL/CG.c:33 */
 
+/* General sparse operator: A x = b for a caller's matrix in CSR form on the
+ * device (square, n rows, 32-bit offsets and column indices, FP64 values).
+ * The reference's AAR accepts any operator through its Lap_Vec_mult callback
+ * (MPI_REAL/AAR.c:37, README:25); a GPU solve needs the operator as data.
+ * precond = 1: Jacobi with the matrix's diagonal (every a_ii must be
+ * non-zero), 0: none.  The row offsets and column indices are checked on the
+ * device before use (LSG_BAD_ARG on a malformed matrix). */
+typedef struct lsg_csr {
+    int n;                  /* rows = columns */
+    long long nnz;          /* stored entries, <= 2^31 - 1 */
+    const int *row_ptr;     /* n + 1 offsets, row_ptr[0] = 0, row_ptr[n] = nnz */
+    const int *col;         /* nnz column indices in 0..n-1 */
+    const double *val;      /* nnz values */
+    int precond;            /* 1: Jacobi from the diagonal; 0: none */
+} lsg_csr;
+/* AAR (MPI_REAL/AAR.c:37-177) with the CSR operator; m <= 8. */
+int lsg_aar_csr(const lsg_csr *A, const lsg_params *prm, double *d_x, const double *d_b,
+                lsg_result *res, void *stream);
+/* y = A x for the CSR operator. */
+int lsg_apply_csr(const lsg_csr *A, const double *d_x, double *d_y, void *stream);
+
 /* Restarted GMRES(m), prm->m = restart length (the reference's comparator:
  * PETSc KSPGMRES, PETSC_REAL/main.c:84-122; PETSc's default restart is 30).
  * Left Jacobi preconditioning, classical Gram-Schmidt; stops when the GMRES

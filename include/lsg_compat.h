@@ -97,6 +97,14 @@ void CG(POISSON *system, lsg_lap_fn Lap_Vec_mult, lsg_precond_fn Precondition, d
  * or is not visible to dlsym).  Up to 8 registrations; returns lsg_status. */
 int lsg_register_operator_callback(void *fn);
 /* Declare that `fn` is the Jacobi division r[i] /= diag of system.c:222-227. */
+/* Binds a user operator callback (a Lap_Vec_mult of the caller's own) to the
+ * CSR form of its matrix (host arrays, copied to the device): the drop-in AAR
+ * then solves with that matrix on the GPU, Jacobi from its diagonal when the
+ * preconditioner is the reference one or registered.  Refused for PGR, PL2R
+ * and CG.  The reference calls any operator through the callback
+ * (MPI_REAL/README:25); a GPU solve needs the operator as data. */
+int lsg_register_operator_csr(void *fn, int n, long long nnz, const int *row_ptr, const int *col,
+                              const double *val);
 int lsg_register_precondition_callback(void *fn);
 /* Precision of the drop-in AAR: 0 (default) FP64 as the reference;
  * 1 mixed: FP32 inner AAR inside FP64 residual refinement, same tol on the

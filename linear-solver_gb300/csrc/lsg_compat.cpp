@@ -8,7 +8,9 @@
 // back.  The host callbacks are identified, never called: the reference
 // operator (system.c:80-213) and Jacobi preconditioner (system.c:222-227)
 // are recognised by address (the process's Lap_Vec_mult / Precondition
-// symbols, or registered addresses); anything else is refused.  Reports are
+// symbols, or registered addresses).  A user operator runs on the GPU when its
+// callback was bound to the CSR form of its matrix (AAR only); anything else
+// is refused.  Reports are
 // printed in the reference's format (AAR.c:151-159, PGR.c:145-153,
 // PL2R.c:144-152, CG.c:157-165).
 #include <dlfcn.h>
@@ -37,6 +39,24 @@ struct Staging {
     double *x = nullptr, *b = nullptr;
     long long n = 0;
 } g_stage;
+
+// Operators bound to a CSR copy of their matrix (lsg_register_operator_csr).
+struct CsrBinding {
+    void *fn = nullptr;
+    int n = 0;
+    long long nnz = 0;
+    int *rp = nullptr, *col = nullptr;
+    double *val = nullptr;
+};
+CsrBinding g_csr_ops[8];
+int g_ncsr = 0;
+
+const CsrBinding *csr_binding(void *fn) {
+    std::lock_guard<std::mutex> g(g_mu);
+    for (int i = 0; i < g_ncsr; i++)
+        if (g_csr_ops[i].fn == fn) return &g_csr_ops[i];
+    return nullptr;
+}
 
 bool listed(void *fn, void *const *list, int count) {
     for (int i = 0; i < count; i++)
@@ -82,7 +102,8 @@ void run_compat(const char *who, int solver, POISSON *system, void *lap, void *p
                 double *x, double *rhs, double omega, double beta, int m, int p, int max_iter,
                 double tol, int Np) {
     if (!system || !x || !rhs) { fail(who, LSG_BAD_ARG, "NULL system, x or rhs"); return; }
-    if (!is_reference_operator(lap)) {
+    const CsrBinding *csr = csr_binding(lap);
+    if (!csr && !is_reference_operator(lap)) {
         fail(who, LSG_UNSUPPORTED,
              "Lap_Vec_mult is not the reference periodic FD operator; register it with "
              "lsg_register_operator_callback (no CPU fallback)");
@@ -104,15 +125,21 @@ void run_compat(const char *who, int solver, POISSON *system, void *lap, void *p
     }
     const long long n = (long long)system->psize[0] * system->psize[1] * system->psize[2];
     if (n != Np || Np <= 0) { fail(who, LSG_BAD_ARG, "Np does not match psize"); return; }
-    if (system->FDn < 1 || system->FDn > LSG_MAX_RADIUS || !system->coeff_lap) {
+    if (csr && (solver != 0 || csr->n != n)) {
+        fail(who, csr->n != n ? LSG_BAD_ARG : LSG_UNSUPPORTED,
+             csr->n != n ? "registered CSR matrix size differs from Np"
+                         : "a registered CSR operator serves AAR only");
+        return;
+    }
+    if (!csr && (system->FDn < 1 || system->FDn > LSG_MAX_RADIUS || !system->coeff_lap)) {
         fail(who, LSG_UNSUPPORTED, "FDn outside 1..8 or coeff_lap missing");
         return;
     }
     lsg_operator op;
     memset(&op, 0, sizeof(op));
     for (int d = 0; d < 3; d++) op.n[d] = system->psize[d];
-    op.radius = system->FDn;
-    for (int k = 0; k <= system->FDn; k++) op.coeff[k] = system->coeff_lap[k];
+    op.radius = csr ? 1 : system->FDn;
+    for (int k = 0; k <= op.radius && !csr; k++) op.coeff[k] = system->coeff_lap[k];
     op.a = a;
     op.sigma = 0.0;
     op.precond = pk;
@@ -148,9 +175,15 @@ void run_compat(const char *who, int solver, POISSON *system, void *lap, void *p
     lsg_result res;
     memset(&res, 0, sizeof(res));
     const double t0 = now_s();
-    int st = (solver == 0 && g_mode == 1)
-                 ? lsg::solve_mixed(&op, &prm, g_stage.x, g_stage.b, &res, nullptr)
-                 : lsg::solve(solver, &op, &prm, LSG_F64, g_stage.x, g_stage.b, &res, nullptr);
+    int st;
+    if (csr) {
+        const lsg_csr A{csr->n, csr->nnz, csr->rp, csr->col, csr->val, pk};
+        st = lsg::solve_csr(&A, &prm, g_stage.x, g_stage.b, &res, nullptr);
+    } else {
+        st = (solver == 0 && g_mode == 1) ? lsg::solve_mixed(&op, &prm, g_stage.x, g_stage.b, &res, nullptr)
+                                          : lsg::solve(solver, &op, &prm, LSG_F64, g_stage.x, g_stage.b, &res,
+                                                       nullptr);
+    }
     const double t1 = now_s();
     if (st == LSG_BAD_ARG || st == LSG_CUDA_ERROR || st == LSG_NO_MEMORY || st == LSG_UNSUPPORTED) {
         fail(who, st, lsg::last_error());
@@ -219,6 +252,44 @@ int lsg_register_operator_callback(void *fn) {
     if (listed(fn, g_ops, g_nops)) return LSG_OK;
     if (g_nops >= 8) return lsg::set_error(LSG_BAD_ARG, "too many registered operators");
     g_ops[g_nops++] = fn;
+    return LSG_OK;
+}
+
+int lsg_register_operator_csr(void *fn, int n, long long nnz, const int *row_ptr, const int *col,
+                              const double *val) {
+    if (!fn || !row_ptr || !col || !val) return lsg::set_error(LSG_BAD_ARG, "NULL callback or CSR array");
+    if (n < 1 || nnz < 1 || nnz > 2147483647LL) return lsg::set_error(LSG_BAD_ARG, "bad CSR sizes");
+    if (row_ptr[0] != 0 || (long long)row_ptr[n] != nnz)
+        return lsg::set_error(LSG_BAD_ARG, "CSR row offsets must run from 0 to nnz");
+    for (int i = 0; i < n; i++)
+        if (row_ptr[i + 1] < row_ptr[i]) return lsg::set_error(LSG_BAD_ARG, "CSR row offsets decrease");
+    for (long long k = 0; k < nnz; k++)
+        if (col[k] < 0 || col[k] >= n) return lsg::set_error(LSG_BAD_ARG, "CSR column index outside 0..n-1");
+    std::lock_guard<std::mutex> g(g_mu);
+    CsrBinding *slot = nullptr;
+    for (int i = 0; i < g_ncsr; i++)
+        if (g_csr_ops[i].fn == fn) slot = &g_csr_ops[i];
+    if (!slot) {
+        if (g_ncsr >= 8) return lsg::set_error(LSG_BAD_ARG, "too many registered CSR operators");
+        slot = &g_csr_ops[g_ncsr++];
+    }
+    if (slot->rp) cudaFree(slot->rp);
+    if (slot->col) cudaFree(slot->col);
+    if (slot->val) cudaFree(slot->val);
+    *slot = CsrBinding();
+    if (cudaMalloc(&slot->rp, sizeof(int) * (size_t)(n + 1)) != cudaSuccess ||
+        cudaMalloc(&slot->col, sizeof(int) * (size_t)nnz) != cudaSuccess ||
+        cudaMalloc(&slot->val, sizeof(double) * (size_t)nnz) != cudaSuccess) {
+        cudaGetLastError();
+        return lsg::set_error(LSG_NO_MEMORY, "device copy of the CSR matrix");
+    }
+    if (cudaMemcpy(slot->rp, row_ptr, sizeof(int) * (size_t)(n + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(slot->col, col, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(slot->val, val, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice) != cudaSuccess)
+        return lsg::set_error(LSG_CUDA_ERROR, "copy of the CSR matrix");
+    slot->fn = fn;
+    slot->n = n;
+    slot->nnz = nnz;
     return LSG_OK;
 }
 

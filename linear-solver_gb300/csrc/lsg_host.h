@@ -33,6 +33,9 @@ int solve_batched(const lsg_operator *ops, int count, const lsg_params *prm, int
 int solve_mixed_batched(const lsg_operator *ops, int count, const lsg_params *prm, int dtype, void *const *xs,
                         const void *const *bs, lsg_result *res, cudaStream_t s);
 int release_batch_workspaces();
+// General sparse operator (lsg_solvers.cu, kernels in lsg_csr.cu).
+int solve_csr(const lsg_csr *A, const lsg_params *prm, double *x, const double *b, lsg_result *res,
+              cudaStream_t s);
 // Restarted GMRES (lsg_krylov.cu).
 int gmres(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, const void *d_b, lsg_result *res,
           cudaStream_t s);

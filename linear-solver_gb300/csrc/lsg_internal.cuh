@@ -453,6 +453,28 @@ cudaError_t batch_resume(const BArgs &a, const int *amap, int nact, double rho, 
 // instance i = 1 if it finished.
 cudaError_t batch_tick(BClock *clk, const BCtl *ctl, int count, int p, bool mixed, cudaStream_t s);
 
+// ----------------------------------------------------------------------------
+// General sparse operator (lsg_csr.cu): A in CSR form on the device, FP64.
+struct CsrView {
+    int n;
+    long long nnz;
+    const int *rp;      // n + 1 row offsets
+    const int *col;     // nnz column indices
+    const double *val;  // nnz values
+    int group;          // lanes per row (4, 8, 16 or 32)
+};
+int csr_group(const CsrView &A);
+cudaError_t csr_check(const CsrView &A, int phase, int *bad, int blocks, cudaStream_t s);
+cudaError_t csr_diag(const CsrView &A, double *dinv, int precond, int *bad, int blocks, cudaStream_t s);
+cudaError_t csr_residual(const CsrView &A, int mode, const double *x, const double *b, double *r, double *df,
+                         double *hc, const double *dinv, double beta, double *partials, int blocks,
+                         const DevCtrl *ctrl, cudaStream_t s);
+cudaError_t csr_richardson(const CsrView &A, const double *x, const double *r, const double *b, double *x2,
+                           double *r2, double *dx, double *df, const double *dinv, double omega, double beta,
+                           int blocks, const DevCtrl *ctrl, cudaStream_t s);
+cudaError_t csr_scale(const double *dinv, const double *r, double *f, long long n, int blocks,
+                      const DevCtrl *ctrl, cudaStream_t s);
+
 // Number of Gram values per block for a kind and history depth.
 __host__ __device__ inline int gram_values(int kind, int m) {
     return kind == GRAM_SYM ? (m * (m + 1)) / 2 + m : m * m + m;

@@ -204,12 +204,15 @@ static int get_workspace(size_t es, long long n, int m, bool mixed, const Geom &
     return LSG_OK;
 }
 
+static void release_csr_extras();
+
 int release_workspaces() {
     cudaDeviceSynchronize();
     {
         std::lock_guard<std::mutex> gl(g_ws_mu);
         g_ws.clear();
     }
+    release_csr_extras();
     release_gmres_workspaces();
     return release_batch_workspaces();
 }
@@ -845,6 +848,184 @@ int apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, cudaStr
     return LSG_OK;
 }
 
+// ---------------------------------------------------------------- general sparse operator
+
+// Per-(device, n) extras of the CSR path: D^-1, the preconditioned residual f
+// and a flag word for the structure checks.
+struct CsrExtra {
+    double *base = nullptr;
+    double *dinv = nullptr, *f = nullptr;
+    int *flag = nullptr;
+    ~CsrExtra() {
+        if (base) cudaFree(base);
+    }
+};
+static std::mutex g_csr_mu;
+static std::map<std::pair<int, long long>, std::unique_ptr<CsrExtra>> g_csr;
+
+static void release_csr_extras() {
+    std::lock_guard<std::mutex> g(g_csr_mu);
+    g_csr.clear();
+}
+
+static int csr_view(const lsg_csr *A, CsrView *v) {
+    if (!A) return set_error(LSG_BAD_ARG, "matrix is NULL");
+    if (A->n < 1) return set_error(LSG_BAD_ARG, "matrix size n = %d < 1", A->n);
+    if (A->nnz < 1 || A->nnz > 2147483647LL)
+        return set_error(LSG_BAD_ARG, "nnz = %lld outside 1..2^31-1 (32-bit row offsets)", A->nnz);
+    if (!A->row_ptr || !A->col || !A->val) return set_error(LSG_BAD_ARG, "NULL CSR array");
+    v->n = A->n;
+    v->nnz = A->nnz;
+    v->rp = A->row_ptr;
+    v->col = A->col;
+    v->val = A->val;
+    v->group = csr_group(*v);
+    return LSG_OK;
+}
+
+// Checks the caller's row offsets, then (only if they are sound) the column
+// indices; returns LSG_BAD_ARG on a malformed matrix before any gather runs.
+static int csr_validate(const CsrView &A, CsrExtra *ex, cudaStream_t s) {
+    const int blocks = (int)std::max<long long>(1, std::min<long long>((A.nnz + 255) / 256, 4LL * sm_count()));
+    for (int phase = 0; phase < 2; phase++) {
+        int bad = 0;
+        LSG_CUDA(cudaMemsetAsync(ex->flag, 0, sizeof(int), s));
+        LSG_CUDA(csr_check(A, phase, ex->flag, blocks, s));
+        LSG_CUDA(cudaMemcpyAsync(&bad, ex->flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+        LSG_CUDA(cudaStreamSynchronize(s));
+        if (bad)
+            return set_error(LSG_BAD_ARG, phase == 0 ? "CSR row offsets are not 0 .. nnz non-decreasing"
+                                                     : "CSR column index outside 0..n-1");
+    }
+    return LSG_OK;
+}
+
+static int csr_extra(long long n, CsrExtra **out) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> g(g_csr_mu);
+    auto &slot = g_csr[std::make_pair(dev, n)];
+    if (!slot) slot.reset(new CsrExtra());
+    CsrExtra *ex = slot.get();
+    if (!ex->base) {
+        const size_t vb = align_up((size_t)n * 8);
+        cudaError_t e = cudaMalloc(&ex->base, 2 * vb + 256);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            ex->base = nullptr;
+            return set_error(LSG_NO_MEMORY, "CSR work arrays: %s", cudaGetErrorString(e));
+        }
+        ex->dinv = ex->base;
+        ex->f = (double *)((char *)ex->base + vb);
+        ex->flag = (int *)((char *)ex->base + 2 * vb);
+    }
+    *out = ex;
+    return LSG_OK;
+}
+
+// AAR.c:37-177 on a general matrix: the reference-form iteration of AarLoop
+// with CSR passes; the extrapolation step materialises f = D^-1 r and reuses
+// the Gram, m x m solve and update kernels with a unit Jacobi factor.
+int solve_csr(const lsg_csr *Ain, const lsg_params *prm, double *x, const double *b, lsg_result *res,
+              cudaStream_t s) {
+    const double t0 = now_s();
+    CsrView A;
+    int rc = csr_view(Ain, &A);
+    if (rc) return rc;
+    rc = check_params(prm, true);
+    if (rc) return rc;
+    if (prm->m > 8) return set_error(LSG_UNSUPPORTED, "CSR AAR: history depth m = %d > 8", prm->m);
+    if (!x || !b) return set_error(LSG_BAD_ARG, "NULL vector");
+    const long long n = A.n;
+    CsrExtra *ex = nullptr;
+    rc = csr_extra(n, &ex);
+    if (rc) return rc;
+    rc = csr_validate(A, ex, s);
+    if (rc) return rc;
+    const int nn[3] = {A.n, 1, 1};
+    const Geom g = make_geom(nn);
+    Workspace *ws = nullptr;
+    std::unique_lock<std::mutex> lk;
+    rc = get_workspace(sizeof(double), n, prm->m, false, g, &ws, &lk);
+    if (rc) return rc;
+    Run R(s, sm_count());
+    const int m = prm->m, p = prm->p;
+    const int cb = (int)std::max<long long>(1, std::min<long long>((n * A.group + 255) / 256, 8LL * R.sms));
+    const int rb = reduce_blocks(n, R.sms);
+    const int gb = Kernels<double>::gram_grid(GRAM_SYM, m, n, R.sms);
+    double *X[2] = {x, (double *)ws->xalt};
+    double *Rv[2] = {(double *)ws->r0, (double *)ws->r1};
+    double *DX = (double *)ws->dx, *DF = (double *)ws->df;
+    DevCtrl *ctrl = ws->ctrl;
+    double *part = ws->partials;
+    int bad = 0;
+    LSG_CUDA(cudaMemsetAsync(ex->flag, 0, sizeof(int), s));
+    LSG_KC(LSG_K_SMALL, csr_diag(A, ex->dinv, Ain->precond ? 1 : 0, ex->flag, cb, s));
+    LSG_CUDA(cudaMemcpyAsync(&bad, ex->flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LSG_CUDA(cudaStreamSynchronize(s));
+    if (bad) return set_error(LSG_BAD_ARG, "zero diagonal entry: Jacobi preconditioning undefined");
+    ws->hctrl[0] = ctrl_init(prm->tol, 0);
+    LSG_CUDA(cudaMemcpyAsync(ctrl, ws->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, s));
+    LSG_CUDA(cudaMemsetAsync(DX, 0, sizeof(double) * (size_t)n * m, s));
+    LSG_CUDA(cudaMemsetAsync(DF, 0, sizeof(double) * (size_t)n * m, s));
+    LSG_KC(LSG_K_UPDATE, Kernels<double>::norm2(b, n, part, rb, ctrl, s));
+    LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, s));
+    LSG_KC(LSG_K_RESIDUAL, csr_residual(A, RES_INIT, x, b, Rv[0], nullptr, nullptr, ex->dinv, 0.0, part, cb, ctrl, s));
+    int xc = 0, rcur = 0;
+    auto is_anderson = [p](int it) { return it % p == 0 && it > 1; };
+    auto enqueue = [&](int it) -> int {
+        const int col = (it - 1) % m;
+        double *dxc = DX + (size_t)col * n, *dfc = DF + (size_t)col * n;
+        if (is_anderson(it)) {
+            LSG_KC(LSG_K_UPDATE, csr_scale(ex->dinv, Rv[rcur], ex->f, n, rb, ctrl, s));
+            LSG_KC(LSG_K_GRAM, Kernels<double>::gram(GRAM_SYM, m, DX, DF, ex->f, n, part, gb, ctrl, s));
+            LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, gb, GRAM_SYM, m, 1.0, ctrl, s));
+            LSG_KC(LSG_K_UPDATE, Kernels<double>::aar_update(m, X[xc], ex->f, DX, dxc, prm->beta, 1.0, n, ctrl, s));
+            LSG_KC(LSG_K_RESIDUAL, csr_residual(A, RES_ANDERSON, X[xc], b, Rv[rcur], dfc, dxc, ex->dinv, prm->beta,
+                                                part, cb, ctrl, s));
+            LSG_KC(LSG_K_SMALL, finalize_norm(part, cb, ctrl, NF_CHECK, prm->tol, it, s));
+        } else {
+            LSG_KC(LSG_K_RICHARDSON, csr_richardson(A, X[xc], Rv[rcur], b, X[xc ^ 1], Rv[rcur ^ 1], dxc, dfc,
+                                                    ex->dinv, prm->omega, prm->beta, cb, ctrl, s));
+            xc ^= 1;
+            rcur ^= 1;
+        }
+        return LSG_OK;
+    };
+    rc = pipelined_loop(R, ws, 1, prm->max_iter, default_per_check(prm, n), enqueue, is_anderson);
+    if (rc != LSG_OK) return rc;
+    DevCtrl c;
+    LSG_CUDA(cudaMemcpy(&c, ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost));
+    const int last = c.done ? c.iters : prm->max_iter;
+    if (richardson_count(last, p) & 1)
+        LSG_CUDA(cudaMemcpyAsync(x, X[1], sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+    LSG_CUDA(cudaStreamSynchronize(s));
+    R.flush();
+    lsg_result tmp;
+    fill_result(&tmp, c, prm->max_iter, now_s() - t0, R.launches);
+    tmp.outer_iters = 0;
+    tmp.inner_iters = 0;
+    if (res) *res = tmp;
+    set_last_status(tmp.status);
+    return tmp.status;
+}
+
+int apply_csr(const lsg_csr *Ain, const double *x, double *y, cudaStream_t s) {
+    CsrView A;
+    int rc = csr_view(Ain, &A);
+    if (rc) return rc;
+    if (!x || !y) return set_error(LSG_BAD_ARG, "NULL vector");
+    CsrExtra *ex = nullptr;
+    rc = csr_extra(A.n, &ex);
+    if (rc) return rc;
+    rc = csr_validate(A, ex, s);
+    if (rc) return rc;
+    const int cb = (int)std::max<long long>(1, std::min<long long>(((long long)A.n * A.group + 255) / 256,
+                                                                   8LL * sm_count()));
+    LSG_CUDA(csr_residual(A, RES_APPLY, x, nullptr, y, nullptr, nullptr, nullptr, 0.0, nullptr, cb, nullptr, s));
+    return LSG_OK;
+}
+
 int pinv(const double *A, const double *b, double *x, int m, cudaStream_t s) {
     if (m < 1 || m > LSG_MAX_M) return set_error(LSG_BAD_ARG, "m = %d outside 1..%d", m, LSG_MAX_M);
     if (!A || !b || !x) return set_error(LSG_BAD_ARG, "NULL pointer");
@@ -923,6 +1104,13 @@ int lsg_aar_mixed(const lsg_operator *op, const lsg_params *prm, double *d_x, co
 int lsg_aar_mixed_c(const lsg_operator *op, const lsg_params *prm, void *d_x, const void *d_b,
                     lsg_result *res, void *stream) {
     return lsg::solve_mixed_c(op, prm, d_x, d_b, res, (cudaStream_t)stream);
+}
+int lsg_aar_csr(const lsg_csr *A, const lsg_params *prm, double *d_x, const double *d_b, lsg_result *res,
+                void *stream) {
+    return lsg::solve_csr(A, prm, d_x, d_b, res, (cudaStream_t)stream);
+}
+int lsg_apply_csr(const lsg_csr *A, const double *d_x, double *d_y, void *stream) {
+    return lsg::apply_csr(A, d_x, d_y, (cudaStream_t)stream);
 }
 int lsg_pinv_solve(const double *d_A, const double *d_b, double *d_x, int m, void *stream) {
     return lsg::pinv(d_A, d_b, d_x, m, (cudaStream_t)stream);

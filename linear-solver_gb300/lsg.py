@@ -62,6 +62,11 @@ class _TuneInfo(C.Structure):
                 ("us_best", C.c_double), ("us_default", C.c_double), ("candidates", C.c_int)]
 
 
+class _Csr(C.Structure):
+    _fields_ = [("n", C.c_int), ("nnz", C.c_longlong), ("row_ptr", C.c_void_p), ("col", C.c_void_p),
+                ("val", C.c_void_p), ("precond", C.c_int)]
+
+
 class POISSON(C.Structure):
     """Leading fields of MPI_REAL/system.h:26-63 (all the library reads)."""
     _fields_ = [("FDn", C.c_int), ("ssize", C.c_int * 3), ("psize", C.c_int * 3),
@@ -92,7 +97,8 @@ EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "ls
            "lsg_register_precondition_callback", "lsg_set_verbose", "lsg_last_result",
            "lsg_profile", "lsg_profile_read", "lsg_set_compat_mode", "lsg_aar_mixed_c",
            "lsg_pinv_solve_noalloc", "lsg_aar_batched", "lsg_aar_mixed_batched", "lsg_autotune",
-           "lsg_set_autotune", "lsg_autotune_save", "lsg_autotune_load", "lsg_gmres"]
+           "lsg_set_autotune", "lsg_autotune_save", "lsg_autotune_load", "lsg_gmres",
+           "lsg_aar_csr", "lsg_apply_csr", "lsg_register_operator_csr"]
 
 KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "unused"]
 
@@ -126,6 +132,10 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
         L.lsg_aar_mixed_c.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), vp, vp,
                                       C.POINTER(_Result), vp]
         L.lsg_pinv_solve.argtypes = [vp, vp, vp, ip, vp]
+        L.lsg_aar_csr.argtypes = [C.POINTER(_Csr), C.POINTER(_Params), vp, vp, C.POINTER(_Result), vp]
+        L.lsg_apply_csr.argtypes = [C.POINTER(_Csr), vp, vp, vp]
+        L.lsg_register_operator_csr.argtypes = [vp, ip, C.c_longlong, C.POINTER(ip), C.POINTER(ip),
+                                                C.POINTER(dp)]
         L.lsg_autotune.argtypes = [C.POINTER(_Operator), ip, C.POINTER(_TuneInfo), vp]
         L.lsg_set_autotune.argtypes = [ip]
         L.lsg_autotune_save.argtypes = [C.c_char_p]
@@ -382,6 +392,62 @@ def autotune_load(path: str) -> int:
     n = C.c_int(0)
     _check(lib().lsg_autotune_load(path.encode(), C.byref(n)), "lsg_autotune_load", allow=(0,))
     return n.value
+
+
+class CsrMatrix:
+    """A square sparse matrix on the device in CSR form (int32 offsets and
+    indices, float64 values) for lsg_aar_csr / lsg_apply_csr.  Build it from
+    a scipy.sparse matrix or from (indptr, indices, data) arrays."""
+
+    def __init__(self, indptr, indices=None, data=None, precond: bool = True):
+        import numpy as np
+        import torch
+        if indices is None:  # a scipy.sparse matrix
+            A = indptr.tocsr()
+            indptr, indices, data = A.indptr, A.indices, A.data
+        self.indptr = torch.as_tensor(np.asarray(indptr, dtype=np.int32)).cuda()
+        self.indices = torch.as_tensor(np.asarray(indices, dtype=np.int32)).cuda()
+        self.data = torch.as_tensor(np.asarray(data, dtype=np.float64)).cuda()
+        self.n = int(self.indptr.numel()) - 1
+        self.precond = bool(precond)
+        self._s = _Csr(self.n, int(self.indices.numel()), self.indptr.data_ptr(), self.indices.data_ptr(),
+                       self.data.data_ptr(), int(self.precond))
+
+
+def aar_csr(A: CsrMatrix, b, x0=None, stream=None, **kw):
+    """AAR (MPI_REAL/AAR.c:37-177) with a general sparse operator; b float64 (n,)."""
+    import torch
+    if b.dtype != torch.float64 or not b.is_cuda or b.numel() != A.n:
+        raise ValueError("b must be a float64 CUDA tensor with n values")
+    x = torch.zeros_like(b) if x0 is None else x0.clone()
+    res = _Result()
+    prm = _params(**kw)
+    rc = lib().lsg_aar_csr(C.byref(A._s), C.byref(prm), C.c_void_p(x.data_ptr()), C.c_void_p(b.data_ptr()),
+                           C.byref(res), _stream_ptr(stream))
+    _check(rc, "lsg_aar_csr")
+    return x, _result(res)
+
+
+def apply_csr(A: CsrMatrix, x, stream=None):
+    import torch
+    y = torch.empty_like(x)
+    _check(lib().lsg_apply_csr(C.byref(A._s), C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
+                               _stream_ptr(stream)), "lsg_apply_csr", allow=(0,))
+    return y
+
+
+def register_operator_csr(callback, A_scipy):
+    """Bind a ctypes operator callback (a Lap_Vec_mult of the caller's own) to
+    the CSR form of its matrix, so the drop-in AAR solves with it on the GPU."""
+    import numpy as np
+    A = A_scipy.tocsr()
+    rp = np.ascontiguousarray(A.indptr, dtype=np.int32)
+    ci = np.ascontiguousarray(A.indices, dtype=np.int32)
+    va = np.ascontiguousarray(A.data, dtype=np.float64)
+    ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
+    _check(lib().lsg_register_operator_csr(C.cast(callback, C.c_void_p), A.shape[0], int(A.nnz),
+                                           rp.ctypes.data_as(ip), ci.ctypes.data_as(ip),
+                                           va.ctypes.data_as(dp)), "lsg_register_operator_csr", allow=(0,))
 
 
 def pinv_solve(A, b, stream=None):

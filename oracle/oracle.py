@@ -332,3 +332,38 @@ def gmres(b: np.ndarray, x0=None, *, restart=30, tol=1e-8, max_iter=2000, radius
         for i in range(k - 1, -1, -1):
             y[i] = (g[i] - H[i, i + 1:k] @ y[i + 1:k]) / H[i, i] if H[i, i] != 0 else 0.0
         x = x + sum((y[i] * s[i]) * W[i] for i in range(k))
+
+
+# ----------------------------------------------------------------------------- AAR on any matrix
+
+def aar_general(matvec, dinv, b, x0=None, *, omega=0.6, beta=0.6, m=7, p=6, tol=1e-8, max_iter=100000):
+    """MPI_REAL/AAR.c:37-177 with any operator `matvec` and Jacobi factors
+    `dinv` (1 / diag(A), or ones), in numpy (test infrastructure for the
+    general sparse operator path).  The m x m solve is the reference's
+    pseudo-inverse (`pinv_solve`).  Returns (x, dict(iters, relres))."""
+    b = np.asarray(b, dtype=np.float64).ravel()
+    n = b.size
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64).ravel()
+    tol_abs = tol * np.linalg.norm(b)                 # AAR.c:78-79
+    r = b - matvec(x)                                 # AAR.c:80-82
+    DX, DF = np.zeros((m, n)), np.zeros((m, n))
+    relres = tol_abs + 1.0
+    x_old = f_old = None
+    it = 1
+    while it <= max_iter and relres > tol_abs:        # AAR.c:91
+        f = dinv * r                                  # Precondition
+        if it > 1:                                    # AAR.c:96-102
+            c = (it - 2) % m
+            DX[c], DF[c] = x - x_old, f - f_old
+        x_old, f_old = x.copy(), f.copy()
+        if it % p == 0 and it > 1:                    # AndersonExtrapolation, AAR.c:109-123
+            G = DF @ DF.T
+            s, _ = pinv_solve(G, DF @ f)
+            x = x_old + beta * f - (DX + beta * DF).T @ s
+            r = b - matvec(x)
+            relres = np.linalg.norm(r)
+        else:
+            x = x_old + omega * f                     # AAR.c:134-135
+            r = b - matvec(x)
+        it += 1
+    return x, dict(iters=it - 1, relres=relres / np.linalg.norm(b), converged=bool(relres <= tol_abs))
