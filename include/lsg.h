@@ -127,6 +127,7 @@ typedef struct lsg_csr {
     const int *col;         /* nnz column indices in 0..n-1 */
     const double *val;      /* nnz values */
     int precond;            /* 1: Jacobi from the diagonal; 0: none */
+    int lanes_per_row;      /* 0: chosen from the mean row length; else 1, 4, 8, 16 or 32 */
 } lsg_csr;
 /* AAR (MPI_REAL/AAR.c:37-177) with the CSR operator; m <= 8. */
 int lsg_aar_csr(const lsg_csr *A, const lsg_params *prm, double *d_x, const double *d_b,

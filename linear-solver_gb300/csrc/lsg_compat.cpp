@@ -177,7 +177,7 @@ void run_compat(const char *who, int solver, POISSON *system, void *lap, void *p
     const double t0 = now_s();
     int st;
     if (csr) {
-        const lsg_csr A{csr->n, csr->nnz, csr->rp, csr->col, csr->val, pk};
+        const lsg_csr A{csr->n, csr->nnz, csr->rp, csr->col, csr->val, pk, 0};
         st = lsg::solve_csr(&A, &prm, g_stage.x, g_stage.b, &res, nullptr);
     } else {
         st = (solver == 0 && g_mode == 1) ? lsg::solve_mixed(&op, &prm, g_stage.x, g_stage.b, &res, nullptr)

@@ -6,8 +6,9 @@
 // caller hands over the matrix.  Jacobi uses the matrix's own diagonal
 // (D^-1, a vector here, a scalar for the stencil).  Rows are processed by
 // groups of G lanes (G from the mean row length), each group reducing its
-// row with warp shuffles; every warp iterates over the same row blocks, so the
-// shuffles never see a lane that has left the loop.
+// row with warp shuffles (G = 1: a row per lane, so neighbouring rows'
+// gathers of structured matrices coalesce); every warp iterates over the same
+// row blocks, so the shuffles never see a lane that has left the loop.
 //
 //   csr_diag        D^-1 = 1 / a_ii (1 without preconditioning; zero diagonal flagged)
 //   csr_residual    r = b - A x (+ ||r||^2); the extrapolation-step form also
@@ -156,11 +157,14 @@ cudaError_t csr_check(const CsrView &A, int phase, int *bad, int blocks, cudaStr
 
 int csr_group(const CsrView &A) {
     const double mean = A.n > 0 ? (double)A.nnz / (double)A.n : 1.0;
-    return mean <= 6 ? 4 : mean <= 20 ? 8 : mean <= 48 ? 16 : 32;
+    // measured on 128^3 matrices (7 and 37 entries per row): a row per lane
+    // is 2x faster than any group; long rows need lanes to share the row
+    return mean <= 48 ? 1 : mean <= 128 ? 8 : 32;
 }
 
 cudaError_t csr_diag(const CsrView &A, double *dinv, int precond, int *bad, int blocks, cudaStream_t s) {
     switch (A.group) {
+    case 1: csr_diag_kernel<1><<<blocks, kReduceThreads, 0, s>>>(A.n, A.rp, A.col, A.val, dinv, precond, bad); break;
     case 4: csr_diag_kernel<4><<<blocks, kReduceThreads, 0, s>>>(A.n, A.rp, A.col, A.val, dinv, precond, bad); break;
     case 8: csr_diag_kernel<8><<<blocks, kReduceThreads, 0, s>>>(A.n, A.rp, A.col, A.val, dinv, precond, bad); break;
     case 16: csr_diag_kernel<16><<<blocks, kReduceThreads, 0, s>>>(A.n, A.rp, A.col, A.val, dinv, precond, bad); break;
@@ -174,6 +178,10 @@ static void csr_residual_mode(const CsrView &A, const double *x, const double *b
                               double *hc, const double *dinv, double beta, double *partials, int blocks,
                               const DevCtrl *ctrl, cudaStream_t s) {
     switch (A.group) {
+    case 1:
+        csr_residual_kernel<1, MODE><<<blocks, kReduceThreads, 0, s>>>(A.n, A.rp, A.col, A.val, x, b, r, df, hc,
+                                                                      dinv, beta, partials, ctrl);
+        break;
     case 4:
         csr_residual_kernel<4, MODE><<<blocks, kReduceThreads, 0, s>>>(A.n, A.rp, A.col, A.val, x, b, r, df, hc,
                                                                       dinv, beta, partials, ctrl);
@@ -206,6 +214,10 @@ cudaError_t csr_richardson(const CsrView &A, const double *x, const double *r, c
                            double *r2, double *dx, double *df, const double *dinv, double omega, double beta,
                            int blocks, const DevCtrl *ctrl, cudaStream_t s) {
     switch (A.group) {
+    case 1:
+        csr_richardson_kernel<1><<<blocks, kReduceThreads, 0, s>>>(A.n, A.rp, A.col, A.val, x, r, b, x2, r2, dx, df,
+                                                                   dinv, omega, beta, ctrl);
+        break;
     case 4:
         csr_richardson_kernel<4><<<blocks, kReduceThreads, 0, s>>>(A.n, A.rp, A.col, A.val, x, r, b, x2, r2, dx, df,
                                                                    dinv, omega, beta, ctrl);

@@ -879,7 +879,10 @@ static int csr_view(const lsg_csr *A, CsrView *v) {
     v->rp = A->row_ptr;
     v->col = A->col;
     v->val = A->val;
-    v->group = csr_group(*v);
+    const int lpr = A->lanes_per_row;
+    if (lpr != 0 && lpr != 1 && lpr != 4 && lpr != 8 && lpr != 16 && lpr != 32)
+        return set_error(LSG_BAD_ARG, "lanes_per_row %d is not 0, 1, 4, 8, 16 or 32", lpr);
+    v->group = lpr ? lpr : csr_group(*v);
     return LSG_OK;
 }
 

@@ -64,7 +64,7 @@ class _TuneInfo(C.Structure):
 
 class _Csr(C.Structure):
     _fields_ = [("n", C.c_int), ("nnz", C.c_longlong), ("row_ptr", C.c_void_p), ("col", C.c_void_p),
-                ("val", C.c_void_p), ("precond", C.c_int)]
+                ("val", C.c_void_p), ("precond", C.c_int), ("lanes_per_row", C.c_int)]
 
 
 class POISSON(C.Structure):
@@ -399,7 +399,7 @@ class CsrMatrix:
     indices, float64 values) for lsg_aar_csr / lsg_apply_csr.  Build it from
     a scipy.sparse matrix or from (indptr, indices, data) arrays."""
 
-    def __init__(self, indptr, indices=None, data=None, precond: bool = True):
+    def __init__(self, indptr, indices=None, data=None, precond: bool = True, lanes_per_row: int = 0):
         import numpy as np
         import torch
         if indices is None:  # a scipy.sparse matrix
@@ -411,7 +411,7 @@ class CsrMatrix:
         self.n = int(self.indptr.numel()) - 1
         self.precond = bool(precond)
         self._s = _Csr(self.n, int(self.indices.numel()), self.indptr.data_ptr(), self.indices.data_ptr(),
-                       self.data.data_ptr(), int(self.precond))
+                       self.data.data_ptr(), int(self.precond), int(lanes_per_row))
 
 
 def aar_csr(A: CsrMatrix, b, x0=None, stream=None, **kw):
