@@ -6,6 +6,8 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <algorithm>
 #include <string.h>
 
 #include "../../include/lsg.h"
@@ -225,23 +227,42 @@ inline dim3 stencil_grid(const Geom &g, int ty, int lz) {
                 (unsigned)((g.nz + lz - 1) / lz));
 }
 
-// z planes per block.  With `slots` = SMs x resident blocks per SM, the xy
-// tiles are split along z into as many chunks as fit in one wave (a second,
-// partial wave would double the time of its blocks); chunks shorter than 8
-// planes are avoided because each chunk re-reads 2R planes to fill its queue.
-template <typename T>
-inline int choose_lz(const Geom &g, int slots) {
-    const int ty = TileOf<T>::BY * TileOf<T>::NY;
+// z planes per block, from a wave-balanced cost model: splitting each xy
+// tile's column into c chunks gives bxy * c blocks, so a launch takes
+// ceil(bxy c / slots) waves of blocks marching ceil(nz / c) planes each plus
+// the 2R planes that refill the register queue of every chunk.  The refill
+// weighs `fill` planes' worth of time: ~1 for bandwidth-bound passes (FP32,
+// where it is reading), ~0.05 for FP64 (compute-bound: refilling is a few
+// loads against ~44 FP64 operations per plane point).  Chunks stay >= 8 planes.
+inline int balanced_lz(const Geom &g, int ty, int slots, double fill) {
     const long long bxy = (long long)((g.nx + 31) / 32) * ((g.ny + ty - 1) / ty);
-    long long chunks = bxy >= slots ? 1 : slots / bxy;
-    if (chunks < 1) chunks = 1;
-    int lz = (int)((g.nz + chunks - 1) / chunks);
-    if (lz < 8) lz = 8;
-    if (lz > g.nz) lz = g.nz;
-    return lz;
+    const int cmax = std::max(1, g.nz / 8);
+    int best_lz = g.nz;
+    double best = 1e300;
+    for (int c = 1; c <= cmax; c++) {
+        const int lz = (g.nz + c - 1) / c;
+        const int cc = (g.nz + lz - 1) / lz;  // chunks actually used at this depth
+        const long long waves = (bxy * cc + slots - 1) / slots;
+        const double cost = (double)waves * (lz + fill * 12.0);
+        if (cost < best - 1e-9) {
+            best = cost;
+            best_lz = lz;
+        }
+    }
+    return std::max(1, std::min(best_lz, g.nz));
 }
 
-// One-wave z depth for a tile of `ty` rows (choose_lz for any tile).
+// Relative cost of a queue refill per vector type (see balanced_lz).
+template <typename T> struct FillCost { static constexpr double value = 1.0; };
+template <> struct FillCost<double> { static constexpr double value = 0.05; };
+template <> struct FillCost<cplx<double>> { static constexpr double value = 0.05; };
+
+template <typename T>
+inline int choose_lz(const Geom &g, int slots) {
+    return balanced_lz(g, TileOf<T>::BY * TileOf<T>::NY, slots, FillCost<T>::value);
+}
+
+// One-wave z depth for a tile of `ty` rows: as many chunks as fit in one wave.
 inline int one_wave_lz(const Geom &g, int ty, int slots) {
     const long long bxy = (long long)((g.nx + 31) / 32) * ((g.ny + ty - 1) / ty);
     long long chunks = bxy >= slots ? 1 : slots / bxy;

@@ -4,8 +4,8 @@
 // shape -- the xy tile (32 x TY columns per block, rows per thread, launch
 // bounds) and the z-march depth (planes per block, hence z chunks and waves)
 // -- is picked per vector type and grid by timing every candidate on the
-// device: each tile variant at its one-wave depth, half and twice that, and
-// the full column.  Entries are cached per (device, vector type, grid); solves
+// device: each tile variant at its one-wave depth, half and twice that, the
+// full column and the wave-balanced depth of the cost model in choose_lz.  Entries are cached per (device, vector type, grid); solves
 // use a cached entry when one exists (mode 1, the default), may tune grids
 // they meet for the first time (mode 2), or ignore the cache (mode 0).  The
 // cache can be saved to and loaded from a text file.
@@ -118,14 +118,17 @@ static int tune_t(const lsg_operator *op, cudaStream_t s, TuneEntry *out, int *n
     if (cudaMemsetAsync(buf, 0, cb + 256, s) != cudaSuccess) rc = set_error(LSG_CUDA_ERROR, "autotune memset");
     TuneEntry best;
     best.tile = 0;
-    best.lz = one_wave_lz(g, tile_var_rows<T>(0), sms * Kernels<T>::stencil_blocks_per_sm(0));
+    const int lz_default = choose_lz<T>(g, sms * Kernels<T>::stencil_blocks_per_sm(0));
+    best.lz = lz_default;
     best.us = 1e30;
     best.us_default = 0;
     int count = 0;
     for (int var = 0; var < kTileVariants && rc == LSG_OK; var++) {
         const int slots = sms * Kernels<T>::stencil_blocks_per_sm(var);
         const int lz1 = one_wave_lz(g, tile_var_rows<T>(var), slots);
-        std::vector<int> cands{lz1, std::max(8, lz1 / 2), std::min(g.nz, 2 * lz1), g.nz};
+        std::vector<int> cands{lz1, std::max(8, lz1 / 2), std::min(g.nz, 2 * lz1), g.nz,
+                               balanced_lz(g, tile_var_rows<T>(var), slots, FillCost<T>::value)};
+        if (var == 0) cands.push_back(lz_default);
         std::sort(cands.begin(), cands.end());
         cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
         for (int lz : cands) {
@@ -136,7 +139,7 @@ static int tune_t(const lsg_operator *op, cudaStream_t s, TuneEntry *out, int *n
             if (rc != LSG_OK) break;
             count++;
             const double us = 1000.0 * ms;
-            if (var == 0 && lz == lz1) best.us_default = us;
+            if (var == 0 && lz == lz_default) best.us_default = us;
             if (us < best.us) {
                 best.us = us;
                 best.tile = var;
