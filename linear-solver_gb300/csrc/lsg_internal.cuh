@@ -183,6 +183,7 @@ struct StencilLaunch {
     int lz;           // z planes per block
     cudaStream_t stream;
     int tile = 0;     // tile variant (passes without partial sums only)
+    int paired = 0;   // 1: run the two-columns-per-lane march (planned by Kernels<T>::paired_plan)
 };
 
 // Tile shape per vector type: FP64 is ALU-bound (narrower tile, fewer live
@@ -234,8 +235,8 @@ inline dim3 stencil_grid(const Geom &g, int ty, int lz) {
 // weighs `fill` planes' worth of time: ~1 for bandwidth-bound passes (FP32,
 // where it is reading), ~0.05 for FP64 (compute-bound: refilling is a few
 // loads against ~44 FP64 operations per plane point).  Chunks stay >= 8 planes.
-inline int balanced_lz(const Geom &g, int ty, int slots, double fill) {
-    const long long bxy = (long long)((g.nx + 31) / 32) * ((g.ny + ty - 1) / ty);
+inline int balanced_lz(const Geom &g, int ty, int slots, double fill, int tw = 32) {
+    const long long bxy = (long long)((g.nx + tw - 1) / tw) * ((g.ny + ty - 1) / ty);
     const int cmax = std::max(1, g.nz / 8);
     int best_lz = g.nz;
     double best = 1e300;
@@ -285,6 +286,9 @@ struct Kernels {
     using S = typename ScalarOf<T>::type;
     // Resident blocks per SM of the fused Richardson stencil kernel (tile variant var).
     static int stencil_blocks_per_sm(int var = 0);
+    // Paired (two columns per lane) march of the FP32 recurrence passes: its z
+    // depth (*lz) and block count on grid g; 0 when T has none.
+    static long long paired_plan(const Geom &g, int *lz);
     // y / r update driven by one stencil pass over x.  RES_ANDERSON also
     // completes the history column hc (holding x_new - x_old) with hb * DF_col.
     static cudaError_t residual(const StencilLaunch &L, const Weights<T> &w, int mode,

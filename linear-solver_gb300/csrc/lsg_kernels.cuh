@@ -159,6 +159,22 @@ struct RichRecurOp {
         dx[i] = fma(hb, dfv, xn - xo);
         df[i] = dfv;
     }
+    // two adjacent points (i even): the paired march
+    static constexpr bool PAIRED = true;
+    __host__ __device__ const void *pair_ptrs_or() const {
+        return (const void *)((uintptr_t)r | (uintptr_t)x | (uintptr_t)r2 | (uintptr_t)dx | (uintptr_t)df);
+    }
+    __device__ __forceinline__ Two<T> fetch_pair(unsigned i) const { return ld_pair(r + i); }
+    __device__ __forceinline__ Two<T> center_pair(unsigned i) const { return ld_pair(x + i); }
+    __device__ __forceinline__ void store_pair(unsigned i, Two<T> rc, Two<T> ar, Two<T> xo, Acc<T> *) const {
+        const T rna = fma(-c, ar.a, rc.a), rnb = fma(-c, ar.b, rc.b);
+        const T xna = fma(c, rc.a, xo.a), xnb = fma(c, rc.b, xo.b);
+        const T dfa = (rna - rc.a) * cf, dfb = (rnb - rc.b) * cf;
+        st_pair(x + i, xna, xnb);
+        st_pair(r2 + i, rna, rnb);
+        st_pair(dx + i, fma(hb, dfa, xna - xo.a), fma(hb, dfb, xnb - xo.b));
+        st_pair(df + i, dfa, dfb);
+    }
 };
 
 // Extrapolation-step residual of the FP32 inner solver: the update kernel
@@ -189,6 +205,22 @@ struct ResRecurOp {
         hc[i] = fma(hb, dfv, step);
         r[i] = rn;
         acc[0].add_prod(rn, rn);
+    }
+    // two adjacent points (i even): the paired march
+    static constexpr bool PAIRED = true;
+    __host__ __device__ const void *pair_ptrs_or() const {
+        return (const void *)((uintptr_t)dxc | (uintptr_t)r | (uintptr_t)df | (uintptr_t)hc);
+    }
+    __device__ __forceinline__ Two<T> fetch_pair(unsigned i) const { return ld_pair(dxc + i); }
+    __device__ __forceinline__ Two<T> center_pair(unsigned i) const { return ld_pair(r + i); }
+    __device__ __forceinline__ void store_pair(unsigned i, Two<T> st, Two<T> au, Two<T> ro, Acc<T> *acc) const {
+        const T rna = ro.a - au.a, rnb = ro.b - au.b;
+        const T dfa = (rna - ro.a) * cf, dfb = (rnb - ro.b) * cf;
+        st_pair(df + i, dfa, dfb);
+        st_pair(hc + i, fma(hb, dfa, st.a), fma(hb, dfb, st.b));
+        st_pair(r + i, rna, rnb);
+        acc[0].add_prod(rna, rna);
+        acc[0].add_prod(rnb, rnb);
     }
 };
 
@@ -244,6 +276,51 @@ struct IrResidualOp {
 
 // ---------------------------------------------------------------- stencil dispatch
 
+template <class Op, class = void> struct IsPaired { static constexpr bool value = false; };
+template <class Op> struct IsPaired<Op, std::void_t<decltype(Op::PAIRED)>> { static constexpr bool value = Op::PAIRED; };
+
+// Paired (two columns per lane) FP32 march: 64 x 16 tiles of 8 warps, 2 blocks/SM.
+constexpr int kPairBY = 8, kPairNY = 2, kPairMINB = 2;
+
+template <typename T, class Op>
+inline bool paired_ok(const StencilLaunch &L, const Weights<T> &w, const Op &op) {
+    if constexpr (IsPaired<Op>::value && std::is_same<T, float>::value) {
+        return w.radius == 6 && L.tile == 0 && (L.g.nx % 2) == 0 && (((uintptr_t)op.pair_ptrs_or()) & 7u) == 0;
+    } else {
+        return false;
+    }
+}
+
+// z depth and block count of the paired march on grid g (64-wide tiles, the
+// paired kernel's residency); 0 blocks when T has no paired march.
+template <typename T>
+long long Kernels<T>::paired_plan(const Geom &g, int *lz) {
+    if constexpr (std::is_same<T, float>::value) {
+        static int slots = 0;
+        if (slots == 0) {
+            int occ = 0, dev = 0, sms = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &occ, stencil_x2_kernel<T, kPairBY, kPairNY, kPairMINB, RichRecurOp<T>>, 32 * kPairBY, 0) !=
+                    cudaSuccess ||
+                occ < 1) {
+                cudaGetLastError();
+                occ = 1;
+            }
+            slots = std::max(1, sms) * occ;
+        }
+        const int z = balanced_lz(g, kPairBY * kPairNY, slots, FillCost<T>::value, 64);
+        if (lz) *lz = z;
+        return (long long)((g.nx + 63) / 64) * ((g.ny + kPairBY * kPairNY - 1) / (kPairBY * kPairNY)) *
+               ((g.nz + z - 1) / z);
+    } else {
+        (void)g;
+        if (lz) *lz = 0;
+        return 0;
+    }
+}
+
 template <typename T, int V, class Op>
 cudaError_t launch_stencil_var(const StencilLaunch &L, const Weights<T> &w, const Op &op) {
     constexpr int BY = TileVar<T, V>::BY, NY = TileVar<T, V>::NY, MB = TileVar<T, V>::MINB;
@@ -257,6 +334,21 @@ cudaError_t launch_stencil_var(const StencilLaunch &L, const Weights<T> &w, cons
 template <typename T, class Op>
 cudaError_t launch_stencil(const StencilLaunch &L, const Weights<T> &w, const Op &op) {
     constexpr int BY = TileOf<T>::BY, NY = TileOf<T>::NY;
+    // L.paired: the caller planned this launch as the paired march (its z depth
+    // in L.lz, its block count in the caller's partial-sum bookkeeping)
+    if (L.paired) {
+        if constexpr (IsPaired<Op>::value && std::is_same<T, float>::value) {
+            if (!paired_ok<T>(L, w, op)) return cudaErrorInvalidValue;
+            const dim3 grid((unsigned)((L.g.nx + 63) / 64), (unsigned)((L.g.ny + kPairBY * kPairNY - 1) /
+                                                                      (kPairBY * kPairNY)),
+                            (unsigned)((L.g.nz + L.lz - 1) / L.lz));
+            stencil_x2_kernel<T, kPairBY, kPairNY, kPairMINB, Op>
+                <<<grid, dim3(32, kPairBY), 0, L.stream>>>(L.g, w, L.lz, op);
+            return cudaGetLastError();
+        } else {
+            return cudaErrorInvalidValue;
+        }
+    }
     if (w.radius == 6) {
         if constexpr (Op::NACC == 0) {
             if (L.tile == 1) return launch_stencil_var<T, 1>(L, w, op);

@@ -149,6 +149,7 @@ static int get_workspace(size_t es, long long n, int m, bool mixed, const Geom &
     long long cap = partials_needed(n, m, sms);
     cap = std::max(cap, stencil_blocks<double>(g, choose_lz<double>(g, stencil_slots<double>(sms))));
     cap = std::max(cap, stencil_blocks<float>(g, choose_lz<float>(g, stencil_slots<float>(sms))));
+    cap = std::max(cap, Kernels<float>::paired_plan(g, nullptr));
     if (es == sizeof(cplx<double>) || es == sizeof(cplx<float>)) {  // complex: (re, im) partials
         cap = std::max(cap, 2 * stencil_blocks<cplx<double>>(g, choose_lz<cplx<double>>(g, stencil_slots<cplx<double>>(sms))));
         cap = std::max(cap, 2 * stencil_blocks<cplx<float>>(g, choose_lz<cplx<float>>(g, stencil_slots<cplx<float>>(sms))));
@@ -427,9 +428,10 @@ struct AarLoop {
     int m, p;
     Weights<T> w;
     S cf;
-    StencilLaunch L;   // residual passes
-    StencilLaunch Lr;  // Richardson passes (autotuned shape when cached)
-    int sb, rb, gb;
+    StencilLaunch L;     // residual passes
+    StencilLaunch Lr;    // Richardson passes (autotuned shape when cached, or the paired march)
+    StencilLaunch Lres;  // extrapolation-step residual of the recurrence form
+    int sb, sbr, rb, gb; // stencil blocks of L and of Lres (partial sums)
     T *X[2];
     T *Rv[2];
     T *DX, *DF;
@@ -448,7 +450,24 @@ struct AarLoop {
         const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
         L = StencilLaunch{g, lz, R.s};
         Lr = rich_launch<T>(op, L);
+        Lres = L;
         sb = (int)stencil_blocks<T>(g, lz);
+        sbr = sb;
+        // FP32 recurrence passes: the two-columns-per-lane march when the grid
+        // and every vector allow 8-byte pairs
+        int plz = 0;
+        const long long pb = Kernels<T>::paired_plan(g, &plz);
+        const uintptr_t al = (uintptr_t)x | (uintptr_t)ws->xalt | (uintptr_t)ws->r0 | (uintptr_t)ws->r1 |
+                             (uintptr_t)ws->dx | (uintptr_t)ws->df;
+        if (recur && pb > 0 && op->radius == 6 && g.nx % 2 == 0 && (al & 7u) == 0) {
+            if (Lr.tile == 0) {
+                Lr.paired = 1;
+                Lr.lz = plz;
+            }
+            Lres.paired = 1;
+            Lres.lz = plz;
+            sbr = (int)pb;
+        }
         rb = reduce_blocks(n, R.sms);
         gb = Kernels<T>::gram_grid(GRAM_SYM, m, n, R.sms);
         X[0] = x;
@@ -485,13 +504,13 @@ struct AarLoop {
                 // the step goes to the spare vector: the residual reads it as its stencil input
                 T *step = (T *)ws->xalt;
                 LSG_KC(LSG_K_UPDATE, Kernels<T>::aar_update(m, X[0], Rv[rc], DX, step, prm->beta, cf, n, ctrl, R.s));
-                LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual_recur(L, w, step, Rv[rc], dfc, dxc, cf, prm->beta, part, ctrl));
+                LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual_recur(Lres, w, step, Rv[rc], dfc, dxc, cf, prm->beta, part, ctrl));
             } else {
                 LSG_KC(LSG_K_UPDATE, Kernels<T>::aar_update(m, X[xc], Rv[rc], DX, dxc, prm->beta, cf, n, ctrl, R.s));
                 LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_ANDERSON, X[xc], b, Rv[rc], dfc, dxc, cf,
                                                             prm->beta, part, ctrl));
             }
-            LSG_KC(LSG_K_SMALL, finalize_norm(part, sb, ctrl, NF_CHECK, prm->tol, it, R.s, W));
+            LSG_KC(LSG_K_SMALL, finalize_norm(part, recur ? sbr : sb, ctrl, NF_CHECK, prm->tol, it, R.s, W));
         } else if (recur) {
             LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson_recur(Lr, w, Rv[rc], X[0], Rv[rc ^ 1], dxc, dfc,
                                                                   prm->omega * cf, cf, prm->beta, ctrl));

@@ -231,4 +231,214 @@ __global__ void __launch_bounds__(32 * BY, MINB) stencil_kernel(Geom g, Weights<
                                           blockIdx.z, blk);
 }
 
+// ---------------------------------------------------------------- two columns per lane
+//
+// The march above with each lane owning two adjacent columns (tile 64 x TY):
+// every shared, global-load and global-store access moves a pair of values
+// (8 bytes for FP32), the x neighbours of both points come from 7 paired
+// shared loads (24 scalar ones otherwise) and the halo strips are staged in
+// pairs, so a point costs ~6.5 shared loads instead of 15 and the halo per
+// point halves.  Each point's sum is evaluated in the same order as above, so
+// results are bit-identical to the one-column march.  Needs nx even and 8-byte
+// aligned vectors (pairs never straddle the periodic wrap then); the functor
+// provides fetch_pair / center_pair / store_pair.
+template <typename T> struct Two { T a, b; };
+template <typename T> struct Vec2Of;
+template <> struct Vec2Of<float> { using type = float2; };
+template <> struct Vec2Of<double> { using type = double2; };
+
+template <typename T>
+__device__ __forceinline__ Two<T> ld_pair(const T *p) {
+    const typename Vec2Of<T>::type v = *reinterpret_cast<const typename Vec2Of<T>::type *>(p);
+    return Two<T>{v.x, v.y};
+}
+template <typename T>
+__device__ __forceinline__ void st_pair(T *p, T a, T b) {
+    typename Vec2Of<T>::type v;
+    v.x = a;
+    v.y = b;
+    *reinterpret_cast<typename Vec2Of<T>::type *>(p) = v;
+}
+
+template <typename T, int BY, int NY, class Op>
+__device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T> &w, int lz, Op &op,
+                                                 T *smem0, T *smem1, int bx, int by, int bz, long long blk) {
+    constexpr int RQ = 6;
+    constexpr int TX = 64;
+    constexpr int TY = BY * NY;
+    constexpr int FX = TX + 2 * RQ;  // even, so every pair offset is 8-byte aligned
+    constexpr int NT = 32 * BY;
+    constexpr int PR = FX / 2;       // pairs per full shared row
+    constexpr int HP = RQ * PR * 2 + TY * RQ;  // halo pairs: top, bottom, then RQ / 2 per side per row
+    constexpr int NH = (HP + NT - 1) / NT;
+    constexpr int Q = 2 * RQ + 1;
+
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * 32 + tx;
+    const int x0 = bx * TX, y0 = by * TY;
+    const int z0 = bz * lz;
+    const int z1 = min(z0 + lz, g.nz);
+
+    // The lane's columns gx, gx + 1 (gx even; partial tiles wrap to valid data).
+    const bool xin = x0 + 2 * tx < g.nx;
+    const int gx = wrap_index(x0 + 2 * tx, g.nx);
+    int col[NY];
+    bool valid[NY];
+#pragma unroll
+    for (int k = 0; k < NY; k++) {
+        const int yy = y0 + ty * NY + k;
+        col[k] = gx + wrap_index(yy, g.ny) * g.nx;
+        valid[k] = xin && (yy < g.ny);
+    }
+    int hs[NH], ho[NH];
+#pragma unroll
+    for (int s = 0; s < NH; s++) {
+        const int h = tid + s * NT;
+        hs[s] = -1;
+        ho[s] = 0;
+        if (h < HP) {
+            int fy, fx;
+            if (h < RQ * PR) {                      // top strip
+                fy = h / PR; fx = 2 * (h % PR);
+            } else if (h < 2 * RQ * PR) {           // bottom strip
+                const int hh = h - RQ * PR;
+                fy = RQ + TY + hh / PR; fx = 2 * (hh % PR);
+            } else {                                // left / right strips
+                const int hh = h - 2 * RQ * PR;
+                const int row = hh / RQ, c = hh % RQ;
+                fy = RQ + row;
+                fx = c < RQ / 2 ? 2 * c : TX + 2 * c;
+            }
+            hs[s] = fy * FX + fx;
+            ho[s] = wrap_index(x0 - RQ + fx, g.nx) + wrap_index(y0 - RQ + fy, g.ny) * g.nx;
+        }
+    }
+
+    Acc<T> acc[Op::NACC > 0 ? Op::NACC : 1];
+#pragma unroll
+    for (int a = 0; a < (Op::NACC > 0 ? Op::NACC : 1); a++) acc[a].zero();
+
+    T q[NY][2][Q];
+    unsigned zl = (unsigned)wrap_index(z0 - RQ, g.nz);
+    const unsigned nxy = (unsigned)g.nxy, nz = (unsigned)g.nz;
+#pragma unroll
+    for (int s = 0; s < 2 * RQ; s++) {
+        const unsigned base = zl * nxy;
+#pragma unroll
+        for (int k = 0; k < NY; k++) {
+            const Two<T> v = op.fetch_pair(base + col[k]);
+            q[k][0][s] = v.a;
+            q[k][1][s] = v.b;
+        }
+        zl = (zl + 1 == nz) ? 0u : zl + 1;
+    }
+    Two<T> qn[NY], hn[NH], cn[NY];
+    {
+        const unsigned lb = zl * nxy, zb = (unsigned)z0 * nxy;
+#pragma unroll
+        for (int k = 0; k < NY; k++) {
+            qn[k] = op.fetch_pair(lb + col[k]);
+            cn[k] = op.center_pair(zb + col[k]);
+        }
+#pragma unroll
+        for (int s = 0; s < NH; s++)
+            if (hs[s] >= 0) hn[s] = op.fetch_pair(zb + ho[s]);
+        zl = (zl + 1 == nz) ? 0u : zl + 1;
+    }
+
+    T *sm = smem0;
+    int z = z0;
+    auto step = [&](auto phase) -> bool {
+        constexpr int P = decltype(phase)::value;
+        constexpr int HEAD = (P + Q - 1) % Q;
+        constexpr int CEN = (P + RQ) % Q;
+        const unsigned zbase = (unsigned)z * nxy;
+#pragma unroll
+        for (int k = 0; k < NY; k++) {
+            q[k][0][HEAD] = qn[k].a;
+            q[k][1][HEAD] = qn[k].b;
+            st_pair(sm + (RQ + ty * NY + k) * FX + RQ + 2 * tx, q[k][0][CEN], q[k][1][CEN]);
+        }
+#pragma unroll
+        for (int s = 0; s < NH; s++)
+            if (hs[s] >= 0) st_pair(sm + hs[s], hn[s].a, hn[s].b);
+        Two<T> cc[NY];
+#pragma unroll
+        for (int k = 0; k < NY; k++) cc[k] = cn[k];
+        if (z + 1 < z1) {
+            const unsigned lb = zl * nxy, nb = zbase + nxy;
+#pragma unroll
+            for (int k = 0; k < NY; k++) {
+                qn[k] = op.fetch_pair(lb + col[k]);
+                cn[k] = op.center_pair(nb + col[k]);
+            }
+#pragma unroll
+            for (int s = 0; s < NH; s++)
+                if (hs[s] >= 0) hn[s] = op.fetch_pair(nb + ho[s]);
+            zl = (zl + 1 == nz) ? 0u : zl + 1;
+        }
+        __syncthreads();
+        const T *col0 = sm + (RQ + ty * NY) * FX + RQ + 2 * tx;
+        // y neighbours of both columns for rows r0-RQ .. r0+NY-1+RQ (own rows from the queue)
+        T ya[NY + 2 * RQ], yb[NY + 2 * RQ];
+#pragma unroll
+        for (int j = 0; j < RQ; j++) {
+            const Two<T> lo = ld_pair(col0 + (j - RQ) * FX), hi = ld_pair(col0 + (NY + j) * FX);
+            ya[j] = lo.a; yb[j] = lo.b;
+            ya[RQ + NY + j] = hi.a; yb[RQ + NY + j] = hi.b;
+        }
+#pragma unroll
+        for (int k = 0; k < NY; k++) {
+            ya[RQ + k] = q[k][0][CEN];
+            yb[RQ + k] = q[k][1][CEN];
+        }
+#pragma unroll
+        for (int k = 0; k < NY; k++) {
+            // x window: columns gx-RQ .. gx+1+RQ of row k as 7 pairs
+            T xv[2 * RQ + 2];
+#pragma unroll
+            for (int j = 0; j <= RQ; j++) {
+                const Two<T> v = ld_pair(col0 + k * FX - RQ + 2 * j);
+                xv[2 * j] = v.a;
+                xv[2 * j + 1] = v.b;
+            }
+            T aa = w.w[0] * q[k][0][CEN], ab = w.w[0] * q[k][1][CEN];
+#pragma unroll
+            for (int p = 1; p <= RQ; p++) {
+                const T sa = (xv[RQ - p] + xv[RQ + p]) + (ya[RQ + k - p] + ya[RQ + k + p]);
+                const T sb = (xv[RQ + 1 - p] + xv[RQ + 1 + p]) + (yb[RQ + k - p] + yb[RQ + k + p]);
+                const T za = q[k][0][(CEN + Q - p) % Q] + q[k][0][(CEN + p) % Q];
+                const T zb = q[k][1][(CEN + Q - p) % Q] + q[k][1][(CEN + p) % Q];
+                aa = fma(w.w[p], sa + za, aa);
+                ab = fma(w.w[p], sb + zb, ab);
+            }
+            if (valid[k])
+                op.store_pair(zbase + col[k], Two<T>{q[k][0][CEN], q[k][1][CEN]}, Two<T>{aa, ab}, cc[k], acc);
+        }
+        sm = (sm == smem0) ? smem1 : smem0;
+        return ++z < z1;
+    };
+    while (z < z1) {
+        if (!unrolled_steps<0, Q>(step)) break;
+    }
+
+    if (Op::NACC > 0) {
+        constexpr int NA = Op::NACC > 0 ? Op::NACC : 1;
+        constexpr int W = AccWidth<T>::value;
+        __shared__ double red[NA * W * 32];
+        block_reduce_store<NA>(acc, red, op.partials + blk * Op::NACC * W);
+    }
+}
+
+template <typename T, int BY, int NY, int MINB, class Op>
+__global__ void __launch_bounds__(32 * BY, MINB) stencil_x2_kernel(Geom g, Weights<T> w, int lz, Op op) {
+    constexpr int FX = 64 + 12;
+    constexpr int FY = BY * NY + 12;
+    __shared__ __align__(16) T smem[2][FX * FY];
+    if (op.skip()) return;
+    op.init();
+    const long long blk = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+    stencil_march_x2<T, BY, NY>(g, w, lz, op, smem[0], smem[1], blockIdx.x, blockIdx.y, blockIdx.z, blk);
+}
+
 }  // namespace lsg
