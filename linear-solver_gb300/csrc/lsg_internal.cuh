@@ -183,7 +183,8 @@ struct StencilLaunch {
     int lz;           // z planes per block
     cudaStream_t stream;
     int tile = 0;     // tile variant (passes without partial sums only)
-    int paired = 0;   // 1: run the two-columns-per-lane march (planned by Kernels<T>::paired_plan)
+    int paired = -1;  // 1: the two-columns-per-lane march (planned by Kernels<T>::paired_plan);
+                      // -1: the solver may choose it; 0: not
 };
 
 // Tile shape per vector type: FP64 is ALU-bound (narrower tile, fewer live
@@ -199,6 +200,8 @@ template <> struct TileOf<cplx<float>> { static constexpr int BY = 8, NY = 2, MI
 // solves and for every stencil pass of a batch: (BY, NY, resident blocks the
 // launch bounds ask for).  Variant 0 is TileOf<T>.
 constexpr int kTileVariants = 3;
+constexpr int kTilePaired = 3;  // tuner code of the two-columns-per-lane FP32 march
+constexpr int kPairBY = 8, kPairNY = 2, kPairMINB = 2;  // its block: 32 x 8 threads, 64 x 16 tile
 template <typename T, int V> struct TileVar;
 template <> struct TileVar<double, 0> { static constexpr int BY = 8, NY = 2, MINB = 1; };
 template <> struct TileVar<double, 1> { static constexpr int BY = 4, NY = 4, MINB = 1; };

@@ -279,8 +279,6 @@ struct IrResidualOp {
 template <class Op, class = void> struct IsPaired { static constexpr bool value = false; };
 template <class Op> struct IsPaired<Op, std::void_t<decltype(Op::PAIRED)>> { static constexpr bool value = Op::PAIRED; };
 
-// Paired (two columns per lane) FP32 march: 64 x 16 tiles of 8 warps, 2 blocks/SM.
-constexpr int kPairBY = 8, kPairNY = 2, kPairMINB = 2;
 
 template <typename T, class Op>
 inline bool paired_ok(const StencilLaunch &L, const Weights<T> &w, const Op &op) {
@@ -336,7 +334,7 @@ cudaError_t launch_stencil(const StencilLaunch &L, const Weights<T> &w, const Op
     constexpr int BY = TileOf<T>::BY, NY = TileOf<T>::NY;
     // L.paired: the caller planned this launch as the paired march (its z depth
     // in L.lz, its block count in the caller's partial-sum bookkeeping)
-    if (L.paired) {
+    if (L.paired == 1) {
         if constexpr (IsPaired<Op>::value && std::is_same<T, float>::value) {
             if (!paired_ok<T>(L, w, op)) return cudaErrorInvalidValue;
             const dim3 grid((unsigned)((L.g.nx + 63) / 64), (unsigned)((L.g.ny + kPairBY * kPairNY - 1) /

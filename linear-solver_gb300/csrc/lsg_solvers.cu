@@ -448,8 +448,9 @@ struct AarLoop {
         w = make_weights<T>(op);
         cf = jacobi_factor<T>(op);
         const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
-        L = StencilLaunch{g, lz, R.s};
-        Lr = rich_launch<T>(op, L);
+        L = StencilLaunch{g, lz, R.s};  // paired -1: untuned
+        Lr = rich_launch<T>(op, L);      // a tuned shape sets paired to 0 (classic) or 1
+        L.paired = 0;
         Lres = L;
         sb = (int)stencil_blocks<T>(g, lz);
         sbr = sb;
@@ -459,15 +460,19 @@ struct AarLoop {
         const long long pb = Kernels<T>::paired_plan(g, &plz);
         const uintptr_t al = (uintptr_t)x | (uintptr_t)ws->xalt | (uintptr_t)ws->r0 | (uintptr_t)ws->r1 |
                              (uintptr_t)ws->dx | (uintptr_t)ws->df;
-        if (recur && pb > 0 && op->radius == 6 && g.nx % 2 == 0 && (al & 7u) == 0) {
-            if (Lr.tile == 0) {
+        const bool pairable = recur && pb > 0 && op->radius == 6 && g.nx % 2 == 0 && (al & 7u) == 0;
+        if (pairable) {
+            if (Lr.paired == -1) {  // untuned: the paired march
                 Lr.paired = 1;
                 Lr.lz = plz;
             }
             Lres.paired = 1;
             Lres.lz = plz;
             sbr = (int)pb;
+        } else if (Lr.paired == 1) {  // tuned paired shape the vectors cannot take
+            Lr = L;
         }
+        if (Lr.paired == -1) Lr.paired = 0;
         rb = reduce_blocks(n, R.sms);
         gb = Kernels<T>::gram_grid(GRAM_SYM, m, n, R.sms);
         X[0] = x;
@@ -570,7 +575,9 @@ int prich_core(Run &R, bool galerkin, const lsg_operator *op, const lsg_params *
     const double cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
     const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
     const StencilLaunch L{g, lz, R.s};
-    const StencilLaunch Lr = rich_launch<T>(op, L);
+    StencilLaunch Lr = rich_launch<T>(op, L);
+    if (Lr.paired == 1) Lr = L;  // the paired march serves the AAR recurrence passes only
+    Lr.paired = 0;
     const int rb = reduce_blocks(n, R.sms);
     T *X[2] = {x, (T *)ws->xalt};
     T *Rv[2] = {(T *)ws->r0, (T *)ws->r1};
