@@ -303,10 +303,14 @@ struct Kernels {
                                   const T *x, const T *r, const T *b, T *x2, T *r2, T *dx,
                                   T *df, S c, S cf, double hb, const DevCtrl *ctrl);
     // Residual-recurrence Richardson step (FP32 inner solver): r2 = r - c A r,
-    // x += c r in place, DF = (r2 - r) cf, H = (x_new - x_old) + hb DF.
+    // x += c r in place, DF = (r2 - r) cf, H = c r + hb DF.
     static cudaError_t richardson_recur(const StencilLaunch &L, const Weights<T> &w, const T *r,
                                         T *x, T *r2, T *dx, T *df, S c, S cf, double hb,
                                         const DevCtrl *ctrl);
+    // The same step with x left out (r2, H, DF only); x is rebuilt by
+    // aar_update_lean or recur_fold.
+    static cudaError_t richardson_lean(const StencilLaunch &L, const Weights<T> &w, const T *r, T *r2,
+                                       T *dx, T *df, S c, S cf, double hb, const DevCtrl *ctrl);
     // Extrapolation-step residual by recurrence: r -= A step; DF = (r_new - r) cf;
     // H_col = step + hb DF; ||r||^2.
     static cudaError_t residual_recur(const StencilLaunch &L, const Weights<T> &w, const T *step,
@@ -322,6 +326,16 @@ struct Kernels {
     // H_j = DX_j + beta DF_j; step = x_new - x_old.
     static cudaError_t aar_update(int m, T *x, const T *r, const T *h, T *step, double beta,
                                   S cf, long long n, const DevCtrl *ctrl, cudaStream_t s);
+    // The extrapolation after lean Richardson passes: x (the cycle-start
+    // iterate) += sum_mask H_j - beta cf (r - rs) + step, step = beta cf r -
+    // sum_j H_j s_j; rs is the cycle-start residual, bit j of mask marks the
+    // cycle's Richardson columns.
+    static cudaError_t aar_update_lean(int m, T *x, const T *r, const T *rs, const T *h, T *step,
+                                       double beta, S cf, long long n, unsigned mask, const DevCtrl *ctrl,
+                                       cudaStream_t s);
+    // x += sum_mask H_j - beta cf (r - rs) (a lean solve stopped mid-cycle).
+    static cudaError_t recur_fold(int m, T *x, const T *r, const T *rs, const T *h, double beta, S cf,
+                                  long long n, unsigned mask, cudaStream_t s);
     // PGR/PL2R projection: tx = DX s, tf = DF s; x += tx; r -= tf; DX_col += tx;
     // DF_col += tf; partial ||r||^2.
     static cudaError_t proj_update(int m, int col, T *x, T *r, T *dx, T *df, long long n,

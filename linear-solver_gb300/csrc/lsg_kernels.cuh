@@ -127,7 +127,7 @@ struct RichOp {
 
 // Richardson step of the FP32 inner solver in residual-recurrence form:
 // f = cf r, r2 = r - omega A f, x += omega f (in place), DF = (r2 - r) cf,
-// history column H = (x_new - x) + beta DF.  Equal in exact arithmetic to the form above; it stages
+// history column H = omega f + beta DF.  Equal in exact arithmetic to the form above; it stages
 // one array (r) instead of two and never reads b, and its rounding is
 // relative to |r| rather than to |x|.
 template <typename T>
@@ -150,13 +150,15 @@ struct RichRecurOp {
     __device__ __forceinline__ Raw fetch(unsigned i) const { return ldg(r + i); }
     __device__ __forceinline__ T value(const Raw &v) const { return v; }
     __device__ __forceinline__ Ctr fetch_center(unsigned i) const { return x[i]; }
+    // H = DX + beta DF with DX = c r taken before it is added to x, so the
+    // residual recurrence (r, H, DF) never depends on how x is accumulated:
+    // this pass and RichLeanOp below give the same r, H and DF bit for bit.
     __device__ __forceinline__ void store(unsigned i, T rc, T ar, const Ctr &xo, Acc<T> *) const {
         const T rn = fma(-c, ar, rc);
-        const T xn = fma(c, rc, xo);
         const T dfv = (rn - rc) * cf;
-        x[i] = xn;
+        x[i] = fma(c, rc, xo);
         r2[i] = rn;
-        dx[i] = fma(hb, dfv, xn - xo);
+        dx[i] = fma(hb, dfv, c * rc);
         df[i] = dfv;
     }
     // two adjacent points (i even): the paired march
@@ -168,11 +170,57 @@ struct RichRecurOp {
     __device__ __forceinline__ Two<T> center_pair(unsigned i) const { return ld_pair(x + i); }
     __device__ __forceinline__ void store_pair(unsigned i, Two<T> rc, Two<T> ar, Two<T> xo, Acc<T> *) const {
         const T rna = fma(-c, ar.a, rc.a), rnb = fma(-c, ar.b, rc.b);
-        const T xna = fma(c, rc.a, xo.a), xnb = fma(c, rc.b, xo.b);
         const T dfa = (rna - rc.a) * cf, dfb = (rnb - rc.b) * cf;
-        st_pair(x + i, xna, xnb);
+        st_pair(x + i, fma(c, rc.a, xo.a), fma(c, rc.b, xo.b));
         st_pair(r2 + i, rna, rnb);
-        st_pair(dx + i, fma(hb, dfa, xna - xo.a), fma(hb, dfb, xnb - xo.b));
+        st_pair(dx + i, fma(hb, dfa, c * rc.a), fma(hb, dfb, c * rc.b));
+        st_pair(df + i, dfa, dfb);
+    }
+};
+
+// The same Richardson step with x left out (reads r, writes r', H, DF: four
+// vectors instead of six).  Within an extrapolation cycle the steps sum to
+//   sum_j DX_j = sum_j H_j - beta (f - f_start),   f = cf r,
+// since the cycle's DF columns telescope; the lean update rebuilds x from the
+// cycle-start x and residual and the cycle's H columns (aar_update_block).
+template <typename T>
+struct RichLeanOp {
+    static constexpr int NACC = 0;
+    using Raw = T;
+    using Ctr = NoCtr;
+    const T *r;
+    T *r2;
+    T *dx;
+    T *df;
+    T c;    // omega * cf
+    T cf;
+    T hb;   // beta
+    double *partials;
+    const DevCtrl *ctrl;
+    __device__ bool skip() const { return solve_done(ctrl); }
+    __device__ void init() {}
+    __device__ __forceinline__ Raw fetch(unsigned i) const { return ldg(r + i); }
+    __device__ __forceinline__ T value(const Raw &v) const { return v; }
+    __device__ __forceinline__ Ctr fetch_center(unsigned) const { return NoCtr{}; }
+    __device__ __forceinline__ void store(unsigned i, T rc, T ar, const Ctr &, Acc<T> *) const {
+        const T rn = fma(-c, ar, rc);
+        const T dfv = (rn - rc) * cf;
+        r2[i] = rn;
+        dx[i] = fma(hb, dfv, c * rc);
+        df[i] = dfv;
+    }
+    static constexpr bool PAIRED = true;
+    static constexpr bool PACKED = true;
+    __host__ __device__ const void *pair_ptrs_or() const {
+        return (const void *)((uintptr_t)r | (uintptr_t)r2 | (uintptr_t)dx | (uintptr_t)df);
+    }
+    __device__ __forceinline__ Two<T> fetch_pair(unsigned i) const { return ld_pair(r + i); }
+    __device__ __forceinline__ Two<T> center_pair(unsigned) const { return Two<T>{T(0), T(0)}; }
+    __device__ __forceinline__ void store_pair(unsigned i, Two<T> rc, Two<T> ar, Two<T>, Acc<T> *) const {
+        const T rna = fma(-c, ar.a, rc.a), rnb = fma(-c, ar.b, rc.b);
+        const T dfa = (rna - rc.a) * cf, dfb = (rnb - rc.b) * cf;
+        st_pair(r2 + i, rna, rnb);
+        st_pair(dx + i, fma(hb, dfa, c * rc.a), fma(hb, dfb, c * rc.b));
         st_pair(df + i, dfa, dfb);
     }
 };
@@ -300,7 +348,7 @@ long long Kernels<T>::paired_plan(const Geom &g, int *lz) {
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                    &occ, stencil_x2_kernel<T, kPairBY, kPairNY, kPairMINB, RichRecurOp<T>>, 32 * kPairBY, 0) !=
+                    &occ, stencil_x2_kernel<T, kPairBY, kPairNY, kPairMINB, RichLeanOp<T>>, 32 * kPairBY, 0) !=
                     cudaSuccess ||
                 occ < 1) {
                 cudaGetLastError();
@@ -363,7 +411,7 @@ cudaError_t launch_stencil(const StencilLaunch &L, const Weights<T> &w, const Op
 template <typename T, int V>
 static int rich_blocks_per_sm() {
     using Tl = TileVar<T, V>;
-    using Op = typename std::conditional<std::is_same<typename RealOf<T>::type, float>::value, RichRecurOp<T>,
+    using Op = typename std::conditional<std::is_same<typename RealOf<T>::type, float>::value, RichLeanOp<T>,
                                          RichOp<T, RICH_AAR>>::type;
     int n = 0;
     const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -518,11 +566,34 @@ __global__ void __launch_bounds__(kReduceThreads) gram_generic_kernel(int kind, 
 // M: history depth known at compile time (all m loads in flight at once),
 // VN points per thread and step through 16-byte vectors; M = 0 is the
 // generic path (runtime m, scalar).
-template <typename T, int M, bool VEC>
+//   FP64 / complex128 (the reference form): x_new = (x + beta cf r) - am,
+//   step = x_new - x, am = sum_j H_j s_j.
+//   FP32 residual recurrence: step = beta cf r - am first, x_new = x + step,
+//   so the step (the next residual's stencil input) does not depend on x.
+//   LEAN (FP32 with x left out of the Richardson passes): x holds the
+//   cycle-start iterate, rs the cycle-start residual, and bit j of `mask`
+//   marks the H columns the cycle's Richardson passes wrote;
+//   x_new = x + (sum_mask H_j - beta cf (r - rs)) + step.
+template <typename T, bool LEAN>
+__device__ __forceinline__ void update_point(T xo, T ro, T rso, T am, T ac, T beta, T cf, T &xn, T &st) {
+    if constexpr (!std::is_same<typename RealOf<T>::type, float>::value) {
+        xn = fma(beta, ro * cf, xo) - am;
+        st = xn - xo;
+    } else if constexpr (!LEAN) {
+        st = beta * (ro * cf) - am;
+        xn = xo + st;
+    } else {
+        st = beta * (ro * cf) - am;
+        xn = xo + ((ac - beta * ((ro - rso) * cf)) + st);
+    }
+}
+
+template <typename T, int M, bool VEC, bool LEAN = false>
 __device__ __forceinline__ void aar_update_block(int m, T *__restrict__ x, const T *__restrict__ r,
                                                  const T *__restrict__ h, T *__restrict__ step,
                                                  T beta, T cf, long long n, const DevCtrl *ctrl,
-                                                 long long blk, long long nblk) {
+                                                 long long blk, long long nblk,
+                                                 const T *__restrict__ rs = nullptr, unsigned mask = 0u) {
     __shared__ T s[LSG_MAX_M];
     if (threadIdx.x < m) s[threadIdx.x] = ctrl_s<T>(ctrl, threadIdx.x);
     __syncthreads();
@@ -535,47 +606,59 @@ __device__ __forceinline__ void aar_update_block(int m, T *__restrict__ x, const
         const V *hv = reinterpret_cast<const V *>(h);
         V *xv = reinterpret_cast<V *>(x);
         const V *rv = reinterpret_cast<const V *>(r);
+        const V *rsv = reinterpret_cast<const V *>(rs);
         V *sv = reinterpret_cast<V *>(step);
-        T sj[M];
+        T sj[M], ij[M];
 #pragma unroll
-        for (int j = 0; j < M; j++) sj[j] = s[j];
+        for (int j = 0; j < M; j++) {
+            sj[j] = s[j];
+            ij[j] = ((mask >> j) & 1u) ? T(1) : T(0);
+        }
         for (long long i = t0; i < nv; i += stride) {
             V hj[M];
 #pragma unroll
             for (int j = 0; j < M; j++) hj[j] = ldv(hv + j * nv + i);
             const V xo = xv[i], ro = rv[i];
+            V rso = ro;
+            if constexpr (LEAN) rso = rsv[i];
             const T *xs = (const T *)&xo;
-            const T *rs = (const T *)&ro;
+            const T *rr = (const T *)&ro;
+            const T *rss = (const T *)&rso;
             V xn, st;
             T *xns = (T *)&xn, *sts = (T *)&st;
 #pragma unroll
             for (int e = 0; e < VN; e++) {
-                T am = T(0);
+                T am = T(0), ac = T(0);
 #pragma unroll
-                for (int j = 0; j < M; j++) am = fma(((const T *)&hj[j])[e], sj[j], am);
-                xns[e] = fma(beta, rs[e] * cf, xs[e]) - am;
-                sts[e] = xns[e] - xs[e];
+                for (int j = 0; j < M; j++) {
+                    am = fma(((const T *)&hj[j])[e], sj[j], am);
+                    if constexpr (LEAN) ac = fma(((const T *)&hj[j])[e], ij[j], ac);
+                }
+                update_point<T, LEAN>(xs[e], rr[e], rss[e], am, ac, beta, cf, xns[e], sts[e]);
             }
             xv[i] = xn;
             sv[i] = st;
         }
     } else {
         for (long long i = t0; i < n; i += stride) {
-            T am = T(0);
-            for (int j = 0; j < m; j++) am = fma(ldg(h + j * n + i), s[j], am);
-            const T xo = x[i];
-            const T xn = fma(beta, r[i] * cf, xo) - am;
+            T am = T(0), ac = T(0);
+            for (int j = 0; j < m; j++) {
+                const T hv = ldg(h + j * n + i);
+                am = fma(hv, s[j], am);
+                if constexpr (LEAN) ac = fma(hv, ((mask >> j) & 1u) ? T(1) : T(0), ac);
+            }
+            const T ro = r[i];
+            T rso = ro;
+            if constexpr (LEAN) rso = rs[i];
+            T xn, st;
+            update_point<T, LEAN>(x[i], ro, rso, am, ac, beta, cf, xn, st);
             x[i] = xn;
-            step[i] = xn - xo;
+            step[i] = st;
         }
     }
 }
 
-// x_new = x + beta cf r - sum_j H_j s_j with H_j = DX_j + beta DF_j
-// (AAR.c:116-117, 225-231); the step x_new - x_old goes to `step`.
-// M: history depth known at compile time (all m loads in flight at once),
-// VN points per thread and step through 16-byte vectors; M = 0 is the
-// generic path (runtime m, scalar).
+// One launch of aar_update_block over the whole vector (M, LEAN as there).
 template <typename T, int M>
 __global__ void __launch_bounds__(kReduceThreads) aar_update_kernel(int m, T *__restrict__ x,
                                                                     const T *__restrict__ r,
@@ -585,6 +668,35 @@ __global__ void __launch_bounds__(kReduceThreads) aar_update_kernel(int m, T *__
                                                                     const DevCtrl *ctrl) {
     if (solve_done(ctrl)) return;
     aar_update_block<T, M, (M > 0)>(m, x, r, h, step, beta, cf, n, ctrl, blockIdx.x, gridDim.x);
+}
+
+template <typename T, int M>
+__global__ void __launch_bounds__(kReduceThreads) aar_update_lean_kernel(int m, T *__restrict__ x,
+                                                                         const T *__restrict__ r,
+                                                                         const T *__restrict__ rs,
+                                                                         const T *__restrict__ h,
+                                                                         T *__restrict__ step, T beta,
+                                                                         T cf, long long n, unsigned mask,
+                                                                         const DevCtrl *ctrl) {
+    if (solve_done(ctrl)) return;
+    aar_update_block<T, M, (M > 0), true>(m, x, r, h, step, beta, cf, n, ctrl, blockIdx.x, gridDim.x, rs, mask);
+}
+
+// x += sum_mask H_j - beta cf (r - rs): the iterate of a lean FP32 solve that
+// stopped between extrapolations (its Richardson passes left x out).
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) recur_fold_kernel(int m, T *__restrict__ x,
+                                                                    const T *__restrict__ r,
+                                                                    const T *__restrict__ rs,
+                                                                    const T *__restrict__ h, T beta,
+                                                                    T cf, long long n, unsigned mask) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        T ac = T(0);
+        for (int j = 0; j < m; j++)
+            if ((mask >> j) & 1u) ac = ac + ldg(h + j * n + i);
+        x[i] = x[i] + (ac - beta * ((r[i] - rs[i]) * cf));
+    }
 }
 
 template <typename T>
@@ -715,6 +827,18 @@ cudaError_t Kernels<T>::richardson_recur(const StencilLaunch &L, const Weights<T
 }
 
 template <typename T>
+cudaError_t Kernels<T>::richardson_lean(const StencilLaunch &L, const Weights<T> &w, const T *r, T *r2,
+                                        T *dx, T *df, S c, S cf, double hb, const DevCtrl *ctrl) {
+    if constexpr (std::is_same<typename RealOf<T>::type, float>::value) {
+        RichLeanOp<T> op{r, r2, dx, df, (T)c, (T)cf, T(hb), nullptr, ctrl};
+        return launch_stencil<T>(L, w, op);
+    } else {  // FP64 keeps the reference form
+        (void)L, (void)w, (void)r, (void)r2, (void)dx, (void)df, (void)c, (void)cf, (void)hb, (void)ctrl;
+        return cudaErrorInvalidValue;
+    }
+}
+
+template <typename T>
 cudaError_t Kernels<T>::residual_recur(const StencilLaunch &L, const Weights<T> &w, const T *step,
                                        T *r, T *df, T *hc, S cf, double hb, double *partials,
                                        const DevCtrl *ctrl) {
@@ -831,6 +955,50 @@ cudaError_t Kernels<T>::gram(int kind, int m, const T *dx, const T *df, const T 
     } else {
     if (kind == GRAM_SYM) return gram_dispatch<T, GRAM_SYM>(m, dx, df, r, n, partials, blocks, ctrl, s);
     return gram_dispatch<T, GRAM_GALERKIN>(m, dx, df, r, n, partials, blocks, ctrl, s);
+    }
+}
+
+template <typename T>
+cudaError_t Kernels<T>::aar_update_lean(int m, T *x, const T *r, const T *rs, const T *h, T *step,
+                                        double beta, S cf, long long n, unsigned mask, const DevCtrl *ctrl,
+                                        cudaStream_t s) {
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 8);
+    if constexpr (!std::is_same<typename RealOf<T>::type, float>::value) {  // FP64 keeps the reference form
+        (void)m, (void)x, (void)r, (void)rs, (void)h, (void)step, (void)beta, (void)cf, (void)mask, (void)ctrl,
+            (void)s, (void)blocks;
+        return cudaErrorInvalidValue;
+    } else if constexpr (IsCplx<T>::value) {
+        aar_update_lean_kernel<T, 0><<<blocks, kReduceThreads, 0, s>>>(m, x, r, rs, h, step, T(beta), (T)cf, n,
+                                                                      mask, ctrl);
+    } else {
+        const bool vec = n % Vec4<T>::N == 0;
+        switch (vec ? m : 0) {
+#define LSG_UPD_CASE(MM)                                                                                      \
+    case MM:                                                                                                  \
+        aar_update_lean_kernel<T, MM><<<blocks, kReduceThreads, 0, s>>>(m, x, r, rs, h, step, (T)beta, (T)cf, \
+                                                                       n, mask, ctrl);                        \
+        break;
+            LSG_UPD_CASE(1) LSG_UPD_CASE(2) LSG_UPD_CASE(3) LSG_UPD_CASE(4)
+            LSG_UPD_CASE(5) LSG_UPD_CASE(6) LSG_UPD_CASE(7) LSG_UPD_CASE(8)
+#undef LSG_UPD_CASE
+        default:
+            aar_update_lean_kernel<T, 0><<<blocks, kReduceThreads, 0, s>>>(m, x, r, rs, h, step, (T)beta, (T)cf,
+                                                                          n, mask, ctrl);
+        }
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kernels<T>::recur_fold(int m, T *x, const T *r, const T *rs, const T *h, double beta, S cf,
+                                   long long n, unsigned mask, cudaStream_t s) {
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 8);
+    if constexpr (!std::is_same<typename RealOf<T>::type, float>::value) {
+        (void)m, (void)x, (void)r, (void)rs, (void)h, (void)beta, (void)cf, (void)mask, (void)s, (void)blocks;
+        return cudaErrorInvalidValue;
+    } else {
+        recur_fold_kernel<T><<<blocks, kReduceThreads, 0, s>>>(m, x, r, rs, h, T(beta), (T)cf, n, mask);
+        return cudaGetLastError();
     }
 }
 

@@ -85,7 +85,8 @@ static int stencil_slots(int sms) {
 // ---------------------------------------------------------------- work arrays
 
 // One allocation per (device, element size, grid points, history depth):
-//   xalt, r0, r1                 three vectors (ping-pong partners)
+//   xalt, r0, r1, rs             four vectors (ping-pong partners; rs: the
+//                                cycle-start residual of the lean FP32 AAR)
 //   dx[m], df[m]                 the history, column j at offset j*n
 //   partials                     per-block FP64 sums
 //   ctrl                         DevCtrl
@@ -97,7 +98,7 @@ struct Workspace {
     long long n = 0;
     int m = 0;
     char *base = nullptr;
-    void *xalt = nullptr, *r0 = nullptr, *r1 = nullptr, *dx = nullptr, *df = nullptr;
+    void *xalt = nullptr, *r0 = nullptr, *r1 = nullptr, *rs = nullptr, *dx = nullptr, *df = nullptr;
     float *r32 = nullptr, *e32 = nullptr;
     double *partials = nullptr;
     long long partials_cap = 0;
@@ -159,6 +160,7 @@ static int get_workspace(size_t es, long long n, int m, bool mixed, const Geom &
     const size_t o_xalt = bytes; bytes += vec;
     const size_t o_r0 = bytes; bytes += vec;
     const size_t o_r1 = bytes; bytes += vec;
+    const size_t o_rs = bytes; bytes += vec;
     const size_t o_dx = bytes; bytes += align_up((size_t)n * es * (size_t)m);
     const size_t o_df = bytes; bytes += align_up((size_t)n * es * (size_t)m);
     size_t o_r32 = 0, o_e32 = 0;
@@ -189,6 +191,7 @@ static int get_workspace(size_t es, long long n, int m, bool mixed, const Geom &
     ws->xalt = base + o_xalt;
     ws->r0 = base + o_r0;
     ws->r1 = base + o_r1;
+    ws->rs = base + o_rs;
     ws->dx = base + o_dx;
     ws->df = base + o_df;
     if (mixed) {
@@ -414,7 +417,10 @@ static long long richardson_count(int last, int p) {
 // (the device sets ctrl->done) and resume from any iteration.
 //   FP64 follows the reference's true-residual form: x and r ping-pong.
 //   FP32 uses the residual recurrence: x in place, only r ping-pongs, and
-//   b is not read after the initial residual.
+//   b is not read after the initial residual.  When a cycle's Richardson
+//   columns all stay in the history (p - 1 <= m) the Richardson passes leave
+//   x out ("lean"): r rotates through three buffers so the cycle-start
+//   residual survives, and the extrapolation rebuilds x from it.
 template <typename T>
 struct AarLoop {
     using S = typename ScalarOf<T>::type;
@@ -433,11 +439,12 @@ struct AarLoop {
     StencilLaunch Lres;  // extrapolation-step residual of the recurrence form
     int sb, sbr, rb, gb; // stencil blocks of L and of Lres (partial sums)
     T *X[2];
-    T *Rv[2];
+    T *Rv[3];
     T *DX, *DF;
     DevCtrl *ctrl;
     double *part;
-    int xc = 0, rc = 0;
+    bool lean = false;
+    int xc = 0, rc = 0, rsc = 0;  // rsc: buffer of the cycle-start residual (lean)
 
     AarLoop(Run &R_, const lsg_operator *op, const lsg_params *prm_, T *x, const T *b_, Workspace *ws_)
         : R(R_), prm(prm_), ws(ws_), b(b_) {
@@ -445,6 +452,7 @@ struct AarLoop {
         n = g.n;
         m = prm->m;
         p = prm->p;
+        lean = recur && m <= 32 && p - 1 <= m;
         w = make_weights<T>(op);
         cf = jacobi_factor<T>(op);
         const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
@@ -459,7 +467,7 @@ struct AarLoop {
         int plz = 0;
         const long long pb = Kernels<T>::paired_plan(g, &plz);
         const uintptr_t al = (uintptr_t)x | (uintptr_t)ws->xalt | (uintptr_t)ws->r0 | (uintptr_t)ws->r1 |
-                             (uintptr_t)ws->dx | (uintptr_t)ws->df;
+                             (uintptr_t)ws->rs | (uintptr_t)ws->dx | (uintptr_t)ws->df;
         const bool pairable = recur && pb > 0 && op->radius == 6 && g.nx % 2 == 0 && (al & 7u) == 0;
         if (pairable) {
             if (Lr.paired == -1) {  // untuned: the paired march
@@ -479,17 +487,50 @@ struct AarLoop {
         X[1] = (T *)ws->xalt;
         Rv[0] = (T *)ws->r0;
         Rv[1] = (T *)ws->r1;
+        Rv[2] = (T *)ws->rs;
         DX = (T *)ws->dx;
         DF = (T *)ws->df;
         ctrl = ws->ctrl;
         part = ws->partials;
     }
     bool is_anderson(int it) const { return it % p == 0 && it > 1; }
-    // r buffer holding the residual after iteration `last`
+    // Lean rotation: a Richardson pass writes the buffer that is neither the
+    // current nor the cycle-start residual; the extrapolation residual is
+    // computed in place and becomes the next cycle's start.
+    static int lean_target(int s, int c) { return s == c ? (s + 1) % 3 : 3 - s - c; }
+    // r buffers holding the residual (and, lean, the cycle-start residual)
+    // after iteration `last`
     void sync_parity(int last) {
+        if (lean) {
+            int s = 0, c = 0;
+            for (int it = 1; it <= last; it++) {
+                if (is_anderson(it)) s = c;
+                else c = lean_target(s, c);
+            }
+            rc = c;
+            rsc = s;
+            xc = 0;
+            return;
+        }
         const long long rich = richardson_count(last, p);
         rc = (int)(rich & 1);
         xc = recur ? 0 : rc;
+    }
+    // History columns written by the Richardson passes since the last
+    // extrapolation, up to iteration `last` (bit (k-1) % m for iteration k).
+    unsigned cycle_mask(int last) const {
+        unsigned mask = 0;
+        for (int k = last; k >= 1 && !is_anderson(k); k--) mask |= 1u << ((k - 1) % m);
+        return mask;
+    }
+    // A lean solve that stopped after Richardson iteration `last` has not
+    // added that cycle's steps to x yet: fold them in.
+    int finish(int last) {
+        if (!lean || last < 1 || is_anderson(last)) return LSG_OK;
+        sync_parity(last);
+        LSG_KC(LSG_K_UPDATE, Kernels<T>::recur_fold(m, X[0], Rv[rc], Rv[rsc], DX, prm->beta, cf, n,
+                                                    cycle_mask(last), R.s));
+        return LSG_OK;
     }
     int reset_history() {
         LSG_CUDA(cudaMemsetAsync(DX, 0, sizeof(T) * (size_t)n * m, R.s));
@@ -508,14 +549,24 @@ struct AarLoop {
             if (recur) {
                 // the step goes to the spare vector: the residual reads it as its stencil input
                 T *step = (T *)ws->xalt;
-                LSG_KC(LSG_K_UPDATE, Kernels<T>::aar_update(m, X[0], Rv[rc], DX, step, prm->beta, cf, n, ctrl, R.s));
+                if (lean)
+                    LSG_KC(LSG_K_UPDATE, Kernels<T>::aar_update_lean(m, X[0], Rv[rc], Rv[rsc], DX, step, prm->beta,
+                                                                     cf, n, cycle_mask(it - 1), ctrl, R.s));
+                else
+                    LSG_KC(LSG_K_UPDATE, Kernels<T>::aar_update(m, X[0], Rv[rc], DX, step, prm->beta, cf, n, ctrl, R.s));
                 LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual_recur(Lres, w, step, Rv[rc], dfc, dxc, cf, prm->beta, part, ctrl));
+                rsc = rc;
             } else {
                 LSG_KC(LSG_K_UPDATE, Kernels<T>::aar_update(m, X[xc], Rv[rc], DX, dxc, prm->beta, cf, n, ctrl, R.s));
                 LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(L, w, RES_ANDERSON, X[xc], b, Rv[rc], dfc, dxc, cf,
                                                             prm->beta, part, ctrl));
             }
             LSG_KC(LSG_K_SMALL, finalize_norm(part, recur ? sbr : sb, ctrl, NF_CHECK, prm->tol, it, R.s, W));
+        } else if (lean) {
+            const int t = lean_target(rsc, rc);
+            LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson_lean(Lr, w, Rv[rc], Rv[t], dxc, dfc, prm->omega * cf,
+                                                                 cf, prm->beta, ctrl));
+            rc = t;
         } else if (recur) {
             LSG_KC(LSG_K_RICHARDSON, Kernels<T>::richardson_recur(Lr, w, Rv[rc], X[0], Rv[rc ^ 1], dxc, dfc,
                                                                   prm->omega * cf, cf, prm->beta, ctrl));
@@ -559,6 +610,10 @@ int aar_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const 
     const int last = c.done ? c.iters : prm->max_iter;
     if (!AarLoop<T>::recur && (richardson_count(last, prm->p) & 1))
         LSG_CUDA(cudaMemcpyAsync(x, A.X[1], sizeof(T) * (size_t)A.n, cudaMemcpyDeviceToDevice, R.s));
+    if (!c.done) {
+        rc = A.finish(last);
+        if (rc != LSG_OK) return rc;
+    }
     LSG_CUDA(cudaStreamSynchronize(R.s));
     *out = c;
     return LSG_OK;
@@ -812,6 +867,10 @@ int solve_mixed_t(const lsg_operator *op, const lsg_params *prm, T64 *x, const T
         LSG_CUDA(cudaMemcpy(&ci, A.ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost));
         if (ci.status == LSG_NAN_DETECTED) { status = LSG_NAN_DETECTED; break; }
         iters = ci.done ? ci.iters : prm->max_iter;
+        if (!ci.done) {
+            rc = A.finish(iters);
+            if (rc != LSG_OK) return rc;
+        }
         // fold the correction into x64 (e = 0 afterwards) and replace the residual
         LSG_KC(LSG_K_REFINE, (ir_correct<T64, T32>(x, e32, n, s)));
         replacements++;

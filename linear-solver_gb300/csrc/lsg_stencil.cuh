@@ -260,6 +260,32 @@ __device__ __forceinline__ void st_pair(T *p, T a, T b) {
     *reinterpret_cast<typename Vec2Of<T>::type *>(p) = v;
 }
 
+// Two-wide arithmetic of the paired march.  FP32 uses the packed f32x2
+// instructions (one instruction, two round-to-nearest results); each lane
+// equals the scalar operation, so the march stays bit-identical to the
+// one-column driver.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ double2 add2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 mul2(double2 a, double2 b) { return make_double2(a.x * b.x, a.y * b.y); }
+__device__ __forceinline__ double2 fma2(double2 a, double2 b, double2 c) {
+    return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y));
+}
+template <typename P, typename T>
+__device__ __forceinline__ P mk2(T a, T b) {
+    P v;
+    v.x = a;
+    v.y = b;
+    return v;
+}
+
+// Functors that set PACKED run the paired march's sums as packed f32x2
+// instructions; the others (a centre operand or a reduction to keep in
+// registers) keep scalar sums, which need fewer aligned register pairs.
+template <class Op, class = void> struct IsPacked { static constexpr bool value = false; };
+template <class Op> struct IsPacked<Op, std::void_t<decltype(Op::PACKED)>> { static constexpr bool value = Op::PACKED; };
+
 template <typename T, int BY, int NY, class Op>
 __device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T> &w, int lz, Op &op,
                                                  T *smem0, T *smem1, int bx, int by, int bz, long long blk) {
@@ -318,7 +344,9 @@ __device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T>
 #pragma unroll
     for (int a = 0; a < (Op::NACC > 0 ? Op::NACC : 1); a++) acc[a].zero();
 
-    T q[NY][2][Q];
+    using PT = typename Vec2Of<T>::type;
+    constexpr bool PACK = IsPacked<Op>::value;
+    PT q[NY][Q];  // the z ring of both columns, as register pairs
     unsigned zl = (unsigned)wrap_index(z0 - RQ, g.nz);
     const unsigned nxy = (unsigned)g.nxy, nz = (unsigned)g.nz;
 #pragma unroll
@@ -327,11 +355,11 @@ __device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T>
 #pragma unroll
         for (int k = 0; k < NY; k++) {
             const Two<T> v = op.fetch_pair(base + col[k]);
-            q[k][0][s] = v.a;
-            q[k][1][s] = v.b;
+            q[k][s] = mk2<PT>(v.a, v.b);
         }
         zl = (zl + 1 == nz) ? 0u : zl + 1;
     }
+
     Two<T> qn[NY], hn[NH], cn[NY];
     {
         const unsigned lb = zl * nxy, zb = (unsigned)z0 * nxy;
@@ -355,9 +383,8 @@ __device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T>
         const unsigned zbase = (unsigned)z * nxy;
 #pragma unroll
         for (int k = 0; k < NY; k++) {
-            q[k][0][HEAD] = qn[k].a;
-            q[k][1][HEAD] = qn[k].b;
-            st_pair(sm + (RQ + ty * NY + k) * FX + RQ + 2 * tx, q[k][0][CEN], q[k][1][CEN]);
+            q[k][HEAD] = mk2<PT>(qn[k].a, qn[k].b);
+            *reinterpret_cast<PT *>(sm + (RQ + ty * NY + k) * FX + RQ + 2 * tx) = q[k][CEN];
         }
 #pragma unroll
         for (int s = 0; s < NH; s++)
@@ -380,40 +407,56 @@ __device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T>
         __syncthreads();
         const T *col0 = sm + (RQ + ty * NY) * FX + RQ + 2 * tx;
         // y neighbours of both columns for rows r0-RQ .. r0+NY-1+RQ (own rows from the queue)
-        T ya[NY + 2 * RQ], yb[NY + 2 * RQ];
+        PT yv[NY + 2 * RQ];
 #pragma unroll
         for (int j = 0; j < RQ; j++) {
-            const Two<T> lo = ld_pair(col0 + (j - RQ) * FX), hi = ld_pair(col0 + (NY + j) * FX);
-            ya[j] = lo.a; yb[j] = lo.b;
-            ya[RQ + NY + j] = hi.a; yb[RQ + NY + j] = hi.b;
+            yv[j] = *reinterpret_cast<const PT *>(col0 + (j - RQ) * FX);
+            yv[RQ + NY + j] = *reinterpret_cast<const PT *>(col0 + (NY + j) * FX);
         }
 #pragma unroll
-        for (int k = 0; k < NY; k++) {
-            ya[RQ + k] = q[k][0][CEN];
-            yb[RQ + k] = q[k][1][CEN];
-        }
+        for (int k = 0; k < NY; k++) yv[RQ + k] = q[k][CEN];
 #pragma unroll
         for (int k = 0; k < NY; k++) {
-            // x window: columns gx-RQ .. gx+1+RQ of row k as 7 pairs
-            T xv[2 * RQ + 2];
+            // x window: columns gx-RQ .. gx+1+RQ of row k as RQ+1 pairs; pair j
+            // holds columns gx-RQ+2j and gx-RQ+2j+1
+            PT xp[RQ + 1];
 #pragma unroll
-            for (int j = 0; j <= RQ; j++) {
-                const Two<T> v = ld_pair(col0 + k * FX - RQ + 2 * j);
-                xv[2 * j] = v.a;
-                xv[2 * j + 1] = v.b;
-            }
-            T aa = w.w[0] * q[k][0][CEN], ab = w.w[0] * q[k][1][CEN];
+            for (int j = 0; j <= RQ; j++) xp[j] = *reinterpret_cast<const PT *>(col0 + k * FX - RQ + 2 * j);
+            PT acc2;
+            if constexpr (PACK) {  // packed two-wide arithmetic
+                acc2 = mul2(mk2<PT>(w.w[0], w.w[0]), q[k][CEN]);
 #pragma unroll
-            for (int p = 1; p <= RQ; p++) {
-                const T sa = (xv[RQ - p] + xv[RQ + p]) + (ya[RQ + k - p] + ya[RQ + k + p]);
-                const T sb = (xv[RQ + 1 - p] + xv[RQ + 1 + p]) + (yb[RQ + k - p] + yb[RQ + k + p]);
-                const T za = q[k][0][(CEN + Q - p) % Q] + q[k][0][(CEN + p) % Q];
-                const T zb = q[k][1][(CEN + Q - p) % Q] + q[k][1][(CEN + p) % Q];
-                aa = fma(w.w[p], sa + za, aa);
-                ab = fma(w.w[p], sb + zb, ab);
+                for (int p = 1; p <= RQ; p++) {
+                    // x pair at distance p: (col gx-p + col gx+p, col gx+1-p + col gx+1+p)
+                    PT xs;
+                    if ((RQ - p) % 2 == 0)  // both operands are loaded pairs
+                        xs = add2(xp[(RQ - p) / 2], xp[(RQ + p) / 2]);
+                    else
+                        xs = mk2<PT>(xp[(RQ - p) / 2].y + xp[(RQ + p) / 2].y,
+                                     xp[(RQ + 1 - p) / 2].x + xp[(RQ + 1 + p) / 2].x);
+                    const PT ys = add2(yv[RQ + k - p], yv[RQ + k + p]);
+                    const PT zs = add2(q[k][(CEN + Q - p) % Q], q[k][(CEN + p) % Q]);
+                    acc2 = fma2(mk2<PT>(w.w[p], w.w[p]), add2(add2(xs, ys), zs), acc2);
+                }
+            } else {  // the same sums, one column at a time
+                T aa = w.w[0] * q[k][CEN].x, ab = w.w[0] * q[k][CEN].y;
+#pragma unroll
+                for (int p = 1; p <= RQ; p++) {
+                    const T xm_a = ((RQ - p) % 2 == 0) ? xp[(RQ - p) / 2].x : xp[(RQ - p) / 2].y;
+                    const T xp_a = ((RQ + p) % 2 == 0) ? xp[(RQ + p) / 2].x : xp[(RQ + p) / 2].y;
+                    const T xm_b = ((RQ + 1 - p) % 2 == 0) ? xp[(RQ + 1 - p) / 2].x : xp[(RQ + 1 - p) / 2].y;
+                    const T xp_b = ((RQ + 1 + p) % 2 == 0) ? xp[(RQ + 1 + p) / 2].x : xp[(RQ + 1 + p) / 2].y;
+                    const T sa = (xm_a + xp_a) + (yv[RQ + k - p].x + yv[RQ + k + p].x);
+                    const T sb = (xm_b + xp_b) + (yv[RQ + k - p].y + yv[RQ + k + p].y);
+                    const T za = q[k][(CEN + Q - p) % Q].x + q[k][(CEN + p) % Q].x;
+                    const T zb = q[k][(CEN + Q - p) % Q].y + q[k][(CEN + p) % Q].y;
+                    aa = fma(w.w[p], sa + za, aa);
+                    ab = fma(w.w[p], sb + zb, ab);
+                }
+                acc2 = mk2<PT>(aa, ab);
             }
             if (valid[k])
-                op.store_pair(zbase + col[k], Two<T>{q[k][0][CEN], q[k][1][CEN]}, Two<T>{aa, ab}, cc[k], acc);
+                op.store_pair(zbase + col[k], Two<T>{q[k][CEN].x, q[k][CEN].y}, Two<T>{acc2.x, acc2.y}, cc[k], acc);
         }
         sm = (sm == smem0) ? smem1 : smem0;
         return ++z < z1;

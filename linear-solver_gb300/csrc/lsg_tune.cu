@@ -66,6 +66,8 @@ template <> int dtype_of<cplx<double>>() { return LSG_C128; }
 template <> int dtype_of<cplx<float>>() { return LSG_C64; }
 
 // Times `reps` launches of the Richardson pass in shape (tile, lz); ms per launch.
+// FP32 vectors time the lean recurrence pass (x left out), the form AAR uses
+// by default (p - 1 <= m).
 template <typename T>
 static int time_rich(const StencilLaunch &L, const Weights<T> &w, T *v, long long n, const DevCtrl *ctrl,
                      cudaEvent_t e0, cudaEvent_t e1, float *ms) {
@@ -75,7 +77,7 @@ static int time_rich(const StencilLaunch &L, const Weights<T> &w, T *v, long lon
     T *x = v, *r = v + n, *r2 = v + 2 * n, *dx = v + 3 * n, *df = v + 4 * n, *x2 = v + 5 * n;
     const T *b = v + 6 * n;
     auto launch = [&]() -> cudaError_t {
-        if (recur) return Kernels<T>::richardson_recur(L, w, r, x, r2, dx, df, c, cf, 0.5, ctrl);
+        if (recur) return Kernels<T>::richardson_lean(L, w, r, r2, dx, df, c, cf, 0.5, ctrl);
         return Kernels<T>::richardson(L, w, RICH_AAR, x, r, b, x2, r2, dx, df, c, cf, 0.5, ctrl);
     };
     for (int k = 0; k < 2; k++)

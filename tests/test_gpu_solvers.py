@@ -140,6 +140,24 @@ def test_fp32_solvers_converge(lsg, oracle):
         assert _merr(x.double().cpu().numpy(), xf) < 5e-3, s
 
 
+@pytest.mark.parametrize("m,p,k", [(7, 6, 17), (7, 6, 18), (7, 6, 5), (3, 6, 17), (3, 1, 9), (5, 4, 13)])
+def test_fp32_iterate_at_max_iter(lsg, oracle, m, p, k):
+    """The FP32 AAR iterate after k iterations against the oracle's FP64
+    iterate: k between extrapolations (the Richardson passes of a lean solve
+    leave x out, so the stop folds the cycle's steps into x), k at an
+    extrapolation, p - 1 > m (the recurrence keeps x in its passes), p = 1."""
+    import torch
+    import workloads
+    b = workloads.uniform_rhs(24, 3)
+    x0 = np.random.default_rng(4).uniform(-1, 1, b.shape)
+    xr, _ = oracle.solve("aar", b, x0, m=m, p=p, max_iter=k, tol=1e-30)
+    x, r = lsg.aar(lsg.Operator(24), _t(b, torch.float32), _t(x0, torch.float32), m=m, p=p, max_iter=k,
+                   tol=1e-30)
+    assert r["status"] != 0  # stopped by max_iter
+    x = x.double().cpu().numpy()
+    assert np.linalg.norm(x - xr) <= 2e-5 * np.linalg.norm(xr), (m, p, k)
+
+
 def test_mixed_precision_to_1e10(lsg, oracle):
     import workloads
     b = workloads.uniform_rhs(48, 0)
