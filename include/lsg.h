@@ -179,7 +179,8 @@ int lsg_aar_mixed_batched(const lsg_operator *ops, int count, const lsg_params *
  * of `op` and vector type `dtype` on the device, caches the fastest, and
  * reports it.  Solves on that grid then use the cached shape.  Radius 6. */
 typedef struct lsg_tune_info {
-    int tile;             /* tile variant index */
+    int tile;             /* tile variant index; 3, 4: the FP32 two-columns-per-lane
+                             march (tile = 64 x (threads_y * rows_per_thread)) */
     int threads_y;        /* block = 32 x threads_y threads */
     int rows_per_thread;  /* tile = 32 x (threads_y * rows_per_thread) columns */
     int lz;               /* z planes per block */

@@ -184,6 +184,7 @@ struct StencilLaunch {
     cudaStream_t stream;
     int tile = 0;     // tile variant (passes without partial sums only)
     int paired = -1;  // 1: the two-columns-per-lane march (planned by Kernels<T>::paired_plan);
+                      // 2: its 64 x 8 shape (passes without partial sums only);
                       // -1: the solver may choose it; 0: not
 };
 
@@ -202,6 +203,11 @@ template <> struct TileOf<cplx<float>> { static constexpr int BY = 8, NY = 2, MI
 constexpr int kTileVariants = 3;
 constexpr int kTilePaired = 3;  // tuner code of the two-columns-per-lane FP32 march
 constexpr int kPairBY = 8, kPairNY = 2, kPairMINB = 2;  // its block: 32 x 8 threads, 64 x 16 tile
+// A second shape of the paired march for the Richardson pass (tuner code 4):
+// 32 x 4 threads, 64 x 8 tile, 4 blocks per SM.  Passes with a reduction
+// keep the first shape (in the second they spill: 4 halo slots per thread).
+constexpr int kTilePaired2 = 4;
+constexpr int kPair2BY = 4, kPair2NY = 2, kPair2MINB = 4;
 template <typename T, int V> struct TileVar;
 template <> struct TileVar<double, 0> { static constexpr int BY = 8, NY = 2, MINB = 1; };
 template <> struct TileVar<double, 1> { static constexpr int BY = 4, NY = 4, MINB = 1; };
@@ -292,6 +298,8 @@ struct Kernels {
     // Paired (two columns per lane) march of the FP32 recurrence passes: its z
     // depth (*lz) and block count on grid g; 0 when T has none.
     static long long paired_plan(const Geom &g, int *lz);
+    // Resident blocks per SM of paired shape 1 or 2 (0 when T has none).
+    static int paired_blocks_per_sm(int shape);
     // y / r update driven by one stencil pass over x.  RES_ANDERSON also
     // completes the history column hc (holding x_new - x_old) with hb * DF_col.
     static cudaError_t residual(const StencilLaunch &L, const Weights<T> &w, int mode,

@@ -367,6 +367,34 @@ long long Kernels<T>::paired_plan(const Geom &g, int *lz) {
     }
 }
 
+template <typename T>
+int Kernels<T>::paired_blocks_per_sm(int shape) {
+    if constexpr (std::is_same<T, float>::value) {
+        int occ = 0;
+        const cudaError_t e =
+            shape == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                             &occ, stencil_x2_kernel<T, kPair2BY, kPair2NY, kPair2MINB, RichLeanOp<T>>, 32 * kPair2BY, 0)
+                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                             &occ, stencil_x2_kernel<T, kPairBY, kPairNY, kPairMINB, RichLeanOp<T>>, 32 * kPairBY, 0);
+        if (e != cudaSuccess || occ < 1) {
+            cudaGetLastError();
+            occ = 1;
+        }
+        return occ;
+    } else {
+        (void)shape;
+        return 0;
+    }
+}
+
+template <typename T, int BY, int NY, int MB, class Op>
+cudaError_t launch_x2(const StencilLaunch &L, const Weights<T> &w, const Op &op) {
+    const dim3 grid((unsigned)((L.g.nx + 63) / 64), (unsigned)((L.g.ny + BY * NY - 1) / (BY * NY)),
+                    (unsigned)((L.g.nz + L.lz - 1) / L.lz));
+    stencil_x2_kernel<T, BY, NY, MB, Op><<<grid, dim3(32, BY), 0, L.stream>>>(L.g, w, L.lz, op);
+    return cudaGetLastError();
+}
+
 template <typename T, int V, class Op>
 cudaError_t launch_stencil_var(const StencilLaunch &L, const Weights<T> &w, const Op &op) {
     constexpr int BY = TileVar<T, V>::BY, NY = TileVar<T, V>::NY, MB = TileVar<T, V>::MINB;
@@ -382,15 +410,13 @@ cudaError_t launch_stencil(const StencilLaunch &L, const Weights<T> &w, const Op
     constexpr int BY = TileOf<T>::BY, NY = TileOf<T>::NY;
     // L.paired: the caller planned this launch as the paired march (its z depth
     // in L.lz, its block count in the caller's partial-sum bookkeeping)
-    if (L.paired == 1) {
+    if (L.paired >= 1) {
         if constexpr (IsPaired<Op>::value && std::is_same<T, float>::value) {
             if (!paired_ok<T>(L, w, op)) return cudaErrorInvalidValue;
-            const dim3 grid((unsigned)((L.g.nx + 63) / 64), (unsigned)((L.g.ny + kPairBY * kPairNY - 1) /
-                                                                      (kPairBY * kPairNY)),
-                            (unsigned)((L.g.nz + L.lz - 1) / L.lz));
-            stencil_x2_kernel<T, kPairBY, kPairNY, kPairMINB, Op>
-                <<<grid, dim3(32, kPairBY), 0, L.stream>>>(L.g, w, L.lz, op);
-            return cudaGetLastError();
+            if (L.paired == 1) return launch_x2<T, kPairBY, kPairNY, kPairMINB>(L, w, op);
+            if constexpr (Op::NACC == 0)
+                if (L.paired == 2) return launch_x2<T, kPair2BY, kPair2NY, kPair2MINB>(L, w, op);
+            return cudaErrorInvalidValue;
         } else {
             return cudaErrorInvalidValue;
         }

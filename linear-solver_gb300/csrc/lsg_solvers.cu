@@ -477,7 +477,7 @@ struct AarLoop {
             Lres.paired = 1;
             Lres.lz = plz;
             sbr = (int)pb;
-        } else if (Lr.paired == 1) {  // tuned paired shape the vectors cannot take
+        } else if (Lr.paired >= 1) {  // tuned paired shape the vectors cannot take
             Lr = L;
         }
         if (Lr.paired == -1) Lr.paired = 0;
@@ -631,7 +631,7 @@ int prich_core(Run &R, bool galerkin, const lsg_operator *op, const lsg_params *
     const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
     const StencilLaunch L{g, lz, R.s};
     StencilLaunch Lr = rich_launch<T>(op, L);
-    if (Lr.paired == 1) Lr = L;  // the paired march serves the AAR recurrence passes only
+    if (Lr.paired >= 1) Lr = L;  // the paired march serves the AAR recurrence passes only
     Lr.paired = 0;
     const int rb = reduce_blocks(n, R.sms);
     T *X[2] = {x, (T *)ws->xalt};

@@ -67,7 +67,7 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
     constexpr int TY = BY * NY;
     constexpr int FX = TX + 2 * RQ;
     constexpr int NT = 32 * BY;
-    constexpr int H = 2 * RQ * FX + TY * 2 * RQ;  // halo cells of one plane
+    constexpr int H = 2 * RQ * TX + TY * 2 * RQ;  // halo cells of one plane (no corners: the stencil is a star)
     constexpr int NH = (H + NT - 1) / NT;
     constexpr int Q = 2 * RQ + 1;
 
@@ -97,13 +97,13 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
         ho[s] = 0;
         if (h < H) {
             int fy, fx;
-            if (h < RQ * FX) {                       // top strip
-                fy = h / FX; fx = h % FX;
-            } else if (h < 2 * RQ * FX) {            // bottom strip
-                const int hh = h - RQ * FX;
-                fy = RQ + TY + hh / FX; fx = hh % FX;
+            if (h < RQ * TX) {                       // top strip
+                fy = h / TX; fx = RQ + h % TX;
+            } else if (h < 2 * RQ * TX) {            // bottom strip
+                const int hh = h - RQ * TX;
+                fy = RQ + TY + hh / TX; fx = RQ + hh % TX;
             } else {                                 // left / right strips
-                const int hh = h - 2 * RQ * FX;
+                const int hh = h - 2 * RQ * TX;
                 const int row = hh / (2 * RQ), c = hh % (2 * RQ);
                 fy = RQ + row;
                 fx = c < RQ ? c : TX + c;
@@ -294,7 +294,7 @@ __device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T>
     constexpr int TY = BY * NY;
     constexpr int FX = TX + 2 * RQ;  // even, so every pair offset is 8-byte aligned
     constexpr int NT = 32 * BY;
-    constexpr int PR = FX / 2;       // pairs per full shared row
+    constexpr int PR = TX / 2;       // pairs per top / bottom halo row (no corners: the stencil is a star)
     constexpr int HP = RQ * PR * 2 + TY * RQ;  // halo pairs: top, bottom, then RQ / 2 per side per row
     constexpr int NH = (HP + NT - 1) / NT;
     constexpr int Q = 2 * RQ + 1;
@@ -325,10 +325,10 @@ __device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T>
         if (h < HP) {
             int fy, fx;
             if (h < RQ * PR) {                      // top strip
-                fy = h / PR; fx = 2 * (h % PR);
+                fy = h / PR; fx = RQ + 2 * (h % PR);
             } else if (h < 2 * RQ * PR) {           // bottom strip
                 const int hh = h - RQ * PR;
-                fy = RQ + TY + hh / PR; fx = 2 * (hh % PR);
+                fy = RQ + TY + hh / PR; fx = RQ + 2 * (hh % PR);
             } else {                                // left / right strips
                 const int hh = h - 2 * RQ * PR;
                 const int row = hh / RQ, c = hh % RQ;

@@ -149,22 +149,37 @@ static int tune_t(const lsg_operator *op, cudaStream_t s, TuneEntry *out, int *n
             }
         }
     }
-    // the paired march (tile code kTilePaired) of the FP32 recurrence pass
+    // the paired march of the FP32 recurrence pass in its two shapes (tile
+    // codes kTilePaired, kTilePaired2) x the same kinds of z depth
     int plz = 0;
     if (rc == LSG_OK && Kernels<T>::paired_plan(g, &plz) > 0 && std::is_same<T, float>::value &&
         g.nx % 2 == 0) {
-        StencilLaunch L{g, plz, s, 0};
-        L.paired = 1;
-        float ms = 0.f;
-        rc = time_rich<T>(L, w, v, n, ctrl, e0, e1, &ms);
-        if (rc == LSG_OK) {
-            count++;
-            const double us = 1000.0 * ms;
-            best.us_default = us;  // the untuned solve runs the paired march
-            if (us < best.us) {
-                best.us = us;
-                best.tile = kTilePaired;
-                best.lz = plz;
+        for (int shape = 1; shape <= 2 && rc == LSG_OK; shape++) {
+            const int rows = shape == 1 ? kPairBY * kPairNY : kPair2BY * kPair2NY;
+            const int slots = sms * Kernels<T>::paired_blocks_per_sm(shape);
+            const long long bxy = (long long)((g.nx + 63) / 64) * ((g.ny + rows - 1) / rows);
+            const long long chunks = std::max<long long>(1, bxy >= slots ? 1 : slots / bxy);
+            const int lz1 = std::max(8, std::min(g.nz, (int)((g.nz + chunks - 1) / chunks)));
+            std::vector<int> cands{lz1, std::max(8, lz1 / 2), std::min(g.nz, 2 * lz1), g.nz,
+                                   balanced_lz(g, rows, slots, FillCost<T>::value, 64)};
+            if (shape == 1) cands.push_back(plz);
+            std::sort(cands.begin(), cands.end());
+            cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
+            for (int lz : cands) {
+                if (lz < 1 || lz > g.nz) continue;
+                StencilLaunch L{g, lz, s, 0};
+                L.paired = shape;
+                float ms = 0.f;
+                rc = time_rich<T>(L, w, v, n, ctrl, e0, e1, &ms);
+                if (rc != LSG_OK) break;
+                count++;
+                const double us = 1000.0 * ms;
+                if (shape == 1 && lz == plz) best.us_default = us;  // the untuned solve runs this one
+                if (us < best.us) {
+                    best.us = us;
+                    best.tile = shape == 1 ? kTilePaired : kTilePaired2;
+                    best.lz = lz;
+                }
             }
         }
     }
@@ -209,9 +224,9 @@ StencilLaunch rich_launch(const lsg_operator *op, const StencilLaunch &L) {
         }
     }
     StencilLaunch r = L;
-    if (e.tile == kTilePaired) {
+    if (e.tile == kTilePaired || e.tile == kTilePaired2) {
         r.tile = 0;
-        r.paired = 1;
+        r.paired = e.tile == kTilePaired ? 1 : 2;
     } else {
         r.tile = e.tile;
         r.paired = 0;  // a tuned classic shape
@@ -253,7 +268,9 @@ int tune_load(const char *path, int *count) {
         double us, usd;
         if (sscanf(line, "%d %d %d %d %d %d %d %lf %lf", &dev, &dt, &nx, &ny, &nz, &tile, &lz, &us, &usd) != 9)
             continue;
-        if (tile < 0 || (tile >= kTileVariants && tile != kTilePaired) || lz < 1 || lz > nz) continue;
+        if (tile < 0 || (tile >= kTileVariants && tile != kTilePaired && tile != kTilePaired2) || lz < 1 ||
+            lz > nz)
+            continue;
         g_tune[TuneKey{dev, dt, nx, ny, nz}] = TuneEntry{tile, lz, us, usd};
         loaded++;
     }
@@ -278,6 +295,11 @@ int lsg_autotune(const lsg_operator *op, int dtype, lsg_tune_info *info, void *s
             if (e.tile == lsg::kTilePaired) {  // 32 x 8 threads, 2 rows x 2 columns each
                 by = lsg::kPairBY;
                 ny = lsg::kPairNY;
+                return;
+            }
+            if (e.tile == lsg::kTilePaired2) {  // 32 x 4 threads, 2 rows x 2 columns each
+                by = lsg::kPair2BY;
+                ny = lsg::kPair2NY;
                 return;
             }
             switch (e.tile) {
