@@ -546,6 +546,140 @@ __global__ void __launch_bounds__(kReduceThreads) gram_kernel(const T *__restric
     gram_block<T, KIND, M, true>(dx, df, r, n, partials + (long long)blockIdx.x * NV, blockIdx.x, gridDim.x);
 }
 
+// ---- Gram by bulk copies (FP32, symmetric kind, m <= 8).  The history
+// streams through a ring of kGramStages shared-memory stages; one thread arms
+// each stage's mbarrier with the byte count and issues one bulk copy
+// (cp.async.bulk) per column, so the loads of the next stages are in flight
+// while the block reduces the current one and no warp stalls on a global
+// load.  A stage holds one float4 per thread of every column (a 1024-float
+// chunk); block b takes chunks b, b + G, ..., so each thread visits the same
+// points in the same order as gram_block's grid-stride loop and the sums are
+// bit-identical to it.  Every wait is bounded: a copy that has not landed
+// after ~2 s sets LSG_TIMEOUT in the control block, the block waits (again
+// bounded) for its own copies in flight and returns.
+constexpr int kGramStages = 3;
+constexpr int kGramChunk = 4 * kReduceThreads;  // floats per column per stage
+constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *b, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *b) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(b))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *b, unsigned phase) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *b, unsigned phase) {
+    if (mbar_try_wait(b, phase)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(b, phase))
+        if (clock64() - t0 > kWaitCycles) return false;
+    return true;
+}
+
+template <int M>
+__global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const float *__restrict__ df,
+                                                                     const float *__restrict__ r, long long n,
+                                                                     double *partials, DevCtrl *ctrl) {
+    constexpr int NP = (M * (M + 1)) / 2;
+    constexpr int NV = NP + M;
+    constexpr int S = kGramStages, CH = kGramChunk, CV = CH / 4;
+    extern __shared__ __align__(128) float gsm[];  // S stages x (M + 1) columns x CH floats
+    __shared__ __align__(8) unsigned long long full[S];
+    __shared__ double red[NV * (kReduceThreads / 32)];
+    __shared__ int abort_flag;
+    if (solve_done(ctrl)) return;
+    const int tid = threadIdx.x;
+    const long long nchunk = (n + CH - 1) / CH;
+    const long long first = blockIdx.x, step = gridDim.x;
+    const long long mine = first < nchunk ? (nchunk - 1 - first) / step + 1 : 0;
+    if (tid == 0) {
+        for (int st = 0; st < S; st++) mbar_init(&full[st], 1);
+        abort_flag = 0;
+        mbar_init_fence();
+    }
+    __syncthreads();
+    auto issue = [&](long long k) {  // the block's k-th chunk into stage k % S (thread 0)
+        const long long off = (first + k * step) * CH;
+        const unsigned bytes = (unsigned)(min((long long)CH, n - off) * 4);
+        unsigned long long *bar = &full[k % S];
+        float *dst = gsm + (size_t)(k % S) * (M + 1) * CH;
+        mbar_expect_tx(bar, bytes * (M + 1));
+#pragma unroll
+        for (int v = 0; v < M; v++) bulk_g2s(dst + v * CH, df + (long long)v * n + off, bytes, bar);
+        bulk_g2s(dst + M * CH, r + off, bytes, bar);
+    };
+    if (tid == 0)
+        for (long long k = 0; k < S && k < mine; k++) issue(k);
+    Acc<float> acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) acc[k].zero();
+    long long k = 0;
+    for (; k < mine; k++) {
+        const int st = (int)(k % S);
+        if (!mbar_wait_bounded(&full[st], (unsigned)((k / S) & 1))) {
+            abort_flag = 1;
+        } else {
+            const long long off = (first + k * step) * CH;
+            if (off + 4 * tid < n) {
+                const float4 *src = reinterpret_cast<const float4 *>(gsm + (size_t)st * (M + 1) * CH);
+                float4 f[M];
+#pragma unroll
+                for (int v = 0; v < M; v++) f[v] = src[v * CV + tid];
+                const float4 rv = src[M * CV + tid];
+                int q = 0;
+#pragma unroll
+                for (int j = 0; j < M; j++)
+#pragma unroll
+                    for (int a = 0; a <= j; a++) { accv(acc[q], f[a], f[j]); q++; }
+#pragma unroll
+                for (int j = 0; j < M; j++) accv(acc[NP + j], f[j], rv);
+            }
+        }
+        __syncthreads();  // stage st is free again (and abort_flag is seen by all)
+        if (abort_flag) break;
+        if (tid == 0 && k + S < mine) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(k + S);
+        }
+    }
+    if (abort_flag) {
+        if (tid == 0) {
+            for (long long kk = k; kk < k + S && kk < mine; kk++)
+                mbar_wait_bounded(&full[kk % S], (unsigned)((kk / S) & 1));
+            if (ctrl) {
+                ctrl->status = LSG_TIMEOUT;
+                ctrl->done = 1;
+            }
+        }
+        return;
+    }
+    block_reduce_store<NV>(acc, red, partials + (long long)blockIdx.x * NV);
+}
+
+template <int M>
+static size_t gram_bulk_smem() {
+    return (size_t)kGramStages * (M + 1) * kGramChunk * sizeof(float);
+}
+
 // Generic Gram (any m <= LSG_MAX_M): one value per (block, thread-slot), the
 // history columns re-read per value from L2.  Used only for m > 8.
 template <typename T>
@@ -917,6 +1051,29 @@ static cudaError_t gram_dispatch(int m, const T *dx, const T *df, const T *r, lo
                                  double *partials, int blocks, const DevCtrl *ctrl,
                                  cudaStream_t s) {
     const int vn = Vec4<T>::N;
+    if constexpr (std::is_same<T, float>::value && KIND == GRAM_SYM) {
+        // the bulk-copy form: 16-byte aligned columns and residual, n % 4 == 0
+        if (n % 4 == 0 && m >= 1 && m <= 8 && (((uintptr_t)df | (uintptr_t)r) & 15u) == 0) {
+            DevCtrl *c = const_cast<DevCtrl *>(ctrl);
+            switch (m) {
+#define LSG_GRAM_BULK(MM)                                                                                     \
+    case MM: {                                                                                                \
+        static bool attr = false;                                                                             \
+        if (!attr) {                                                                                          \
+            cudaFuncSetAttribute(gram_bulk_kernel<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize,           \
+                                 (int)gram_bulk_smem<MM>());                                                  \
+            attr = true;                                                                                      \
+        }                                                                                                     \
+        gram_bulk_kernel<MM><<<blocks, kReduceThreads, gram_bulk_smem<MM>(), s>>>(df, r, n, partials, c);     \
+        return cudaGetLastError();                                                                            \
+    }
+                LSG_GRAM_BULK(1) LSG_GRAM_BULK(2) LSG_GRAM_BULK(3) LSG_GRAM_BULK(4)
+                LSG_GRAM_BULK(5) LSG_GRAM_BULK(6) LSG_GRAM_BULK(7) LSG_GRAM_BULK(8)
+#undef LSG_GRAM_BULK
+            default: break;
+            }
+        }
+    }
     switch (n % vn == 0 ? m : 0) {
 #define LSG_GRAM_CASE(MM) \
     case MM: gram_kernel<T, KIND, MM><<<blocks, kReduceThreads, 0, s>>>(dx, df, r, n, partials, ctrl); break;
