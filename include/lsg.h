@@ -69,7 +69,7 @@ typedef struct lsg_params {
     int max_iter;        /* iteration limit (inner limit for the mixed solver) */
     double tol;          /* stop when ||b - A x|| <= tol * ||b|| */
     /* mixed precision (lsg_aar_mixed) */
-    double inner_tol;    /* FP32 residual reduction between FP64 residual replacements (0 = 3e-2) */
+    double inner_tol;    /* FP32 residual reduction between FP64 residual replacements (0 = 3e-4) */
     int max_outer;       /* FP64 residual replacements (0 = 50) */
     /* execution */
     int check_every;     /* extrapolation cycles enqueued between convergence reads (0 = auto) */

@@ -551,7 +551,7 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
     const int var = generic ? 0 : ws->tvar;
     const double lscale = generic ? 1.0 : ws->tscale;
     const int slots = sm_count() * BatchKernels<T>::stencil_blocks_per_sm(generic, var);
-    BatchRun<T> B{ws, prm, mixed, generic, prm->inner_tol > 0 ? prm->inner_tol : 3e-2,
+    BatchRun<T> B{ws, prm, mixed, generic, prm->inner_tol > 0 ? prm->inner_tol : 3e-4,
                   prm->max_outer > 0 ? prm->max_outer : 50, BPlan(), 0};
     make_plan<T>(ws, geo, act, generic, var, slots, lscale, &B.plan);
     rc = upload_tables<T>(ws, B.plan);

@@ -824,7 +824,7 @@ int solve_mixed_t(const lsg_operator *op, const lsg_params *prm, T64 *x, const T
     DevCtrl *octrl = wo->ctrl;
     double *opart = wo->partials;
     const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
-    const double rho = prm->inner_tol > 0 ? prm->inner_tol : 3e-2;
+    const double rho = prm->inner_tol > 0 ? prm->inner_tol : 3e-4;
     T32 *e32 = (T32 *)wo->e32;
     AarLoop<T32> A(R, op, prm, e32, nullptr, wi);
 
@@ -1161,7 +1161,7 @@ void lsg_params_default(lsg_params *prm) {
     prm->p = 6;
     prm->max_iter = 100000;
     prm->tol = 1e-8;
-    prm->inner_tol = 3e-2;
+    prm->inner_tol = 3e-4;
     prm->max_outer = 50;
 }
 

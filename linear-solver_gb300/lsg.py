@@ -221,7 +221,7 @@ class Operator:
         return [self._s.coeff[i] for i in range(self.radius + 1)]
 
 
-def _params(omega=0.6, beta=0.6, m=7, p=6, max_iter=100000, tol=1e-8, inner_tol=3e-2,
+def _params(omega=0.6, beta=0.6, m=7, p=6, max_iter=100000, tol=1e-8, inner_tol=3e-4,
             max_outer=50, check_every=0) -> _Params:
     prm = _Params()
     lib().lsg_params_default(C.byref(prm))
