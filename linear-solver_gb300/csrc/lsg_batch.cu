@@ -68,7 +68,7 @@ struct BatchWs {
     DevCtrl *d_ctrl = nullptr, *h_ctrl = nullptr;  // 2 per instance: ctrl, octrl
     size_t clk_bytes = 0;
     long long smap_cap = 0, umap_cap = 0;
-    std::vector<char *> vec;      // per instance: xalt r0 r1 dx[m] df[m] (e)
+    std::vector<char *> vec;      // per instance: xalt r0 r1 dx[m] df[m] (e) (FP32: rs)
     std::vector<double *> part;
     std::vector<long long> part_cap;
     int tuned = 0;               // 1: tile variant and z-depth scale measured for this batch
@@ -141,7 +141,7 @@ static int batch_ws_get(const std::vector<Geom> &geo, int m, bool mixed, bool ge
     const long long nvmax = (long long)(m * (m + 1)) / 2 + m;
     const long long ucap = (long long)kUcapPerSm * sms;
     const size_t es = sizeof(T);
-    const int nvec = 3 + 2 * m + (mixed ? 1 : 0);
+    const int nvec = 3 + 2 * m + (mixed ? 1 : 0) + (IsRecur<T>::value ? 1 : 0);
     size_t bytes = 0;
     std::vector<size_t> o_vec(count), o_part(count);
     ws->part_cap.resize(count);
@@ -314,6 +314,7 @@ struct BatchRun {
     int max_outer;
     BPlan plan;
     long long launches = 0;
+    bool deflating = false;  // mixed: some instance has a non-zero shift
 
     BArgs args(const int *map, int k, int gate = 0) const {
         BArgs a;
@@ -326,6 +327,7 @@ struct BatchRun {
         a.max_iter = prm->max_iter;
         a.beta = prm->beta;
         a.gate = gate;
+        a.lean = IsRecur<T>::value && prm->p - 1 <= prm->m;
         return a;
     }
     const BInst<T> *tab() const { return (const BInst<T> *)ws->d_inst; }
@@ -344,7 +346,13 @@ struct BatchRun {
     int refine(int k, int gate) {
         cudaStream_t s = ws->stream;
         const int W = AccWidth<T>::value;
+        if (gate == 1) LSG_BL(BatchKernels<T>::fold(tab(), args(ws->d_umap, k, 1), plan.ugrid, s));
         LSG_BL(BatchKernels<T>::ir_correct(tab(), args(ws->d_umap, k, gate), plan.ugrid, s));
+        if (deflating) {
+            LSG_BL(BatchKernels<T>::mean_deflate(tab(), args(ws->d_umap, k, gate), plan.ugrid, args(nullptr, k, gate),
+                                                 ws->d_amap, nact(), 1, s));
+            launches += 2;
+        }
         LSG_BL(BatchKernels<T>::ir_residual(tab(), args(ws->d_smap, k, gate), plan.sgrid, generic, plan.var, s));
         LSG_BL(batch_finalize_norm(args(nullptr, k, gate), ws->d_amap, nact(), BF_REPLACE, prm->tol, W, s));
         if (gate == 0) LSG_BL(batch_resume(args(nullptr, k, 0), ws->d_amap, nact(), rho, max_outer, s));
@@ -489,6 +497,7 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
     const size_t es = sizeof(T);
     // Instance records.
     BInst<T> *hi = (BInst<T> *)ws->h_inst;
+    bool deflating = false;
     for (int i = 0; i < count; i++) {
         BInst<T> &I = hi[i];
         memset((void *)&I, 0, sizeof(I));
@@ -507,6 +516,7 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
         I.r1 = (T *)(v + 2 * vb);
         I.dx = (T *)(v + 3 * vb);
         I.df = (T *)(v + (3 + m) * vb);
+        if (IsRecur<T>::value) I.rs = (T *)(v + (3 + 2 * m + (mixed ? 1 : 0)) * vb);
         if (mixed) {
             I.x = (T *)(v + (3 + 2 * m) * vb);
             I.b = nullptr;
@@ -528,6 +538,9 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
         } else {
             C.hre = cf;
         }
+        C.sig_re = ops[i].sigma;
+        C.sig_im = IsCplx<T>::value ? ops[i].sigma_im : 0.0;
+        if (mixed && (C.sig_re != 0.0 || C.sig_im != 0.0)) deflating = true;
         ws->h_ctrl[2 * i] = ctrl_init(prm->tol, mixed ? 12 : 0);
         ws->h_ctrl[2 * i + 1] = ctrl_init(prm->tol, 0);
         if (mixed) ws->h_ctrl[2 * i].done = 1;  // opens the first refinement pass
@@ -553,6 +566,7 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
     const int slots = sm_count() * BatchKernels<T>::stencil_blocks_per_sm(generic, var);
     BatchRun<T> B{ws, prm, mixed, generic, prm->inner_tol > 0 ? prm->inner_tol : 3e-4,
                   prm->max_outer > 0 ? prm->max_outer : 50, BPlan(), 0};
+    B.deflating = deflating;
     make_plan<T>(ws, geo, act, generic, var, slots, lscale, &B.plan);
     rc = upload_tables<T>(ws, B.plan);
     if (rc) return rc;
@@ -566,6 +580,12 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
                                     AccWidth<TW>::value, s);
             if (e != cudaSuccess) return set_error(LSG_CUDA_ERROR, "batched rhs norm: %s", cudaGetErrorString(e));
             B.launches += 2;
+            if (B.deflating) {  // mean(b64) of the instances with a shift
+                e = BatchKernels<T>::mean_deflate(B.tab(), B.args(ws->d_umap, -1), B.plan.ugrid, B.args(nullptr, -1),
+                                                  ws->d_amap, B.nact(), 0, s);
+                if (e != cudaSuccess) return set_error(LSG_CUDA_ERROR, "batched rhs mean: %s", cudaGetErrorString(e));
+                B.launches += 2;
+            }
         }
         rc = B.refine(-1, 0);
         if (rc) return rc;
@@ -642,6 +662,12 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
         // take their true residual after the last iteration
         rc = B.refine(prm->max_iter - it0 - 1, 1);
         if (rc) return rc;
+    } else if (it0 >= prm->max_iter) {
+        // a lean batch stopped between extrapolations: add the cycle's steps to x
+        const cudaError_t e = BatchKernels<T>::fold(B.tab(), B.args(ws->d_umap, prm->max_iter - it0 - 1, 1),
+                                                    B.plan.ugrid, s);
+        if (e != cudaSuccess) return set_error(LSG_CUDA_ERROR, "batched fold: %s", cudaGetErrorString(e));
+        B.launches++;
     }
     LSG_BCUDA(cudaMemcpyAsync(ws->h_ctrl, ws->d_ctrl, sizeof(DevCtrl) * 2 * count, cudaMemcpyDeviceToHost, s));
     LSG_BCUDA(cudaStreamSynchronize(s));

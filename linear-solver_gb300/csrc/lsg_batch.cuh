@@ -19,9 +19,21 @@ __device__ __forceinline__ int batch_iter(const BArgs &a) { return a.clk->it0 + 
 
 template <typename T>
 __device__ __forceinline__ T *rbuf(const BInst<T> &I, int par) { return par ? I.r1 : I.r0; }
-
 template <typename T>
-struct IsRecur { static constexpr bool value = std::is_same<typename RealOf<T>::type, float>::value; };
+__device__ __forceinline__ T *rbuf3(const BInst<T> &I, int k) { return k == 0 ? I.r0 : (k == 1 ? I.r1 : I.rs); }
+
+// The residual after iterations 1..last: the ping-pong buffer, or (lean) the
+// rotating one.
+template <typename T>
+__device__ __forceinline__ T *rcur(const BInst<T> &I, const BArgs &a, int last) {
+    if (a.lean) {
+        int s, c;
+        lean_buffers(last, a.p, &s, &c);
+        return rbuf3(I, c);
+    }
+    return rbuf(I, richardson_parity(last, a.p));
+}
+
 
 // Refinement passes act on instances whose FP32 iteration paused (gate 0), or
 // on every unfinished one (gate 1, the final pass after max_iter).
@@ -45,6 +57,24 @@ struct PassRichRecur {  // AAR.c:93-107,134-139 in residual-recurrence form
         const int rc = richardson_parity(it - 1, a.p);
         const long long off = (long long)((it - 1) % a.m) * I.g.n;
         op = Op{rbuf(I, rc), I.x, rbuf(I, rc ^ 1), I.dx + off, I.df + off, I.c, I.cf, T(a.beta), nullptr, C.ctrl};
+        return true;
+    }
+    __device__ static Weights<TS> weights(const BInst<T> &I) { return I.w; }
+};
+
+template <typename T>
+struct PassRichLean {  // the same step with x left out (rebuilt at the extrapolation)
+    using TS = T;
+    using Op = RichLeanOp<T>;
+    static constexpr int MINB = 0;  // the tile variant's
+    __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &a, Op &op) {
+        const int it = batch_iter(a);
+        if (it > a.max_iter) return false;
+        int s, c;
+        lean_buffers(it - 1, a.p, &s, &c);
+        const long long off = (long long)((it - 1) % a.m) * I.g.n;
+        op = Op{rbuf3(I, c), rbuf3(I, lean_target(s, c)), I.dx + off, I.df + off, I.c, I.cf, T(a.beta), nullptr,
+                C.ctrl};
         return true;
     }
     __device__ static Weights<TS> weights(const BInst<T> &I) { return I.w; }
@@ -104,9 +134,8 @@ struct PassResRecur {  // AAR.c:116-123, residual recurrence on the step in xalt
     __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &a, Op &op) {
         const int it = batch_iter(a);
         if (it > a.max_iter) return false;
-        const int rc = richardson_parity(it - 1, a.p);
         const long long off = (long long)((it - 1) % a.m) * I.g.n;
-        op = Op{I.xalt, rbuf(I, rc), I.df + off, I.dx + off, I.cf, T(a.beta), C.part, C.ctrl};
+        op = Op{I.xalt, rcur(I, a, it - 1), I.df + off, I.dx + off, I.cf, T(a.beta), C.part, C.ctrl};
         return true;
     }
     __device__ static Weights<TS> weights(const BInst<T> &I) { return I.w; }
@@ -120,7 +149,7 @@ struct PassIrResidual {  // r = float(b64 - A x64) after iteration it (mixed sol
     __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &a, Op &op) {
         if (!replace_gate(C, a)) return false;
         const int it = batch_iter(a);
-        op = Op{I.x64, I.b64, rbuf(I, richardson_parity(it, a.p)), C.part, nullptr};
+        op = Op{I.x64, I.b64, rcur(I, a, it), C.part, nullptr};
         return true;
     }
     __device__ static Weights<TS> weights(const BInst<T> &I) { return I.w64; }
@@ -188,7 +217,7 @@ __global__ void __launch_bounds__(kReduceThreads) batch_gram_kernel(const BInst<
     const int it = batch_iter(a);
     if (it > a.max_iter || solve_done(C.ctrl)) return;
     const BInst<T> &I = tab[i];
-    const T *r = rbuf(I, richardson_parity(it - 1, a.p));
+    const T *r = rcur(I, a, it - 1);
     const long long lb = blockIdx.x - C.ublk0;
     if constexpr (IsCplx<T>::value) {
         gram_c_block<typename RealOf<T>::type, M>(I.df, r, I.g.n, C.part + lb * 2 * NV, lb, C.ublocks);
@@ -205,6 +234,24 @@ __global__ void __launch_bounds__(kReduceThreads) batch_update_kernel(const BIns
     const int it = batch_iter(a);
     if (it > a.max_iter || solve_done(C.ctrl)) return;
     const BInst<T> &I = tab[i];
+    const long long lb = blockIdx.x - C.ublk0;
+    if constexpr (IsRecur<T>::value) {
+        if (a.lean) {  // x: the cycle-start iterate, rebuilt from the cycle's H columns
+            int s, c;
+            lean_buffers(it - 1, a.p, &s, &c);
+            const unsigned mask = lean_mask(it - 1, a.p, a.m);
+            if constexpr (!IsCplx<T>::value) {
+                if (I.vec) {
+                    aar_update_block<T, M, true, true>(a.m, I.x, rbuf3(I, c), I.dx, I.xalt, T(a.beta), I.cf, I.g.n,
+                                                       C.ctrl, lb, C.ublocks, rbuf3(I, s), mask);
+                    return;
+                }
+            }
+            aar_update_block<T, M, false, true>(a.m, I.x, rbuf3(I, c), I.dx, I.xalt, T(a.beta), I.cf, I.g.n, C.ctrl,
+                                                lb, C.ublocks, rbuf3(I, s), mask);
+            return;
+        }
+    }
     const int rc = richardson_parity(it - 1, a.p);
     T *x, *step;
     if (IsRecur<T>::value) {
@@ -214,7 +261,6 @@ __global__ void __launch_bounds__(kReduceThreads) batch_update_kernel(const BIns
         x = rc ? I.xalt : I.x;
         step = I.dx + (long long)((it - 1) % a.m) * I.g.n;  // completed by the residual pass
     }
-    const long long lb = blockIdx.x - C.ublk0;
     if constexpr (!IsCplx<T>::value) {
         if (I.vec) {
             aar_update_block<T, M, true>(a.m, x, rbuf(I, rc), I.dx, step, T(a.beta), I.cf, I.g.n, C.ctrl, lb,
@@ -224,6 +270,110 @@ __global__ void __launch_bounds__(kReduceThreads) batch_update_kernel(const BIns
     }
     aar_update_block<T, M, false>(a.m, x, rbuf(I, rc), I.dx, step, T(a.beta), I.cf, I.g.n, C.ctrl, lb,
                                   C.ublocks);
+}
+
+// x += sum_mask H_j - beta cf (r - r_start) of instances still iterating at
+// iteration it (a lean batch stopped by max_iter between extrapolations).
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) batch_fold_kernel(const BInst<T> *tab, BArgs a) {
+    const int i = a.map[blockIdx.x];
+    const BCtl &C = a.ctl[i];
+    if (solve_done(C.ctrl) || solve_done(C.octrl)) return;
+    const int it = batch_iter(a);
+    const unsigned mask = lean_mask(it, a.p, a.m);
+    if (mask == 0u) return;
+    const BInst<T> &I = tab[i];
+    int s, c;
+    lean_buffers(it, a.p, &s, &c);
+    const T *r = rbuf3(I, c), *rs = rbuf3(I, s);
+    const long long n = I.g.n;
+    const long long lb = blockIdx.x - C.ublk0;
+    const long long stride = (long long)C.ublocks * blockDim.x;
+    for (long long j = lb * blockDim.x + threadIdx.x; j < n; j += stride) {
+        T ac = T(0);
+        for (int q = 0; q < a.m; q++)
+            if ((mask >> q) & 1u) ac = ac + ldg(I.dx + (long long)q * n + j);
+        I.x[j] = I.x[j] + (ac - T(a.beta) * ((r[j] - rs[j]) * I.cf));
+    }
+}
+
+// Constant-mode deflation of mixed batches: instances with a non-zero shift;
+// which 1 only those being refined (the refinement passes' gate).
+__device__ __forceinline__ bool deflate_gate(const BCtl &C, const BArgs &a, int which) {
+    if (!(C.sig_re != 0.0 || C.sig_im != 0.0)) return false;
+    return which == 0 || replace_gate(C, a);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) batch_mean_sum_kernel(const BInst<T> *tab, BArgs a, int which) {
+    using TW = typename WideOf<T>::type;
+    __shared__ double red[2 * (kReduceThreads / 32)];
+    const int i = a.map[blockIdx.x];
+    const BCtl &C = a.ctl[i];
+    if (!deflate_gate(C, a, which)) return;
+    const BInst<T> &I = tab[i];
+    const TW *v = which ? I.x64 : I.b64;
+    double re = 0.0, im = 0.0;
+    const long long lb = blockIdx.x - C.ublk0;
+    const long long stride = (long long)C.ublocks * blockDim.x;
+    for (long long j = lb * blockDim.x + threadIdx.x; j < I.g.n; j += stride) {
+        if constexpr (IsCplx<TW>::value) {
+            const TW u = v[j];
+            re += u.x;
+            im += u.y;
+        } else {
+            re += v[j];
+        }
+    }
+    Acc<double> acc[2];
+    acc[0].v = re;
+    acc[1].v = im;
+    block_reduce_store<2>(acc, red, C.part + 2 * lb);
+}
+
+// One block per active instance: the mean from its ublocks partials into
+// octrl->bmean (which 0) or octrl->shift = bmean / sigma - mean (which 1).
+static __global__ void batch_mean_finalize_kernel(BArgs a, const int *amap, int which) {
+    __shared__ double red[2 * (kReduceThreads / 32)];
+    __shared__ double out[2];
+    const BCtl &C = a.ctl[amap[blockIdx.x]];
+    if (!deflate_gate(C, a, which)) return;
+    double re = 0.0, im = 0.0;
+    for (int k = threadIdx.x; k < C.ublocks; k += blockDim.x) {
+        re += C.part[2 * k];
+        im += C.part[2 * k + 1];
+    }
+    Acc<double> acc[2];
+    acc[0].v = re;
+    acc[1].v = im;
+    block_reduce_store<2>(acc, red, out);
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const double mr = out[0] / (double)C.n, mi = out[1] / (double)C.n;
+    DevCtrl *o = C.octrl;
+    if (which == 0) {
+        o->bmean[0] = mr;
+        o->bmean[1] = mi;
+    } else {
+        const double sr = C.sig_re, si = C.sig_im, d = sr * sr + si * si;
+        o->shift[0] = (o->bmean[0] * sr + o->bmean[1] * si) / d - mr;
+        o->shift[1] = (o->bmean[1] * sr - o->bmean[0] * si) / d - mi;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) batch_shift_kernel(const BInst<T> *tab, BArgs a) {
+    using TW = typename WideOf<T>::type;
+    const int i = a.map[blockIdx.x];
+    const BCtl &C = a.ctl[i];
+    if (!deflate_gate(C, a, 1)) return;
+    const BInst<T> &I = tab[i];
+    TW c;
+    if constexpr (IsCplx<TW>::value) c = TW(C.octrl->shift[0], C.octrl->shift[1]);
+    else c = C.octrl->shift[0];
+    const long long lb = blockIdx.x - C.ublk0;
+    const long long stride = (long long)C.ublocks * blockDim.x;
+    for (long long j = lb * blockDim.x + threadIdx.x; j < I.g.n; j += stride) I.x64[j] = I.x64[j] + c;
 }
 
 template <typename T, bool WIDE>
@@ -276,7 +426,7 @@ int BatchKernels<T>::tile_y(bool generic, int var) {
 
 template <typename T, int V, bool GENERIC>
 static int batch_rich_occupancy() {
-    using P = typename std::conditional<IsRecur<T>::value, PassRichRecur<T>, PassRich<T>>::type;
+    using P = typename std::conditional<IsRecur<T>::value, PassRichLean<T>, PassRich<T>>::type;
     using Tl = BTile<T, V, GENERIC>;
     int n = 0;
     const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -300,8 +450,24 @@ int BatchKernels<T>::stencil_blocks_per_sm(bool generic, int var) {
 template <typename T>
 cudaError_t BatchKernels<T>::richardson(const BInst<T> *tab, const BArgs &a, int grid, bool generic, int var,
                                         cudaStream_t s) {
-    if constexpr (IsRecur<T>::value) return launch_batch_stencil<T, PassRichRecur<T>>(tab, a, grid, generic, var, s);
-    else return launch_batch_stencil<T, PassRich<T>>(tab, a, grid, generic, var, s);
+    if constexpr (IsRecur<T>::value) {
+        if (a.lean) return launch_batch_stencil<T, PassRichLean<T>>(tab, a, grid, generic, var, s);
+        return launch_batch_stencil<T, PassRichRecur<T>>(tab, a, grid, generic, var, s);
+    } else {
+        return launch_batch_stencil<T, PassRich<T>>(tab, a, grid, generic, var, s);
+    }
+}
+
+template <typename T>
+cudaError_t BatchKernels<T>::fold(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s) {
+    if (grid <= 0) return cudaSuccess;
+    if constexpr (IsRecur<T>::value) {
+        if (!a.lean) return cudaSuccess;
+        batch_fold_kernel<T><<<grid, kReduceThreads, 0, s>>>(tab, a);
+        return cudaGetLastError();
+    } else {
+        return cudaSuccess;
+    }
 }
 
 template <typename T>
@@ -355,6 +521,21 @@ cudaError_t BatchKernels<T>::norm2_rhs(const BInst<T> *tab, const BArgs &a, int 
     if (wide) batch_norm2_kernel<T, true><<<grid, kReduceThreads, 0, s>>>(tab, a);
     else batch_norm2_kernel<T, false><<<grid, kReduceThreads, 0, s>>>(tab, a);
     return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t BatchKernels<T>::mean_deflate(const BInst<T> *tab, const BArgs &au, int ugrid, const BArgs &aa,
+                                          const int *amap, int nact, int which, cudaStream_t s) {
+    if (ugrid <= 0 || nact <= 0) return cudaSuccess;
+    if constexpr (IsRecur<T>::value) {
+        batch_mean_sum_kernel<T><<<ugrid, kReduceThreads, 0, s>>>(tab, au, which);
+        batch_mean_finalize_kernel<<<nact, kReduceThreads, 0, s>>>(aa, amap, which);
+        if (which == 1) batch_shift_kernel<T><<<ugrid, kReduceThreads, 0, s>>>(tab, au);
+        return cudaGetLastError();
+    } else {
+        (void)tab, (void)au, (void)aa, (void)amap, (void)which, (void)s;
+        return cudaErrorInvalidValue;
+    }
 }
 
 template <typename T>

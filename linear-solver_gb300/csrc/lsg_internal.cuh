@@ -37,8 +37,39 @@ struct DevCtrl {
     int stall_limit;  // 0: off; else stop (done, stalled = 1) after this many checks
     int stalled;      // set when the stall rule ended the solve
     int svd_fallbacks;  // extrapolation steps whose Gram needed the Jacobi SVD
+    double tol_frac;  // mixed solves (outer block): the next run's floor, as a fraction of tol_abs
+    int floor_misses; // mixed solves (outer block): consecutive runs that reached the floor, true residual > tol
+    double bmean[2];  // mixed solves (outer block): mean of b (re, im)
+    double shift[2];  // mixed solves (outer block): constant added to x64 by the last deflation
     double s[LSG_MAX_M];  // m x m solve output
 };
+
+// Mixed solves: the residual the next FP32 run stops at (absolute), from the
+// true residual after a replacement and the FP32 residual the previous run
+// paused at: a reduction rho, floored at tol_frac * tol_abs (tol_frac
+// starting at 1).  The FP32 recurrence drifts from the true residual, so a
+// run that reaches the tol floor can leave the true residual just above tol.
+// One such miss is normal (the next run restarts from the exact residual and
+// usually lands below tol); after two in a row the floor drops by the
+// observed drift, with a factor 2 margin, instead of repeating itself.
+// tol_frac and the miss count are per solve (the outer control block), so
+// single and batched solves follow the same schedule.
+__host__ __device__ inline double next_target(double *tol_frac, int *misses, double rho, double true_res,
+                                              double fp32_res, double tol_abs, bool first) {
+    if (!(*tol_frac > 0.0)) *tol_frac = 1.0;
+    if (!first) {
+        if (fp32_res <= *tol_frac * tol_abs && true_res > tol_abs && true_res > 0.0) {
+            if (++*misses >= 2) {
+                *tol_frac *= 0.5 * fp32_res / true_res;
+                *misses = 0;
+            }
+        } else {
+            *misses = 0;
+        }
+    }
+    const double a = *tol_frac * tol_abs, b = rho * true_res;
+    return a > b ? a : b;
+}
 
 // Geometry of one periodic grid.
 struct Geom {
@@ -372,6 +403,18 @@ cudaError_t ir_residual(const StencilLaunch &L, const Weights<T64> &w, const T64
 // x64 += e32; e32 = 0
 template <typename T64, typename T32>
 cudaError_t ir_correct(T64 *x, T32 *e, long long n, cudaStream_t s);
+// Constant-mode deflation of mixed solves.  On the periodic grid the
+// operator maps the constant vector to sigma times itself (the FD Laplacian's
+// rows sum to zero), so the solution's mean is mean(b) / sigma exactly, and
+// that mode -- the slowest one when sigma is small -- decouples.
+// rhs_mean: ctrl->bmean = mean(b).  deflate_x: x += mean(b) / sigma -
+// mean(x) (shift kept in ctrl->shift); the residual b - A x then has zero
+// mean.  partials: >= 2 * reduce_blocks(n) doubles.
+template <typename T64>
+cudaError_t rhs_mean(const T64 *b, long long n, double *partials, DevCtrl *ctrl, cudaStream_t s);
+template <typename T64>
+cudaError_t deflate_x(T64 *x, long long n, double *partials, DevCtrl *ctrl, double sig_re, double sig_im,
+                      cudaStream_t s);
 
 // Finalize kernels (lsg_small.cu).
 enum NormFinal {
@@ -406,6 +449,10 @@ cudaError_t pinv_solve_dev(const double *A, const double *b, double *x, int m, i
 // fields of that instance's BCtl.  Finished instances are skipped through
 // their DevCtrl flags, exactly as single solves skip queued work.
 
+// FP32 vectors (real or complex) run AAR in residual-recurrence form.
+template <typename T>
+struct IsRecur { static constexpr bool value = std::is_same<typename RealOf<T>::type, float>::value; };
+
 template <typename T> struct WideOf { using type = T; };
 template <> struct WideOf<float> { using type = double; };
 template <> struct WideOf<cplx<float>> { using type = cplx<double>; };
@@ -415,6 +462,30 @@ template <> struct WideOf<cplx<float>> { using type = cplx<double>; };
 __host__ __device__ inline int richardson_parity(int last, int p) {
     if (last < 1) return 0;
     return (last - last / p + (p == 1 ? 1 : 0)) & 1;
+}
+
+// Lean FP32 AAR (Richardson passes leave x out): r rotates through three
+// buffers.  A Richardson pass writes the buffer that is neither the current
+// residual c nor the cycle-start residual s; the extrapolation residual is
+// computed in place and starts the next cycle (s = c).  The buffers after
+// iterations 1..last, in closed form: k complete cycles move s by
+// 1 + ((p - 2) & 1) each; inside a cycle the passes alternate s+1, s+2.
+__host__ __device__ inline void lean_buffers(int last, int p, int *s, int *c) {
+    if (last < 1) { *s = 0; *c = 0; return; }
+    if (p == 1) { *s = last == 1 ? 0 : 1; *c = 1; return; }  // iteration 1 is the only Richardson one
+    const int k = last / p, rem = last % p;
+    const int st = (int)(((long long)k * (1 + ((p - 2) & 1))) % 3);
+    *s = st;
+    *c = rem == 0 ? st : (st + 1 + ((rem - 1) & 1)) % 3;
+}
+// The buffer a Richardson pass writes, given s and c.
+__host__ __device__ inline int lean_target(int s, int c) { return s == c ? (s + 1) % 3 : 3 - s - c; }
+// History columns written by the Richardson passes since the last
+// extrapolation, up to iteration `last` (bit (k-1) % m for iteration k).
+__host__ __device__ inline unsigned lean_mask(int last, int p, int m) {
+    unsigned mask = 0;
+    for (int k = last; k >= 1 && !(k % p == 0 && k > 1); k--) mask |= 1u << ((k - 1) % m);
+    return mask;
 }
 
 struct BClock {
@@ -432,6 +503,7 @@ struct BCtl {
     int sblk0, sblocks;  // its share of the batched stencil launches
     int ublk0, ublocks;  // its share of the batched point-local launches
     double hre, him;     // scale of the Gram right-hand side (the Jacobi factor)
+    double sig_re, sig_im;  // the operator's shift (mixed solves deflate the constant mode when non-zero)
 };
 
 template <typename T>
@@ -443,6 +515,7 @@ struct BInst {
     Weights<typename WideOf<T>::type> w64;
     T cf, c;             // Jacobi factor, omega * cf
     T *x, *xalt, *r0, *r1, *dx, *df;
+    T *rs;               // lean FP32: the third residual buffer
     const T *b;
     typename WideOf<T>::type *x64;        // mixed: the FP64 iterate and rhs
     const typename WideOf<T>::type *b64;
@@ -456,6 +529,7 @@ struct BArgs {
     int m, p, max_iter;
     double beta;
     int gate;            // refinement passes: 0 = paused instances, 1 = every unfinished one
+    int lean;            // FP32: the Richardson passes leave x out (p - 1 <= m)
 };
 
 template <typename T>
@@ -464,6 +538,9 @@ struct BatchKernels {
     static int stencil_blocks_per_sm(bool generic, int var);
     // Tile height of the batched stencil passes in tile variant var.
     static int tile_y(bool generic, int var);
+    // A lean batch stopped at max_iter between extrapolations: x += the
+    // cycle's steps (unfinished instances; k as for the refinement passes).
+    static cudaError_t fold(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s);
     // Richardson iteration k of the cycle (residual-recurrence form for FP32
     // vectors, the reference form for FP64 ones).
     static cudaError_t richardson(const BInst<T> *tab, const BArgs &a, int grid, bool generic, int var,
@@ -483,6 +560,12 @@ struct BatchKernels {
                                    cudaStream_t s);
     // Mixed solves: x64 += e; e = 0.
     static cudaError_t ir_correct(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s);
+    // Constant-mode deflation of mixed batches (deflate_x for each instance
+    // with a non-zero shift): which 0 stores mean(b64); 1 shifts x64 of the
+    // instances being refined.  au: point-local map, aa + amap: one block per
+    // active instance.  Three launches.
+    static cudaError_t mean_deflate(const BInst<T> *tab, const BArgs &au, int ugrid, const BArgs &aa,
+                                    const int *amap, int nact, int which, cudaStream_t s);
 };
 
 // Batched finalize kernels (lsg_small.cu): one block per active instance.

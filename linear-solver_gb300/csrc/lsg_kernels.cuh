@@ -1260,6 +1260,84 @@ __global__ void ir_correct_kernel(T64 *__restrict__ x, T32 *__restrict__ e, long
     }
 }
 
+// ---- constant-mode deflation (mixed solves)
+template <typename T64>
+__global__ void __launch_bounds__(kReduceThreads) mean_sum_kernel(const T64 *__restrict__ v, long long n,
+                                                                  double *partials) {
+    __shared__ double red[2 * (kReduceThreads / 32)];
+    double re = 0.0, im = 0.0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if constexpr (IsCplx<T64>::value) {
+            const T64 u = v[i];
+            re += u.x;
+            im += u.y;
+        } else {
+            re += v[i];
+        }
+    }
+    Acc<double> acc[2];
+    acc[0].v = re;
+    acc[1].v = im;
+    block_reduce_store<2>(acc, red, partials + 2 * (long long)blockIdx.x);
+}
+
+// which 0: ctrl->bmean = the mean; 1: ctrl->shift = bmean / sigma - the mean
+static __global__ void mean_finalize_kernel(const double *partials, int nparts, long long n, DevCtrl *ctrl, int which,
+                                     double sr, double si) {
+    __shared__ double red[2 * (kReduceThreads / 32)];
+    double re = 0.0, im = 0.0;
+    for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
+        re += partials[2 * k];
+        im += partials[2 * k + 1];
+    }
+    Acc<double> acc[2];
+    acc[0].v = re;
+    acc[1].v = im;
+    __shared__ double out[2];
+    block_reduce_store<2>(acc, red, out);
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const double mr = out[0] / (double)n, mi = out[1] / (double)n;
+    if (which == 0) {
+        ctrl->bmean[0] = mr;
+        ctrl->bmean[1] = mi;
+    } else {
+        const double d = sr * sr + si * si;
+        const double br = ctrl->bmean[0], bi = ctrl->bmean[1];
+        ctrl->shift[0] = (br * sr + bi * si) / d - mr;
+        ctrl->shift[1] = (bi * sr - br * si) / d - mi;
+    }
+}
+
+template <typename T64>
+__global__ void __launch_bounds__(kReduceThreads) shift_kernel(T64 *__restrict__ x, long long n,
+                                                               const DevCtrl *ctrl) {
+    T64 c;
+    if constexpr (IsCplx<T64>::value) c = T64(ctrl->shift[0], ctrl->shift[1]);
+    else c = ctrl->shift[0];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) x[i] = x[i] + c;
+}
+
+template <typename T64>
+cudaError_t rhs_mean(const T64 *b, long long n, double *partials, DevCtrl *ctrl, cudaStream_t s) {
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 4);
+    mean_sum_kernel<T64><<<blocks, kReduceThreads, 0, s>>>(b, n, partials);
+    mean_finalize_kernel<<<1, kReduceThreads, 0, s>>>(partials, blocks, n, ctrl, 0, 0.0, 0.0);
+    return cudaGetLastError();
+}
+
+template <typename T64>
+cudaError_t deflate_x(T64 *x, long long n, double *partials, DevCtrl *ctrl, double sig_re, double sig_im,
+                      cudaStream_t s) {
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 4);
+    mean_sum_kernel<T64><<<blocks, kReduceThreads, 0, s>>>(x, n, partials);
+    mean_finalize_kernel<<<1, kReduceThreads, 0, s>>>(partials, blocks, n, ctrl, 1, sig_re, sig_im);
+    shift_kernel<T64><<<blocks, kReduceThreads, 0, s>>>(x, n, ctrl);
+    return cudaGetLastError();
+}
+
 template <typename T64, typename T32>
 cudaError_t ir_correct(T64 *x, T32 *e, long long n, cudaStream_t s) {
     const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 8);

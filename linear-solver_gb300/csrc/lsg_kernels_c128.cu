@@ -12,5 +12,8 @@ template cudaError_t ir_residual<cplx<double>, cplx<float>>(const StencilLaunch 
                                                             double *, const DevCtrl *);
 template cudaError_t ir_correct<cplx<double>, cplx<float>>(cplx<double> *, cplx<float> *, long long,
                                                            cudaStream_t);
+template cudaError_t rhs_mean<cplx<double>>(const cplx<double> *, long long, double *, DevCtrl *, cudaStream_t);
+template cudaError_t deflate_x<cplx<double>>(cplx<double> *, long long, double *, DevCtrl *, double, double,
+                                             cudaStream_t);
 
 }  // namespace lsg

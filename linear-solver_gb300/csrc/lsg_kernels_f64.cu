@@ -9,5 +9,7 @@ template cudaError_t ir_residual<double, float>(const StencilLaunch &, const Wei
                                                 const double *, const double *, float *, double *,
                                                 const DevCtrl *);
 template cudaError_t ir_correct<double, float>(double *, float *, long long, cudaStream_t);
+template cudaError_t rhs_mean<double>(const double *, long long, double *, DevCtrl *, cudaStream_t);
+template cudaError_t deflate_x<double>(double *, long long, double *, DevCtrl *, double, double, cudaStream_t);
 
 }  // namespace lsg

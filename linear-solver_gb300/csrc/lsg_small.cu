@@ -570,11 +570,14 @@ __global__ void batch_resume_kernel(BArgs a, const int *amap, int nact, double r
         out->iters = it;
         return;
     }
+    const double target =
+        next_target(&out->tol_frac, &out->floor_misses, rho, out->relres, in->relres, out->tol_abs,
+                    out->restarts == 0);
     out->restarts++;
     in->stall = 0;
     in->stalled = 0;
     in->best = __longlong_as_double(0x7ff0000000000000LL);  // +inf
-    in->tol_abs = fmax(out->tol_abs, rho * out->relres);
+    in->tol_abs = target;
     in->rhs_norm = out->rhs_norm;
     __threadfence();
     in->done = 0;

@@ -494,21 +494,11 @@ struct AarLoop {
         part = ws->partials;
     }
     bool is_anderson(int it) const { return it % p == 0 && it > 1; }
-    // Lean rotation: a Richardson pass writes the buffer that is neither the
-    // current nor the cycle-start residual; the extrapolation residual is
-    // computed in place and becomes the next cycle's start.
-    static int lean_target(int s, int c) { return s == c ? (s + 1) % 3 : 3 - s - c; }
     // r buffers holding the residual (and, lean, the cycle-start residual)
     // after iteration `last`
     void sync_parity(int last) {
         if (lean) {
-            int s = 0, c = 0;
-            for (int it = 1; it <= last; it++) {
-                if (is_anderson(it)) s = c;
-                else c = lean_target(s, c);
-            }
-            rc = c;
-            rsc = s;
+            lean_buffers(last, p, &rsc, &rc);
             xc = 0;
             return;
         }
@@ -516,13 +506,7 @@ struct AarLoop {
         rc = (int)(rich & 1);
         xc = recur ? 0 : rc;
     }
-    // History columns written by the Richardson passes since the last
-    // extrapolation, up to iteration `last` (bit (k-1) % m for iteration k).
-    unsigned cycle_mask(int last) const {
-        unsigned mask = 0;
-        for (int k = last; k >= 1 && !is_anderson(k); k--) mask |= 1u << ((k - 1) % m);
-        return mask;
-    }
+    unsigned cycle_mask(int last) const { return lean_mask(last, p, m); }
     // A lean solve that stopped after Richardson iteration `last` has not
     // added that cycle's steps to x yet: fold them in.
     int finish(int last) {
@@ -835,12 +819,25 @@ int solve_mixed_t(const lsg_operator *op, const lsg_params *prm, T64 *x, const T
     if (rc) return rc;
     LSG_KC(LSG_K_UPDATE, Kernels<T64>::norm2(b, n, opart, rb, octrl, s));
     LSG_KC(LSG_K_SMALL, finalize_norm(opart, rb, octrl, NF_RHS, prm->tol, 0, s, W));
+    // the constant mode decouples when the shift is non-zero (deflate_x)
+    const double sig_re = op->sigma, sig_im = IsCplx<T64>::value ? op->sigma_im : 0.0;
+    const bool deflate = sig_re != 0.0 || sig_im != 0.0;
+    if (deflate) {
+        LSG_KC(LSG_K_REFINE, rhs_mean<T64>(b, n, opart, octrl, s));
+        R.launches += 1;  // sum + finalize
+    }
 
     int status = LSG_NOT_CONVERGED, replacements = 0, it = 1, iters = 0;
+    double frac_run = 1.0;
+    int misses_run = 0;
     DevCtrl co, ci;
     for (;;) {
         // r = b - A x64 in FP64, stored as the FP32 residual the iteration continues from
         A.sync_parity(it - 1);
+        if (deflate) {
+            LSG_KC(LSG_K_REFINE, deflate_x<T64>(x, n, opart, octrl, sig_re, sig_im, s));
+            R.launches += 2;  // sum + finalize + shift
+        }
         LSG_KC(LSG_K_REFINE, (ir_residual<T64, T32>(L64, w64, x, b, A.Rv[A.rc], opart, octrl)));
         LSG_KC(LSG_K_SMALL, finalize_norm(opart, sb64, octrl, NF_CHECK, prm->tol, it - 1, s, W));
         LSG_CUDA(cudaMemcpyAsync(&wo->hctrl[0], octrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost, s));
@@ -858,7 +855,7 @@ int solve_mixed_t(const lsg_operator *op, const lsg_params *prm, T64 *x, const T
             ci.stalled = 0;
             ci.best = INFINITY;
         }
-        ci.tol_abs = std::max(co.tol_abs, rho * co.relres);
+        ci.tol_abs = next_target(&frac_run, &misses_run, rho, co.relres, ci.relres, co.tol_abs, it == 1);
         ci.rhs_norm = co.rhs_norm;
         wi->hctrl[0] = ci;
         LSG_CUDA(cudaMemcpyAsync(A.ctrl, wi->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, s));

@@ -139,7 +139,15 @@ def test_differentiable_batch_16x128(lsg):
     # by the slow modes (~1e3 here: 0.9e-6 to 1.3e-6 measured for FP64
     # replacements every 3e-2 and every 3e-4 of FP32 residual reduction)
     assert ((gb - gb64).norm() / gb64.norm()).item() <= 3e-6
-    assert ((gs - gs64).abs() / gs64.abs()).max().item() <= 1e-5
+    # dL/dsigma = -x . lambda sums N products of both signs: its error follows
+    # the solves' error times ||x|| ||lambda||, not |dL/dsigma|, so instances
+    # whose sum cancels are compared against a floor of 0.1 x the batch's
+    # largest |dL/dsigma| (absolute errors here: 1e-11 .. 1e-9)
+    def rel(g, ref):
+        scale = torch.maximum(ref.abs(), 0.1 * ref.abs().max())
+        return ((g - ref).abs() / scale).max().item()
+
+    assert rel(gs, gs64) <= 1e-5
     with torch.no_grad():
         h = 1e-4 * st
         solve = lambda rhs, s, prec, tol: lsg.solve_shifted(rhs, s, a=a, precision=prec, tol=tol,
@@ -147,8 +155,8 @@ def test_differentiable_batch_16x128(lsg):
         xm = mean_free(solve(bt, st - h, "mixed", 1e-11))
         y = mean_free(solve(xm, st + h, "fp64", 1e-10))
         fd = -dot(y, xm - h[:, None, None, None] * y - xst)
-        err64 = ((gs64 - fd).abs() / fd.abs()).max().item()
-        err = ((gs - fd).abs() / fd.abs()).max().item()
+        err64 = rel(gs64, fd)
+        err = rel(gs, fd)
         assert err64 <= 1e-7
         assert err <= 1e-5
         g = torch.Generator(device="cuda").manual_seed(3)

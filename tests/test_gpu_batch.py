@@ -52,17 +52,22 @@ def test_batched_real_matches_single(lsg, dtype_name):
         assert rel <= (1e-9 if dt == torch.float64 else 1e-4)
 
 
-def test_batched_p1_and_max_iter(lsg):
-    """p = 1 (iteration 1 is the only Richardson one) and a max_iter stop."""
+@pytest.mark.parametrize("dtype_name", ["float64", "float32"])
+def test_batched_p1_and_max_iter(lsg, dtype_name):
+    """p = 1 (iteration 1 is the only Richardson one) and max_iter stops.  In
+    FP32 the Richardson passes leave x out, so a stop between extrapolations
+    (17, 23) folds the cycle's steps into x, and p = 1 rotates the residual
+    buffers differently; each instance must match its single solve."""
     import torch
+    dt = getattr(torch, dtype_name)
     ops = [lsg.Operator(n, a=-float(n * n), sigma=1.0) for n in (12, 16)]
-    bs = [_cuda(_real_problem(n, 3 + n), torch.float64) for n in (12, 16)]
-    for kw in (dict(p=1, m=3), dict(max_iter=17)):
+    bs = [_cuda(_real_problem(n, 3 + n), dt) for n in (12, 16)]
+    for kw in (dict(p=1, m=3), dict(max_iter=17), dict(max_iter=23, m=5, p=4), dict(max_iter=18)):
         xs, rs = lsg.aar_batched(ops, bs, **kw)
         for op, b, x, r in zip(ops, bs, xs, rs):
             x1, r1 = lsg.aar(op, b, **kw)
             assert r["iters"] == r1["iters"] and r["status"] == r1["status"]
-            assert ((x - x1).norm() / x1.norm()).item() <= 1e-9
+            assert ((x - x1).norm() / x1.norm()).item() <= (1e-9 if dt == torch.float64 else 1e-5)
 
 
 def test_batched_generic_radius(lsg, oracle):
