@@ -48,7 +48,7 @@ CPU_SAMPLE_ITERS = 24
 # DRAM bytes (read + write) of one launch of the dominant kernel at this
 # workload, from the ncu capture summarised in
 # profiles/richardson_f32_lean_256cube.md.
-RICH32_TRAFFIC_BYTES = 225.0e6
+RICH32_TRAFFIC_BYTES = 224.2e6
 
 
 def _peaks():
@@ -339,7 +339,7 @@ def run_lsg(args):
                  "richardson_ms": rich64_ms,
                  "richardson_gpts": N / (rich64_ms * 1e-3) / 1e9},
         "roofline": {"bound": "hbm",
-                     "kernel": "stencil_x2_kernel<float, 8, 2, 2, RichLeanOp> (fused Richardson step, x left out)",
+                     "kernel": "stencil_x2_kernel<float, RichLeanOp> in the tuned paired shape (fused Richardson step, x left out)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
                      "traffic": RICH32_TRAFFIC_BYTES, "traffic_unit": "bytes per launch (ncu)",
@@ -442,6 +442,7 @@ def run_case(case: str):
     workload -- the initial residual, five fused Richardson steps and one
     Anderson step (Gram, m x m solve, update, residual).
     mixed / fp64: one complete solve of the benchmark workload.
+    Launch shapes are autotuned first, as in the benchmark run.
     """
     import torch
 
@@ -451,6 +452,11 @@ def run_case(case: str):
     torch.cuda.set_device(0)
     op = lsg.Operator(N_GRID)
     b = torch.from_numpy(workloads.uniform_rhs(N_GRID, SEED)).cuda()
+    lsg.autotune(op, torch.float32 if case in ("rich32", "mixed") else torch.float64)
+    torch.cuda.synchronize()
+    # the solve's launches sit in an NVTX range "solve" (ncu --nvtx
+    # --nvtx-include "solve/" leaves out the tuner's launches)
+    torch.cuda.nvtx.range_push("solve")
     if case == "rich32":
         x, info = lsg.aar(op, b.float(), max_iter=6, **SOLVER_KW)
     elif case == "rich64":
@@ -460,6 +466,7 @@ def run_case(case: str):
     else:
         x, info = lsg.aar(op, b, **SOLVER_KW)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     print(json.dumps({"case": case, "iters": info["iters"], "relres": info["relres"],
                       "launches": info["launches"], "status": info["status_name"]}))
     return 0
