@@ -147,9 +147,12 @@ int lsg_gmres(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_
 /* Mixed precision: FP64 x and b (lsg_aar_mixed_c: complex128 x and b with a
  * complex64 inner iteration).  One FP32 AAR (FP32 vectors, history and
  * stencil; FP64-class reductions and m x m solve) runs on the correction;
- * each time its residual has dropped by inner_tol the correction is folded
- * into x (FP64), r = b - A x is recomputed in FP64 and the FP32 iteration
- * resumes from it with its history intact.  Stops when the FP64 residual
+ * each time its residual has dropped by inner_tol (or reached tol) the
+ * correction is folded into x (FP64), r = b - A x is recomputed in FP64 and
+ * the FP32 iteration resumes from it with its history intact.  With a
+ * non-zero shift sigma the constant mode is set exactly before each
+ * replacement (mean(x) = mean(b) / sigma: the periodic operator maps the
+ * constant vector to sigma times itself).  Stops when the FP64 residual
  * satisfies tol.  res->iters counts FP32 iterations, res->outer_iters the
  * FP64 residual replacements. */
 int lsg_aar_mixed(const lsg_operator *op, const lsg_params *prm, double *d_x, const double *d_b,
