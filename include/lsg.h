@@ -84,6 +84,9 @@ typedef struct lsg_result {
     int inner_iters;     /* mixed solver: total FP32 iterations */
     double seconds;      /* host wall time of the call */
     long long launches;  /* kernels launched by the call */
+    int svd_fallbacks;   /* extrapolations whose m x m solve took the Jacobi SVD
+                            (the Gram was not provably well enough conditioned
+                            for the LDL^T path) */
 } lsg_result;
 
 /* Fills c[0..radius] with the reference FD coefficients.  Returns LSG_BAD_ARG

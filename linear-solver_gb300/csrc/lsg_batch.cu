@@ -704,6 +704,7 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
         }
         r.seconds = secs;
         r.launches = B.launches;
+        r.svd_fallbacks = c.svd_fallbacks;
         if (res) res[i] = r;
         if (r.status != LSG_OK && worst == LSG_OK) worst = r.status;
     }

@@ -397,6 +397,7 @@ static void fill_result(lsg_result *res, const DevCtrl &c, int max_iter, double 
     else res->status = (c.status == LSG_SVD_NO_CONVERGENCE) ? LSG_SVD_NO_CONVERGENCE : LSG_NOT_CONVERGED;
     res->seconds = seconds;
     res->launches = launches;
+    res->svd_fallbacks = c.svd_fallbacks;
 }
 
 static double now_s() {
@@ -884,6 +885,7 @@ int solve_mixed_t(const lsg_operator *op, const lsg_params *prm, T64 *x, const T
         res->status = status;
         res->seconds = now_s() - t0;
         res->launches = R.launches;
+        res->svd_fallbacks = ci.svd_fallbacks;
     }
     set_last_status(status);
     return status;

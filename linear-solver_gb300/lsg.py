@@ -50,7 +50,7 @@ class _Params(C.Structure):
 class _Result(C.Structure):
     _fields_ = [("iters", C.c_int), ("relres", C.c_double), ("rhs_norm", C.c_double),
                 ("status", C.c_int), ("outer_iters", C.c_int), ("inner_iters", C.c_int),
-                ("seconds", C.c_double), ("launches", C.c_longlong)]
+                ("seconds", C.c_double), ("launches", C.c_longlong), ("svd_fallbacks", C.c_int)]
 
 
 class _KernelStats(C.Structure):
@@ -257,7 +257,8 @@ def _check_vec(t, op: Operator, name: str):
 def _result(r: _Result) -> dict:
     return dict(iters=r.iters, relres=r.relres, rhs_norm=r.rhs_norm, status=r.status,
                 status_name=STATUS.get(r.status, str(r.status)), outer_iters=r.outer_iters,
-                inner_iters=r.inner_iters, seconds=r.seconds, launches=r.launches)
+                inner_iters=r.inner_iters, seconds=r.seconds, launches=r.launches,
+                svd_fallbacks=r.svd_fallbacks)
 
 
 def apply(op: Operator, x, out=None, stream=None):
