@@ -39,6 +39,7 @@ struct DevCtrl {
     int svd_fallbacks;  // extrapolation steps whose Gram needed the Jacobi SVD
     double tol_frac;  // mixed solves (outer block): the next run's floor, as a fraction of tol_abs
     int floor_misses; // mixed solves (outer block): consecutive runs that reached the floor, true residual > tol
+    int x_zero;       // mixed solves (outer block): the initial x64 was exactly zero
     double bmean[2];  // mixed solves (outer block): mean of b (re, im)
     double shift[2];  // mixed solves (outer block): constant added to x64 by the last deflation
     double s[LSG_MAX_M];  // m x m solve output
@@ -399,7 +400,18 @@ struct Kernels {
 // r32 = float(b - A x64), partial ||b - A x64||^2 (FP64 stencil).
 template <typename T64, typename T32>
 cudaError_t ir_residual(const StencilLaunch &L, const Weights<T64> &w, const T64 *x,
-                        const T64 *b, T32 *r32, double *partials, const DevCtrl *ctrl);
+                        const T64 *b, T32 *r32, double *partials, const DevCtrl *ctrl, int zgate = 0);
+// The first refinement residual without the stencil when the initial x64
+// was zero (ctrl->x_zero, set by zero_check): x64 is then the constant the
+// deflation added (or 0), which A maps to sigma times itself, so
+// r = b - sigma * shift.  It writes the partials of the stencil pass it
+// replaces (`blocks` of them); ir_residual with zgate = 1 stands down then.
+template <typename T64, typename T32>
+cudaError_t ir_residual_const(const T64 *b, T32 *r32, long long n, double *partials, int blocks,
+                              const DevCtrl *ctrl, double sig_re, double sig_im, cudaStream_t s);
+// ctrl->x_zero = 0 when x holds a non-zero value (the host sets it to 1 first).
+template <typename T64>
+cudaError_t zero_check(const T64 *x, long long n, DevCtrl *ctrl, cudaStream_t s);
 // x64 += e32; e32 = 0
 template <typename T64, typename T32>
 cudaError_t ir_correct(T64 *x, T32 *e, long long n, cudaStream_t s);

@@ -310,7 +310,8 @@ struct IrResidualOp {
     T32 *r32;
     double *partials;
     const DevCtrl *ctrl;
-    __device__ bool skip() const { return solve_done(ctrl); }
+    int zgate;  // 1: stand down when ctrl->x_zero (ir_residual_const serves)
+    __device__ bool skip() const { return solve_done(ctrl) || (zgate && ctrl->x_zero); }
     __device__ void init() {}
     __device__ __forceinline__ Raw fetch(unsigned i) const { return ldg(x + i); }
     __device__ __forceinline__ T64 value(const Raw &v) const { return v; }
@@ -1245,9 +1246,64 @@ cudaError_t Kernels<T>::axpy(T *x, const T *y, double alpha, long long n, cudaSt
 
 template <typename T64, typename T32>
 cudaError_t ir_residual(const StencilLaunch &L, const Weights<T64> &w, const T64 *x,
-                        const T64 *b, T32 *r32, double *partials, const DevCtrl *ctrl) {
-    IrResidualOp<T64, T32> op{x, b, r32, partials, ctrl};
+                        const T64 *b, T32 *r32, double *partials, const DevCtrl *ctrl, int zgate) {
+    IrResidualOp<T64, T32> op{x, b, r32, partials, ctrl, zgate};
     return launch_stencil<T64>(L, w, op);
+}
+
+template <typename T64, typename T32>
+__global__ void __launch_bounds__(kReduceThreads) ir_residual_const_kernel(const T64 *__restrict__ b,
+                                                                           T32 *__restrict__ r32, long long n,
+                                                                           double *partials, const DevCtrl *ctrl,
+                                                                           double sr, double si) {
+    constexpr int W = AccWidth<T64>::value;
+    __shared__ double red[(kReduceThreads / 32) * W];
+    if (solve_done(ctrl) || !ctrl->x_zero) return;
+    T64 c;  // sigma * shift
+    if constexpr (IsCplx<T64>::value)
+        c = T64(sr * ctrl->shift[0] - si * ctrl->shift[1], sr * ctrl->shift[1] + si * ctrl->shift[0]);
+    else
+        c = sr * ctrl->shift[0];
+    Acc<T64> acc;
+    acc.zero();
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const T64 rn = ldg(b + i) - c;
+        r32[i] = (T32)rn;
+        acc.add_prod(rn, rn);
+    }
+    Acc<T64> a1[1] = {acc};
+    block_reduce_store<1>(a1, red, partials + (long long)blockIdx.x * W);
+}
+
+template <typename T64, typename T32>
+cudaError_t ir_residual_const(const T64 *b, T32 *r32, long long n, double *partials, int blocks,
+                              const DevCtrl *ctrl, double sig_re, double sig_im, cudaStream_t s) {
+    ir_residual_const_kernel<T64, T32><<<blocks, kReduceThreads, 0, s>>>(b, r32, n, partials, ctrl, sig_re, sig_im);
+    return cudaGetLastError();
+}
+
+template <typename T64>
+__global__ void __launch_bounds__(kReduceThreads) zero_check_kernel(const T64 *__restrict__ x, long long n,
+                                                                    DevCtrl *ctrl) {
+    bool nz = false;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if constexpr (IsCplx<T64>::value) {
+            const T64 v = x[i];
+            nz |= (v.x != 0.0) || (v.y != 0.0);
+        } else {
+            nz |= x[i] != 0.0;  // NaN counts as non-zero
+        }
+    }
+    if (__syncthreads_or(nz) && threadIdx.x == 0) ctrl->x_zero = 0;
+}
+
+template <typename T64>
+cudaError_t zero_check(const T64 *x, long long n, DevCtrl *ctrl, cudaStream_t s) {
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 4);
+    zero_check_kernel<T64><<<blocks, kReduceThreads, 0, s>>>(x, n, ctrl);
+    return cudaGetLastError();
 }
 
 // x64 += e32; e32 = 0 (the correction is folded into x and restarts at zero).

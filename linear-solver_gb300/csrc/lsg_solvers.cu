@@ -814,8 +814,11 @@ int solve_mixed_t(const lsg_operator *op, const lsg_params *prm, T64 *x, const T
     AarLoop<T32> A(R, op, prm, e32, nullptr, wi);
 
     wo->hctrl[0] = ctrl_init(prm->tol, 0);
+    wo->hctrl[0].x_zero = 1;
     LSG_CUDA(cudaMemcpyAsync(octrl, wo->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, s));
     LSG_CUDA(cudaMemsetAsync(e32, 0, sizeof(T32) * (size_t)n, s));
+    // x0 = 0 (the usual start): the first residual needs no stencil pass
+    LSG_KC(LSG_K_REFINE, zero_check<T64>(x, n, octrl, s));
     rc = A.reset_history();
     if (rc) return rc;
     LSG_KC(LSG_K_UPDATE, Kernels<T64>::norm2(b, n, opart, rb, octrl, s));
@@ -839,7 +842,11 @@ int solve_mixed_t(const lsg_operator *op, const lsg_params *prm, T64 *x, const T
             LSG_KC(LSG_K_REFINE, deflate_x<T64>(x, n, opart, octrl, sig_re, sig_im, s));
             R.launches += 2;  // sum + finalize + shift
         }
-        LSG_KC(LSG_K_REFINE, (ir_residual<T64, T32>(L64, w64, x, b, A.Rv[A.rc], opart, octrl)));
+        const int first = it == 1 ? 1 : 0;
+        LSG_KC(LSG_K_REFINE, (ir_residual<T64, T32>(L64, w64, x, b, A.Rv[A.rc], opart, octrl, first)));
+        if (first)
+            LSG_KC(LSG_K_REFINE, (ir_residual_const<T64, T32>(b, A.Rv[A.rc], n, opart, sb64, octrl, sig_re, sig_im,
+                                                             s)));
         LSG_KC(LSG_K_SMALL, finalize_norm(opart, sb64, octrl, NF_CHECK, prm->tol, it - 1, s, W));
         LSG_CUDA(cudaMemcpyAsync(&wo->hctrl[0], octrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost, s));
         LSG_CUDA(cudaStreamSynchronize(s));

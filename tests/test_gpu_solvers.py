@@ -184,6 +184,30 @@ def test_mixed_deflates_constant_mode(lsg, oracle, sigma):
     assert abs(x.mean().item() - b.mean() / sigma) <= 1e-9 * abs(b.mean() / sigma)
 
 
+@pytest.mark.parametrize("sigma", [0.0, 2.0])
+def test_mixed_initial_guess(lsg, oracle, sigma):
+    """x0 = 0 starts from r = b without a stencil pass (b - sigma c after the
+    constant-mode deflation); a non-zero x0 takes the FP64 residual.  Both
+    converge to the same solution."""
+    import torch
+    import workloads
+    n = 40
+    b = workloads.uniform_rhs(n, 21)
+    b = b - b.mean()
+    op = lsg.Operator(n, sigma=sigma)
+    bt = _t(b)
+    x0 = _t(np.random.default_rng(3).uniform(-1, 1, b.shape))
+    xa, ra = lsg.aar_mixed(op, bt, tol=1e-10)
+    xb, rb = lsg.aar_mixed(op, bt, x0, tol=1e-10)
+    for x, r in ((xa, ra), (xb, rb)):
+        assert r["status"] == 0, r
+        assert ((bt - lsg.apply(op, x)).norm() / bt.norm()).item() <= 1e-10 * 1.01
+    if sigma == 0.0:
+        assert _merr(xa.cpu().numpy(), xb.cpu().numpy()) < 1e-6
+    else:
+        assert ((xa - xb).norm() / xa.norm()).item() < 1e-6
+
+
 def test_mixed_precision_to_1e10(lsg, oracle):
     import workloads
     b = workloads.uniform_rhs(48, 0)
