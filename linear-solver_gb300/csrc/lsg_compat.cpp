@@ -39,6 +39,8 @@ struct Staging {
     double *x = nullptr, *b = nullptr;
     long long n = 0;
 } g_stage;
+// Two copy streams: x and rhs go to the device concurrently.
+cudaStream_t g_copy[2] = {nullptr, nullptr};
 
 // Operators bound to a CSR copy of their matrix (lsg_register_operator_csr).
 struct CsrBinding {
@@ -167,8 +169,14 @@ void run_compat(const char *who, int solver, POISSON *system, void *lap, void *p
         }
         g_stage.n = n;
     }
-    if (cudaMemcpy(g_stage.x, x, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(g_stage.b, rhs, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+    for (auto &c : g_copy)
+        if (!c && cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            c = nullptr;
+        }
+    if (cudaMemcpyAsync(g_stage.x, x, sizeof(double) * n, cudaMemcpyHostToDevice, g_copy[0]) != cudaSuccess ||
+        cudaMemcpyAsync(g_stage.b, rhs, sizeof(double) * n, cudaMemcpyHostToDevice, g_copy[1]) != cudaSuccess ||
+        cudaStreamSynchronize(g_copy[0]) != cudaSuccess || cudaStreamSynchronize(g_copy[1]) != cudaSuccess) {
         fail(who, LSG_CUDA_ERROR, "host to device copy failed");
         return;
     }
