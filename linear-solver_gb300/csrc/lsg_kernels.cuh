@@ -11,6 +11,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cstdlib>
 #include <type_traits>
 
 #include "lsg_stencil.cuh"
@@ -596,10 +597,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *b, unsigne
     return true;
 }
 
+// extra_tx: bytes armed on each stage beyond the copies' (0; the failure
+// test arms more, so the waits run out and the timeout path is taken).
 template <int M>
 __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const float *__restrict__ df,
                                                                      const float *__restrict__ r, long long n,
-                                                                     double *partials, DevCtrl *ctrl) {
+                                                                     double *partials, DevCtrl *ctrl,
+                                                                     unsigned extra_tx) {
     constexpr int NP = (M * (M + 1)) / 2;
     constexpr int NV = NP + M;
     constexpr int S = kGramStages, CH = kGramChunk, CV = CH / 4;
@@ -623,7 +627,7 @@ __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const floa
         const unsigned bytes = (unsigned)(min((long long)CH, n - off) * 4);
         unsigned long long *bar = &full[k % S];
         float *dst = gsm + (size_t)(k % S) * (M + 1) * CH;
-        mbar_expect_tx(bar, bytes * (M + 1));
+        mbar_expect_tx(bar, bytes * (M + 1) + extra_tx);
 #pragma unroll
         for (int v = 0; v < M; v++) bulk_g2s(dst + v * CH, df + (long long)v * n + off, bytes, bar);
         bulk_g2s(dst + M * CH, r + off, bytes, bar);
@@ -1056,6 +1060,12 @@ static cudaError_t gram_dispatch(int m, const T *dx, const T *df, const T *r, lo
         // the bulk-copy form: 16-byte aligned columns and residual, n % 4 == 0
         if (n % 4 == 0 && m >= 1 && m <= 8 && (((uintptr_t)df | (uintptr_t)r) & 15u) == 0) {
             DevCtrl *c = const_cast<DevCtrl *>(ctrl);
+            // LSG_FAULT_GRAM_TX=<bytes>: failure test of the bounded waits
+            static const unsigned extra_tx = [] {
+                const char *e = getenv("LSG_FAULT_GRAM_TX");
+                const long v = e ? atol(e) : 0;
+                return (unsigned)(v > 0 && v < 65536 ? v : 0);
+            }();
             switch (m) {
 #define LSG_GRAM_BULK(MM)                                                                                     \
     case MM: {                                                                                                \
@@ -1065,7 +1075,8 @@ static cudaError_t gram_dispatch(int m, const T *dx, const T *df, const T *r, lo
                                  (int)gram_bulk_smem<MM>());                                                  \
             attr = true;                                                                                      \
         }                                                                                                     \
-        gram_bulk_kernel<MM><<<blocks, kReduceThreads, gram_bulk_smem<MM>(), s>>>(df, r, n, partials, c);     \
+        gram_bulk_kernel<MM><<<blocks, kReduceThreads, gram_bulk_smem<MM>(), s>>>(df, r, n, partials, c,      \
+                                                                                  extra_tx);                  \
         return cudaGetLastError();                                                                            \
     }
                 LSG_GRAM_BULK(1) LSG_GRAM_BULK(2) LSG_GRAM_BULK(3) LSG_GRAM_BULK(4)

@@ -393,6 +393,7 @@ static void fill_result(lsg_result *res, const DevCtrl &c, int max_iter, double 
     res->rhs_norm = c.rhs_norm;
     res->relres = c.rhs_norm > 0 ? c.relres / c.rhs_norm : c.relres;
     if (c.status == LSG_NAN_DETECTED) res->status = LSG_NAN_DETECTED;
+    else if (c.status == LSG_TIMEOUT) res->status = LSG_TIMEOUT;
     else if (c.done && !c.stalled && !(c.relres > c.tol_abs)) res->status = LSG_OK;
     else res->status = (c.status == LSG_SVD_NO_CONVERGENCE) ? LSG_SVD_NO_CONVERGENCE : LSG_NOT_CONVERGED;
     res->seconds = seconds;
@@ -871,6 +872,7 @@ int solve_mixed_t(const lsg_operator *op, const lsg_params *prm, T64 *x, const T
         if (rc != LSG_OK) return rc;
         LSG_CUDA(cudaMemcpy(&ci, A.ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost));
         if (ci.status == LSG_NAN_DETECTED) { status = LSG_NAN_DETECTED; break; }
+        if (ci.status == LSG_TIMEOUT) { status = LSG_TIMEOUT; break; }
         iters = ci.done ? ci.iters : prm->max_iter;
         if (!ci.done) {
             rc = A.finish(iters);
