@@ -203,6 +203,12 @@ int lsg_set_autotune(int mode);
 int lsg_autotune_save(const char *path);
 int lsg_autotune_load(const char *path, int *count);
 
+/* Bounds-checked build (built with LSG_BOUNDS=1): *first_bad = the first
+ * out-of-range global or shared index a stencil march met since the library
+ * loaded, or -1 when none (the access was skipped, nothing faulted).  The
+ * normal build returns LSG_UNSUPPORTED and sets -1.  first_bad may be NULL. */
+int lsg_bounds_errors(long long *first_bad);
+
 /* m x m pseudo-inverse solve with the reference's semantics
  * (x = V diag(1/w) V^T b, w < m*wmax*2.22044605e-16 dropped; MPI_REAL/tools.c:52-105),
  * computed on the device by one warp.  A row-major, device pointers. */

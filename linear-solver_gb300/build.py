@@ -2,6 +2,11 @@
 
     python linear-solver_gb300/build.py            # incremental
     python linear-solver_gb300/build.py --force    # rebuild everything
+    LSG_BOUNDS=1 python linear-solver_gb300/build.py   # bounds-checked debug build
+
+The bounds-checked build (-DLSG_BOUNDS) checks every global and shared index
+of the stencil marches, records the first one out of range and skips the
+access (lsg_bounds_errors reads it): the substitute for a sanitizer run.
 
 Each translation unit is compiled in parallel into ``_build/`` and linked
 into ``liblsg.so`` next to this file.  No CMake, no torch extension machinery:
@@ -18,12 +23,14 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
+BOUNDS = os.environ.get("LSG_BOUNDS", "") == "1"
+BUILD = os.path.join(HERE, "_build_bounds" if BOUNDS else "_build")
 LIB = os.path.join(HERE, "liblsg.so")
+VARIANT = os.path.join(HERE, "_build", "liblsg.variant")  # which build the library holds
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
-              "-diag-suppress", "177", f"-I{os.path.join(ROOT, 'include')}"]
+              "-diag-suppress", "177", f"-I{os.path.join(ROOT, 'include')}"] + (["-DLSG_BOUNDS"] if BOUNDS else [])
 SOURCES = ["lsg_kernels_f64.cu", "lsg_kernels_f32.cu", "lsg_kernels_c128.cu", "lsg_kernels_c64.cu",
            "lsg_batch_f64.cu", "lsg_batch_f32.cu", "lsg_batch_c128.cu", "lsg_batch_c64.cu",
            "lsg_small.cu", "lsg_solvers.cu", "lsg_batch.cu", "lsg_tune.cu", "lsg_krylov.cu", "lsg_csr.cu", "lsg_compat.cpp"]
@@ -67,11 +74,16 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, force), SOURCES))
-    if force or _stale(LIB, objs):
+    variant = "bounds" if BOUNDS else "normal"
+    held = open(VARIANT).read().strip() if os.path.exists(VARIANT) else ""
+    if force or held != variant or _stale(LIB, objs):
         cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        os.makedirs(os.path.dirname(VARIANT), exist_ok=True)
+        with open(VARIANT, "w") as f:
+            f.write(variant)
     if verbose:
         print("built", LIB)
     return LIB

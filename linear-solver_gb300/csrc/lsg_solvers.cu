@@ -12,6 +12,7 @@
 // enqueues `check_every` extrapolation cycles ahead and reads the flag
 // through pinned memory, so the GPU never idles waiting for the host.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <chrono>
@@ -319,8 +320,41 @@ struct Run {
     }
 };
 
+// Readers of the per-translation-unit bounds words (bounds-checked build).
+std::vector<unsigned long long (*)()> &bounds_readers() {
+    static std::vector<unsigned long long (*)()> v;
+    return v;
+}
+int register_bounds_reader(unsigned long long (*read)()) {
+    bounds_readers().push_back(read);
+    return 0;
+}
+
+// Tracing: with LSG_NVTX=1 in the environment every solve and every kernel
+// launch sits in an NVTX range (the solver's name; the kernel class), for
+// profiler timelines and `ncu --nvtx --nvtx-include "<class>/"` filters.
+static bool trace_on() {
+    static const bool on = [] {
+        const char *e = getenv("LSG_NVTX");
+        return e && e[0] == '1';
+    }();
+    return on;
+}
+struct TraceRange {
+    bool on;
+    explicit TraceRange(const char *name) : on(trace_on()) {
+        if (on) nvtxRangePushA(name);
+    }
+    ~TraceRange() {
+        if (on) nvtxRangePop();
+    }
+};
+static const char *const kClassNames[LSG_K_CLASSES] = {"richardson", "residual", "gram",   "update",
+                                                       "small",      "cg",       "refine", "other"};
+
 #define LSG_KC(cls, call)                                                                    \
     do {                                                                                     \
+        TraceRange tr_(kClassNames[cls]);                                                    \
         cudaEvent_t ea_ = nullptr;                                                           \
         if (R.prof && (ea_ = R.event()) != nullptr) cudaEventRecord(ea_, R.s);               \
         cudaError_t e_ = (call);                                                             \
@@ -722,6 +756,8 @@ int cg_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const T
 template <typename T>
 static int solve_t(int solver, const lsg_operator *op, const lsg_params *prm, void *d_x,
                    const void *d_b, lsg_result *res, cudaStream_t s) {
+    static const char *const names[4] = {"lsg_aar", "lsg_pgr", "lsg_pl2r", "lsg_cg"};
+    TraceRange trace(names[solver & 3]);
     const double t0 = now_s();
     const Geom g = make_geom(op->n);
     Workspace *ws = nullptr;
@@ -785,6 +821,7 @@ template <typename T64, typename T32>
 int solve_mixed_t(const lsg_operator *op, const lsg_params *prm, T64 *x, const T64 *b,
                   lsg_result *res, cudaStream_t s) {
     constexpr int W = AccWidth<T64>::value;
+    TraceRange trace("lsg_aar_mixed");
     const double t0 = now_s();
     int rc = check_operator(op);
     if (rc) return rc;
@@ -1024,6 +1061,7 @@ static int csr_extra(long long n, CsrExtra **out) {
 // the Gram, m x m solve and update kernels with a unit Jacobi factor.
 int solve_csr(const lsg_csr *Ain, const lsg_params *prm, double *x, const double *b, lsg_result *res,
               cudaStream_t s) {
+    TraceRange trace("lsg_aar_csr");
     const double t0 = now_s();
     CsrView A;
     int rc = csr_view(Ain, &A);
@@ -1227,6 +1265,21 @@ int lsg_profile_read(lsg_kernel_stats *stats) {
     return LSG_OK;
 }
 int lsg_last_status(void) { return lsg::last_status(); }
+
+int lsg_bounds_errors(long long *first_bad) {
+#ifdef LSG_BOUNDS
+    unsigned long long first = 0;
+    for (auto read : lsg::bounds_readers()) {
+        const unsigned long long v = read();
+        if (v && !first) first = v;
+    }
+    if (first_bad) *first_bad = first ? (long long)(first - 1) : -1;
+    return LSG_OK;
+#else
+    if (first_bad) *first_bad = -1;
+    return LSG_UNSUPPORTED;
+#endif
+}
 const char *lsg_last_error(void) { return lsg::last_error(); }
 
 const char *lsg_status_string(int st) {

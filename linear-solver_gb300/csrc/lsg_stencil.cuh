@@ -42,6 +42,35 @@ __device__ __forceinline__ T ldg(const T *p) { return __ldg(p); }
 
 struct NoCtr {};
 
+// Bounds-checked build (-DLSG_BOUNDS): every global and shared index of the
+// stencil marches is checked; the first out-of-range index is recorded
+// (+1, in this translation unit's word) and the access is skipped (a load
+// reads element 0 instead).  lsg_bounds_errors() reads the words of every
+// unit.  The normal build compiles the checks away.
+#ifdef LSG_BOUNDS
+static __device__ unsigned long long g_bounds_bad;
+__device__ __forceinline__ bool bounds_ok(unsigned long long i, unsigned long long n) {
+    if (i < n) return true;
+    atomicCAS(&g_bounds_bad, 0ull, i + 1ull);
+    return false;
+}
+__device__ __forceinline__ unsigned bounds_ix(unsigned long long i, unsigned long long n) {
+    return bounds_ok(i, n) ? (unsigned)i : 0u;
+}
+int register_bounds_reader(unsigned long long (*read)());
+static unsigned long long bounds_read_unit() {
+    unsigned long long v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_bounds_bad, sizeof(v)) != cudaSuccess) cudaGetLastError();
+    return v;
+}
+static const int g_bounds_registered = register_bounds_reader(&bounds_read_unit);
+#define LSG_IX(i, n) ::lsg::bounds_ix((unsigned long long)(i), (unsigned long long)(n))
+#define LSG_IX_OK(i, n) ::lsg::bounds_ok((unsigned long long)(i), (unsigned long long)(n))
+#else
+#define LSG_IX(i, n) (i)
+#define LSG_IX_OK(i, n) true
+#endif
+
 // Calls f(integral_constant<P>), f(integral_constant<P+1>), ... up to Q-1
 // while f returns true; returns false as soon as one call does.
 template <int P, int Q, class F>
@@ -70,6 +99,9 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
     constexpr int H = 2 * RQ * TX + TY * 2 * RQ;  // halo cells of one plane (no corners: the stencil is a star)
     constexpr int NH = (H + NT - 1) / NT;
     constexpr int Q = 2 * RQ + 1;
+    constexpr int FY = TY + 2 * RQ;
+    const unsigned long long gn = (unsigned long long)g.n;
+    (void)gn;
 
     const int radius = GENERIC ? w.radius : RQ;
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -129,7 +161,7 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
     for (int s = 0; s < 2 * RQ; s++) {
         const unsigned base = zl * nxy;
 #pragma unroll
-        for (int k = 0; k < NY; k++) q[k][s] = op.value(op.fetch(base + col[k]));
+        for (int k = 0; k < NY; k++) q[k][s] = op.value(op.fetch(LSG_IX(base + col[k], gn)));
         zl = (zl + 1 == nz) ? 0u : zl + 1;
     }
     // In flight for the next plane: queue head (plane z+RQ), halo and centres (plane z).
@@ -139,12 +171,12 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
         const unsigned lb = zl * nxy, zb = (unsigned)z0 * nxy;
 #pragma unroll
         for (int k = 0; k < NY; k++) {
-            qn[k] = op.fetch(lb + col[k]);
-            cn[k] = op.fetch_center(zb + col[k]);
+            qn[k] = op.fetch(LSG_IX(lb + col[k], gn));
+            cn[k] = op.fetch_center(LSG_IX(zb + col[k], gn));
         }
 #pragma unroll
         for (int s = 0; s < NH; s++)
-            if (hs[s] >= 0) hn[s] = op.fetch(zb + ho[s]);
+            if (hs[s] >= 0) hn[s] = op.fetch(LSG_IX(zb + ho[s], gn));
         zl = (zl + 1 == nz) ? 0u : zl + 1;
     }
 
@@ -158,11 +190,11 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
 #pragma unroll
         for (int k = 0; k < NY; k++) {
             q[k][HEAD] = op.value(qn[k]);
-            sm[(RQ + ty * NY + k) * FX + RQ + tx] = q[k][CEN];
+            sm[LSG_IX((RQ + ty * NY + k) * FX + RQ + tx, FX * FY)] = q[k][CEN];
         }
 #pragma unroll
         for (int s = 0; s < NH; s++)
-            if (hs[s] >= 0) sm[hs[s]] = op.value(hn[s]);
+            if (hs[s] >= 0) sm[LSG_IX(hs[s], FX * FY)] = op.value(hn[s]);
         Ctr cc[NY];
 #pragma unroll
         for (int k = 0; k < NY; k++) cc[k] = cn[k];
@@ -170,12 +202,12 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
             const unsigned lb = zl * nxy, nb = zbase + nxy;
 #pragma unroll
             for (int k = 0; k < NY; k++) {
-                qn[k] = op.fetch(lb + col[k]);
-                cn[k] = op.fetch_center(nb + col[k]);
+                qn[k] = op.fetch(LSG_IX(lb + col[k], gn));
+                cn[k] = op.fetch_center(LSG_IX(nb + col[k], gn));
             }
 #pragma unroll
             for (int s = 0; s < NH; s++)
-                if (hs[s] >= 0) hn[s] = op.fetch(nb + ho[s]);
+                if (hs[s] >= 0) hn[s] = op.fetch(LSG_IX(nb + ho[s], gn));
             zl = (zl + 1 == nz) ? 0u : zl + 1;
         }
         __syncthreads();  // plane z staged; the other buffer is no longer read
@@ -202,7 +234,7 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
                 const T sz = q[k][(CEN + Q - p) % Q] + q[k][(CEN + p) % Q];
                 au = fma(w.w[p], sxy + sz, au);
             }
-            if (valid[k]) op.store(zbase + col[k], q[k][CEN], au, cc[k], acc);
+            if (valid[k] && LSG_IX_OK(zbase + col[k], gn)) op.store(zbase + col[k], q[k][CEN], au, cc[k], acc);
         }
         sm = (sm == smem0) ? smem1 : smem0;
         return ++z < z1;
@@ -298,6 +330,9 @@ __device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T>
     constexpr int HP = RQ * PR * 2 + TY * RQ;  // halo pairs: top, bottom, then RQ / 2 per side per row
     constexpr int NH = (HP + NT - 1) / NT;
     constexpr int Q = 2 * RQ + 1;
+    constexpr int FY = TY + 2 * RQ;
+    const unsigned long long gp = (unsigned long long)g.n - 1;  // a pair at i needs i + 1 < n
+    (void)gp;
 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * 32 + tx;
@@ -354,7 +389,7 @@ __device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T>
         const unsigned base = zl * nxy;
 #pragma unroll
         for (int k = 0; k < NY; k++) {
-            const Two<T> v = op.fetch_pair(base + col[k]);
+            const Two<T> v = op.fetch_pair(LSG_IX(base + col[k], gp));
             q[k][s] = mk2<PT>(v.a, v.b);
         }
         zl = (zl + 1 == nz) ? 0u : zl + 1;
@@ -365,12 +400,12 @@ __device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T>
         const unsigned lb = zl * nxy, zb = (unsigned)z0 * nxy;
 #pragma unroll
         for (int k = 0; k < NY; k++) {
-            qn[k] = op.fetch_pair(lb + col[k]);
-            cn[k] = op.center_pair(zb + col[k]);
+            qn[k] = op.fetch_pair(LSG_IX(lb + col[k], gp));
+            cn[k] = op.center_pair(LSG_IX(zb + col[k], gp));
         }
 #pragma unroll
         for (int s = 0; s < NH; s++)
-            if (hs[s] >= 0) hn[s] = op.fetch_pair(zb + ho[s]);
+            if (hs[s] >= 0) hn[s] = op.fetch_pair(LSG_IX(zb + ho[s], gp));
         zl = (zl + 1 == nz) ? 0u : zl + 1;
     }
 
@@ -384,11 +419,11 @@ __device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T>
 #pragma unroll
         for (int k = 0; k < NY; k++) {
             q[k][HEAD] = mk2<PT>(qn[k].a, qn[k].b);
-            *reinterpret_cast<PT *>(sm + (RQ + ty * NY + k) * FX + RQ + 2 * tx) = q[k][CEN];
+            *reinterpret_cast<PT *>(sm + LSG_IX((RQ + ty * NY + k) * FX + RQ + 2 * tx, FX * FY - 1)) = q[k][CEN];
         }
 #pragma unroll
         for (int s = 0; s < NH; s++)
-            if (hs[s] >= 0) st_pair(sm + hs[s], hn[s].a, hn[s].b);
+            if (hs[s] >= 0) st_pair(sm + LSG_IX(hs[s], FX * FY - 1), hn[s].a, hn[s].b);
         Two<T> cc[NY];
 #pragma unroll
         for (int k = 0; k < NY; k++) cc[k] = cn[k];
@@ -396,12 +431,12 @@ __device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T>
             const unsigned lb = zl * nxy, nb = zbase + nxy;
 #pragma unroll
             for (int k = 0; k < NY; k++) {
-                qn[k] = op.fetch_pair(lb + col[k]);
-                cn[k] = op.center_pair(nb + col[k]);
+                qn[k] = op.fetch_pair(LSG_IX(lb + col[k], gp));
+                cn[k] = op.center_pair(LSG_IX(nb + col[k], gp));
             }
 #pragma unroll
             for (int s = 0; s < NH; s++)
-                if (hs[s] >= 0) hn[s] = op.fetch_pair(nb + ho[s]);
+                if (hs[s] >= 0) hn[s] = op.fetch_pair(LSG_IX(nb + ho[s], gp));
             zl = (zl + 1 == nz) ? 0u : zl + 1;
         }
         __syncthreads();
@@ -455,7 +490,7 @@ __device__ __forceinline__ void stencil_march_x2(const Geom &g, const Weights<T>
                 }
                 acc2 = mk2<PT>(aa, ab);
             }
-            if (valid[k])
+            if (valid[k] && LSG_IX_OK(zbase + col[k], gp))
                 op.store_pair(zbase + col[k], Two<T>{q[k][CEN].x, q[k][CEN].y}, Two<T>{acc2.x, acc2.y}, cc[k], acc);
         }
         sm = (sm == smem0) ? smem1 : smem0;

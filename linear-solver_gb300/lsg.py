@@ -98,7 +98,7 @@ EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "ls
            "lsg_profile", "lsg_profile_read", "lsg_set_compat_mode", "lsg_aar_mixed_c",
            "lsg_pinv_solve_noalloc", "lsg_aar_batched", "lsg_aar_mixed_batched", "lsg_autotune",
            "lsg_set_autotune", "lsg_autotune_save", "lsg_autotune_load", "lsg_gmres",
-           "lsg_aar_csr", "lsg_apply_csr", "lsg_register_operator_csr"]
+           "lsg_aar_csr", "lsg_apply_csr", "lsg_register_operator_csr", "lsg_bounds_errors"]
 
 KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "unused"]
 
@@ -140,6 +140,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
         L.lsg_set_autotune.argtypes = [ip]
         L.lsg_autotune_save.argtypes = [C.c_char_p]
         L.lsg_autotune_load.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
+        L.lsg_bounds_errors.argtypes = [C.POINTER(C.c_longlong)]
         for f in ("lsg_aar_batched", "lsg_aar_mixed_batched"):
             getattr(L, f).argtypes = [C.POINTER(_Operator), ip, C.POINTER(_Params), ip,
                                       C.POINTER(vp), C.POINTER(vp), C.POINTER(_Result), vp]
@@ -179,6 +180,14 @@ def _check(rc: int, what: str, allow=(0, 1, 2, 8)):
         msg = lib().lsg_last_error().decode(errors="replace")
         raise CudaLibraryError(f"{what}: {STATUS.get(rc, rc)}: {msg}")
     return rc
+
+
+def bounds_errors():
+    """Bounds-checked build: the first out-of-range index a stencil march met
+    (-1: none).  None for the normal build."""
+    v = C.c_longlong(-1)
+    rc = lib().lsg_bounds_errors(C.byref(v))
+    return None if rc == 6 else v.value
 
 
 def lap_coefficient(radius: int):
