@@ -47,6 +47,11 @@ def test_host_only_entry_points(lsg):
     op = lsg.Operator((9, 10, 11), radius=3, sigma=0.5)
     assert op.shape == (11, 10, 9)
     assert op.diag == pytest.approx(op.a * 3 * op.coeff[0] + 0.5)
+    assert L.lsg_status_string(5).decode() == "device wait timed out"
+    # the index checks exist only in the LSG_BOUNDS=1 build
+    variant = os.path.join(os.path.dirname(lsg.__file__), "_build", "liblsg.variant")
+    if not os.path.exists(variant) or open(variant).read().strip() == "normal":
+        assert lsg.bounds_errors() is None
 
 
 def test_bad_arguments_rejected_before_any_device_call(lsg):
