@@ -344,6 +344,8 @@ def run_lsg(args):
                      "peak_kind": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
                      "traffic": RICH32_TRAFFIC_BYTES, "traffic_unit": "bytes per launch (ncu)",
                      "bytes_per_launch": rich_bytes, "avg_launch_ms": rich_ms,
+                     "note": ("lean form: 4 vectors per launch (x left out; the x-carrying form moved 6 and ran "
+                              "at a higher fraction but slower); latency-bound at 16 warps/SM, see the profile"),
                      "share_of_kernel_time": rms / total_ms if total_ms else None},
         "kernel_profile_ms": {k: round(v[1], 4) for k, v in prof.items() if v[0]},
         "updates_per_s": {"mixed": N * infos[-1]["inner_iters"] / value, "fp64": N * i64["iters"] / fp64_s},
