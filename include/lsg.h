@@ -36,7 +36,9 @@ typedef enum lsg_status {
     LSG_TIMEOUT = 5,           /* a bounded device wait gave up */
     LSG_UNSUPPORTED = 6,       /* valid request this build does not serve */
     LSG_NO_MEMORY = 7,         /* device allocation failed */
-    LSG_SVD_NO_CONVERGENCE = 8 /* the m x m Jacobi SVD hit its sweep limit */
+    LSG_SVD_NO_CONVERGENCE = 8,/* the m x m Jacobi SVD hit its sweep limit */
+    LSG_RANGE = 9              /* an FP64 stencil input exceeded the double-float range
+                                  (|u| >= 2^127 ||b||); repeat with lsg_set_fp64_arith(1) */
 } lsg_status;
 
 typedef enum lsg_dtype {
@@ -101,6 +103,17 @@ int lsg_operator_init(lsg_operator *op, int nx, int ny, int nz, int radius, doub
 /* Reference parameter defaults: omega = beta = 0.6, m = 7, p = 6, tol = 1e-8,
  * max_iter = 100000 (MPI_REAL/main.c:37, README:18-21). */
 void lsg_params_default(lsg_params *prm);
+
+/* Arithmetic of the FP64 stencil passes inside the solvers.  0 (default):
+ * double-float -- each double is split into two floats and the 37-point sums
+ * run on the FP32 pipe with error-free transformations (result within ~2^-48
+ * of sum |w_p| |u|, FP64's own rounding being ~2^-53 of it), because GB300
+ * executes FP64 at ~1/64 of its FP32 rate.  Solves asking for tol < 1e-10
+ * use FP64 arithmetic regardless (the double-float residual floor is near
+ * 1e-13).  1: FP64 arithmetic throughout.  The environment variable
+ * LSG_FP64_ARITH=1 sets 1 at load.  Returns the previous mode.  lsg_apply
+ * always uses FP64 arithmetic. */
+int lsg_set_fp64_arith(int mode);
 
 /* y = A x on the device (replaces MPI_REAL/system.c:80-213). */
 int lsg_apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, void *stream);

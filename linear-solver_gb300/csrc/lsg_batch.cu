@@ -328,6 +328,7 @@ struct BatchRun {
         a.beta = prm->beta;
         a.gate = gate;
         a.lean = IsRecur<T>::value && prm->p - 1 <= prm->m;
+        a.exact = fp64_exact_for(prm->tol);
         return a;
     }
     const BInst<T> *tab() const { return (const BInst<T> *)ws->d_inst; }
@@ -696,6 +697,7 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
         const bool ok = o.done && !o.stalled && !(o.relres > o.tol_abs) && o.status != LSG_NAN_DETECTED;
         r.iters = o.done ? o.iters : prm->max_iter;
         if (o.status == LSG_NAN_DETECTED || c.status == LSG_NAN_DETECTED) r.status = LSG_NAN_DETECTED;
+        else if (o.df_range || c.df_range) r.status = LSG_RANGE;
         else if (ok) r.status = LSG_OK;
         else r.status = (c.status == LSG_SVD_NO_CONVERGENCE) ? LSG_SVD_NO_CONVERGENCE : LSG_NOT_CONVERGED;
         if (mixed) {

@@ -149,7 +149,7 @@ struct PassIrResidual {  // r = float(b64 - A x64) after iteration it (mixed sol
     __device__ static bool make(const BInst<T> &I, const BCtl &C, const BArgs &a, Op &op) {
         if (!replace_gate(C, a)) return false;
         const int it = batch_iter(a);
-        op = Op{I.x64, I.b64, rcur(I, a, it), C.part, nullptr};
+        op = Op{I.x64, I.b64, rcur(I, a, it), C.part, C.octrl};
         return true;
     }
     __device__ static Weights<TS> weights(const BInst<T> &I) { return I.w64; }
@@ -157,12 +157,13 @@ struct PassIrResidual {  // r = float(b64 - A x64) after iteration it (mixed sol
 
 // ---------------------------------------------------------------- kernels
 
-template <typename T, int RQ, int BY, int NY, int MINB, bool GENERIC, class Pass>
+// DFM: FP64 passes in double-float arithmetic (stencil_march_df).
+template <typename T, int RQ, int BY, int NY, int MINB, bool GENERIC, class Pass, bool DFM = false>
 __global__ void __launch_bounds__(32 * BY, MINB) batch_stencil_kernel(const BInst<T> *tab, BArgs a) {
     using TS = typename Pass::TS;
     constexpr int FX = 32 + 2 * RQ;
     constexpr int FY = BY * NY + 2 * RQ;
-    __shared__ TS smem[2][FX * FY];
+    __shared__ __align__(16) TS smem[2][FX * FY];
     const int i = a.map[blockIdx.x];
     const BCtl &C = a.ctl[i];
     const BInst<T> &I = tab[i];
@@ -173,8 +174,13 @@ __global__ void __launch_bounds__(32 * BY, MINB) batch_stencil_kernel(const BIns
     const int lb = blockIdx.x - C.sblk0;
     const int t = lb / I.tx;
     const Weights<TS> w = Pass::weights(I);
-    stencil_march<TS, RQ, BY, NY, GENERIC>(I.g, w, I.lz, op, smem[0], smem[1], lb - t * I.tx, t % I.ty,
-                                           t / I.ty, lb);
+    if constexpr (DFM && std::is_same<TS, double>::value) {
+        stencil_march_df<RQ, BY, NY, GENERIC>(I.g, w, I.lz, op, smem[0], smem[1], lb - t * I.tx, t % I.ty,
+                                              t / I.ty, lb);
+    } else {
+        stencil_march<TS, RQ, BY, NY, GENERIC>(I.g, w, I.lz, op, smem[0], smem[1], lb - t * I.tx, t % I.ty,
+                                               t / I.ty, lb);
+    }
 }
 
 // Batched stencil tile: tile variant V of the vector type (the refinement
@@ -191,6 +197,12 @@ template <typename T, int V, class Pass>
 cudaError_t launch_batch_var(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s) {
     using Tl = BTile<T, V, false>;
     constexpr int MB = Pass::MINB == 0 ? Tl::MINB : Pass::MINB;
+    if constexpr (DfOk<typename Pass::Op>::value) {
+        if (!a.exact) {
+            batch_stencil_kernel<T, 6, Tl::BY, Tl::NY, MB, false, Pass, true><<<grid, dim3(32, Tl::BY), 0, s>>>(tab, a);
+            return cudaGetLastError();
+        }
+    }
     batch_stencil_kernel<T, 6, Tl::BY, Tl::NY, MB, false, Pass><<<grid, dim3(32, Tl::BY), 0, s>>>(tab, a);
     return cudaGetLastError();
 }
@@ -205,6 +217,13 @@ cudaError_t launch_batch_stencil(const BInst<T> *tab, const BArgs &a, int grid, 
         return launch_batch_var<T, 0, Pass>(tab, a, grid, s);
     }
     using Tl = BTile<T, 0, true>;
+    if constexpr (DfOk<typename Pass::Op>::value) {
+        if (!a.exact) {
+            batch_stencil_kernel<T, LSG_MAX_RADIUS, Tl::BY, Tl::NY, 1, true, Pass, true>
+                <<<grid, dim3(32, Tl::BY), 0, s>>>(tab, a);
+            return cudaGetLastError();
+        }
+    }
     batch_stencil_kernel<T, LSG_MAX_RADIUS, Tl::BY, Tl::NY, 1, true, Pass><<<grid, dim3(32, Tl::BY), 0, s>>>(tab, a);
     return cudaGetLastError();
 }
@@ -430,7 +449,8 @@ static int batch_rich_occupancy() {
     using Tl = BTile<T, V, GENERIC>;
     int n = 0;
     const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &n, batch_stencil_kernel<T, GENERIC ? LSG_MAX_RADIUS : 6, Tl::BY, Tl::NY, Tl::MINB, GENERIC, P>,
+        &n, batch_stencil_kernel<T, GENERIC ? LSG_MAX_RADIUS : 6, Tl::BY, Tl::NY, Tl::MINB, GENERIC, P,
+                                 DfOk<typename P::Op>::value>,
         32 * Tl::BY, 0);
     if (e != cudaSuccess || n < 1) {
         cudaGetLastError();

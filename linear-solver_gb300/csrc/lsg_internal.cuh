@@ -8,6 +8,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <string.h>
 
 #include "../../include/lsg.h"
@@ -40,6 +41,7 @@ struct DevCtrl {
     double tol_frac;  // mixed solves (outer block): the next run's floor, as a fraction of tol_abs
     int floor_misses; // mixed solves (outer block): consecutive runs that reached the floor, true residual > tol
     int x_zero;       // mixed solves (outer block): the initial x64 was exactly zero
+    int df_range;     // FP64 double-float stencil: a value beyond the float range was split
     double bmean[2];  // mixed solves (outer block): mean of b (re, im)
     double shift[2];  // mixed solves (outer block): constant added to x64 by the last deflation
     double s[LSG_MAX_M];  // m x m solve output
@@ -98,7 +100,21 @@ template <typename T>
 struct Weights {
     T w[LSG_MAX_RADIUS + 1];
     int radius;
+    // FP64 weights as three floats w = w1 + w2 + w3 (exactly: 72 >= 53 bits)
+    // for the double-float march (zero for the other vector types)
+    float wf[3 * (LSG_MAX_RADIUS + 1)];
 };
+
+// Three floats whose sum is exactly the double w (each the float nearest the
+// remainder left by the previous ones).
+inline void split3(double w, float *out) {
+    const float a = (float)w;
+    const double r1 = w - (double)a;
+    const float b = (float)r1;
+    out[0] = a;
+    out[1] = b;
+    out[2] = (float)(r1 - (double)b);
+}
 
 // Host: weights and Jacobi factor of an operator in a vector type.
 template <typename T>
@@ -112,8 +128,17 @@ inline Weights<T> make_weights(const lsg_operator *op) {
     } else {
         w.w[0] = (T)(op->a * 3.0 * op->coeff[0] + op->sigma);
         for (int p = 1; p <= op->radius; p++) w.w[p] = (T)(op->a * op->coeff[p]);
+        if constexpr (std::is_same<T, double>::value)
+            for (int p = 0; p <= op->radius; p++) split3(w.w[p], w.wf + 3 * p);
     }
     return w;
+}
+
+// Re-derives the three-float weights after w.w changed.
+template <typename T>
+inline void refresh_df_weights(Weights<T> &w) {
+    if constexpr (std::is_same<T, double>::value)
+        for (int p = 0; p <= LSG_MAX_RADIUS; p++) split3(w.w[p], w.wf + 3 * p);
 }
 
 // Jacobi factor cf = 1 / diag (or 1 without preconditioning), in the
@@ -145,6 +170,13 @@ StencilLaunch rich_launch(const lsg_operator *op, const StencilLaunch &L);
 
 // Host helpers of lsg_solvers.cu.
 int sm_count();
+// 1: FP64 stencil passes in FP64 arithmetic (lsg_set_fp64_arith); 0: double-float.
+int fp64_exact();
+// The same for a solve to relative tolerance tol: the double-float sums leave
+// a residual floor near 1e-13, so solves asking for less than kDfMinTol take
+// the FP64-arithmetic march.
+constexpr double kDfMinTol = 1e-10;
+int fp64_exact_for(double tol);
 int check_params(const lsg_params *prm, bool history);
 // Initial control block: relres = tol + 1 (AAR.c:76), stall rule off (0) or on.
 DevCtrl ctrl_init(double tol, int stall_limit);
@@ -218,13 +250,14 @@ struct StencilLaunch {
     int paired = -1;  // 1: the two-columns-per-lane march (planned by Kernels<T>::paired_plan);
                       // 2: its 64 x 8 shape (passes without partial sums only);
                       // -1: the solver may choose it; 0: not
+    int exact = 0;    // FP64 passes: 1 = FP64-arithmetic march, 0 = the double-float one
 };
 
 // Tile shape per vector type: FP64 is ALU-bound (narrower tile, fewer live
 // registers); FP32 is bandwidth-bound (taller tile, less halo per point).
 // A block is 32 x BY threads covering 32 x (BY*NY) columns.
 template <typename T> struct TileOf;
-template <> struct TileOf<double> { static constexpr int BY = 8, NY = 2, MINB = 1; };
+template <> struct TileOf<double> { static constexpr int BY = 8, NY = 1, MINB = 2; };
 template <> struct TileOf<float> { static constexpr int BY = 4, NY = 4, MINB = 4; };
 template <> struct TileOf<cplx<double>> { static constexpr int BY = 8, NY = 1, MINB = 1; };
 template <> struct TileOf<cplx<float>> { static constexpr int BY = 8, NY = 2, MINB = 2; };
@@ -241,9 +274,9 @@ constexpr int kPairBY = 8, kPairNY = 2, kPairMINB = 2;  // its block: 32 x 8 thr
 constexpr int kTilePaired2 = 4;
 constexpr int kPair2BY = 4, kPair2NY = 2, kPair2MINB = 4;
 template <typename T, int V> struct TileVar;
-template <> struct TileVar<double, 0> { static constexpr int BY = 8, NY = 2, MINB = 1; };
-template <> struct TileVar<double, 1> { static constexpr int BY = 4, NY = 4, MINB = 1; };
-template <> struct TileVar<double, 2> { static constexpr int BY = 8, NY = 1, MINB = 2; };
+template <> struct TileVar<double, 0> { static constexpr int BY = 8, NY = 1, MINB = 2; };
+template <> struct TileVar<double, 1> { static constexpr int BY = 16, NY = 1, MINB = 1; };
+template <> struct TileVar<double, 2> { static constexpr int BY = 8, NY = 1, MINB = 3; };
 template <> struct TileVar<float, 0> { static constexpr int BY = 4, NY = 4, MINB = 4; };
 template <> struct TileVar<float, 1> { static constexpr int BY = 8, NY = 2, MINB = 2; };
 template <> struct TileVar<float, 2> { static constexpr int BY = 4, NY = 2, MINB = 4; };
@@ -542,6 +575,7 @@ struct BArgs {
     double beta;
     int gate;            // refinement passes: 0 = paused instances, 1 = every unfinished one
     int lean;            // FP32: the Richardson passes leave x out (p - 1 <= m)
+    int exact;           // FP64 stencil passes: 1 = FP64-arithmetic march (double-float otherwise)
 };
 
 template <typename T>

@@ -47,6 +47,9 @@ template <typename T> struct Triple { T a, b, c; };
 template <typename T, int MODE>
 struct ResidualOp {
     static constexpr int NACC = (MODE == RES_APPLY) ? 0 : 1;
+    // FP64 solves evaluate the sums in double-float; y = A x (lsg_apply, used
+    // to check results) keeps FP64 arithmetic
+    static constexpr bool DF = std::is_same<T, double>::value && MODE != RES_APPLY;
     using Raw = T;
     using Ctr = typename std::conditional<MODE == RES_ANDERSON, Triple<T>,
                 typename std::conditional<MODE == RES_INIT, T, NoCtr>::type>::type;
@@ -59,14 +62,37 @@ struct ResidualOp {
     T hb;
     double *partials;
     const DevCtrl *ctrl;
+    float2 cfp;  // cf as a double-float pair (double-float march)
     __device__ bool skip() const { return solve_done(ctrl); }
-    __device__ void init() {}
+    __device__ void init() {
+        if constexpr (DF) cfp = df_weight((double)cf);
+    }
     __device__ __forceinline__ Raw fetch(unsigned i) const { return ldg(x + i); }
     __device__ __forceinline__ T value(const Raw &v) const { return v; }
     __device__ __forceinline__ Ctr fetch_center(unsigned i) const {
         if constexpr (MODE == RES_ANDERSON) return Ctr{ldg(b + i), r[i], hc[i]};
         else if constexpr (MODE == RES_INIT) return ldg(b + i);
         else return Ctr{};
+    }
+    // Double-float epilogue: r_new = b - Au and DF formed from pairs, each
+    // rounded to a double once.
+    static constexpr bool STORE_DF = DF;
+    __device__ __forceinline__ void store_df(unsigned i, float2, float2 au, const Ctr &c, int k,
+                                             Acc<T> *acc) const {
+        bool nb = false;
+        if constexpr (MODE == RES_INIT) {
+            const double rn = df_to_double(df_sub(df_split(c, k, nb), au), k);
+            r[i] = rn;
+            acc[0].add_prod(rn, rn);
+        } else if constexpr (MODE == RES_ANDERSON) {
+            const float2 rn = df_sub(df_split(c.a, k, nb), au);
+            const double dfv = df_to_double(df_mul(df_sub(rn, df_split(c.b, k, nb)), cfp), k);
+            const double rnd = df_to_double(rn, k);
+            df[i] = dfv;
+            hc[i] = fma(hb, dfv, c.c);
+            r[i] = rnd;
+            acc[0].add_prod(rnd, rnd);
+        }
     }
     __device__ __forceinline__ void store(unsigned i, T u, T au, const Ctr &c, Acc<T> *acc) const {
         if constexpr (MODE == RES_APPLY) {
@@ -95,6 +121,7 @@ struct ResidualOp {
 template <typename T, int MODE>
 struct RichOp {
     static constexpr int NACC = 0;
+    static constexpr bool DF = std::is_same<T, double>::value;
     using Raw = Pair<T>;    // (x, r)
     using Ctr = Triple<T>;  // (b, x, r) at the centre
     const T *x;
@@ -109,10 +136,22 @@ struct RichOp {
     T hb;  // beta (AAR) or 0
     double *partials;
     const DevCtrl *ctrl;
+    float2 cp, cfp, hbp;  // c, cf, hb as double-float pairs (double-float march)
     __device__ bool skip() const { return solve_done(ctrl); }
-    __device__ void init() {}
+    __device__ void init() {
+        if constexpr (DF) {
+            cp = df_weight((double)c);
+            cfp = df_weight((double)cf);
+            hbp = df_weight((double)hb);
+        }
+    }
     __device__ __forceinline__ Raw fetch(unsigned i) const { return Raw{ldg(x + i), ldg(r + i)}; }
     __device__ __forceinline__ T value(const Raw &v) const { return fma(c, v.b, v.a); }
+    // u = x + c r from the split operands (double-float march; no FP64 operation)
+    static constexpr bool VALUE_DF = DF;
+    __device__ __forceinline__ float2 value_df(const Raw &v, int k, bool &bad) const {
+        return df_add2(df_split(v.a, k, bad), df_mul(df_split(v.b, k, bad), cp));
+    }
     __device__ __forceinline__ Ctr fetch_center(unsigned i) const {
         return Ctr{ldg(b + i), ldg(x + i), ldg(r + i)};
     }
@@ -123,6 +162,22 @@ struct RichOp {
         r2[i] = rn;
         dx[i] = fma(hb, dfv, u - cc.b);
         df[i] = dfv;
+    }
+    // Double-float epilogue: x2 = x + c r in FP64 (the reference's update);
+    // r2 = b - Au, DF and the history column c r + hb DF (x2 - x + hb DF in
+    // exact arithmetic) from double-float pairs, each rounded to a double once.
+    static constexpr bool STORE_DF = DF;
+    __device__ __forceinline__ void store_df(unsigned i, float2, float2 au, const Ctr &cc, int k,
+                                             Acc<T> *) const {
+        bool nb = false;
+        const float2 rd = df_split(cc.c, k, nb);
+        const float2 rn = df_sub(df_split(cc.a, k, nb), au);
+        const float2 dfv = (MODE == RICH_AAR) ? df_mul(df_sub(rn, rd), cfp) : df_sub(rd, rn);
+        const float2 dxv = df_add(df_mul(rd, cp), df_mul(dfv, hbp));
+        x2[i] = fma(c, cc.c, cc.b);
+        r2[i] = df_to_double(rn, k);
+        dx[i] = df_to_double(dxv, k);
+        df[i] = df_to_double(dfv, k);
     }
 };
 
@@ -277,6 +332,7 @@ struct ResRecurOp {
 template <typename T>
 struct CgDirOp {
     static constexpr int NACC = 1;
+    static constexpr bool DF = std::is_same<T, double>::value;
     using Raw = Pair<T>;  // (r, d_old)
     using Ctr = NoCtr;
     const T *r;
@@ -287,10 +343,23 @@ struct CgDirOp {
     T beta;
     double *partials;
     const DevCtrl *ctrl;
+    float2 cfp, betap;  // cf, beta as double-float pairs (double-float march)
     __device__ bool skip() const { return solve_done(ctrl); }
-    __device__ void init() { beta = (T)ctrl->beta; }
+    __device__ void init() {
+        beta = (T)ctrl->beta;
+        if constexpr (DF) {
+            cfp = df_weight((double)cf);
+            betap = df_weight((double)beta);
+        }
+    }
     __device__ __forceinline__ Raw fetch(unsigned i) const { return Raw{ldg(r + i), ldg(d_old + i)}; }
     __device__ __forceinline__ T value(const Raw &v) const { return fma(beta, v.b, cf * v.a); }
+    // d = cf r + beta d_old from the split operands (double-float march); the
+    // stored direction is the pair the sums used, rounded once
+    static constexpr bool VALUE_DF = DF;
+    __device__ __forceinline__ float2 value_df(const Raw &v, int k, bool &bad) const {
+        return df_add2(df_mul(df_split(v.a, k, bad), cfp), df_mul(df_split(v.b, k, bad), betap));
+    }
     __device__ __forceinline__ Ctr fetch_center(unsigned) const { return Ctr{}; }
     __device__ __forceinline__ void store(unsigned i, T u, T au, const Ctr &, Acc<T> *acc) const {
         d_new[i] = u;
@@ -304,6 +373,7 @@ struct CgDirOp {
 template <typename T64, typename T32>
 struct IrResidualOp {
     static constexpr int NACC = 1;
+    static constexpr bool DF = std::is_same<T64, double>::value;
     using Raw = T64;
     using Ctr = T64;  // b
     const T64 *x;
@@ -321,6 +391,16 @@ struct IrResidualOp {
         const T64 rn = bb - au;
         r32[i] = (T32)rn;
         acc[0].add_prod(rn, rn);
+    }
+    static constexpr bool STORE_DF = DF;
+    __device__ __forceinline__ void store_df(unsigned i, float2, float2 au, const Ctr &bb, int k,
+                                             Acc<T64> *acc) const {
+        if constexpr (DF) {
+            bool nb = false;
+            const double rn = df_to_double(df_sub(df_split(bb, k, nb), au), k);
+            r32[i] = (T32)rn;
+            acc[0].add_prod(rn, rn);
+        }
     }
 };
 
@@ -401,6 +481,12 @@ template <typename T, int V, class Op>
 cudaError_t launch_stencil_var(const StencilLaunch &L, const Weights<T> &w, const Op &op) {
     constexpr int BY = TileVar<T, V>::BY, NY = TileVar<T, V>::NY, MB = TileVar<T, V>::MINB;
     const dim3 grid = stencil_grid(L.g, BY * NY, L.lz);
+    if constexpr (DfOk<Op>::value) {
+        if (!L.exact) {
+            stencil_kernel<T, 6, BY, NY, MB, false, Op, true><<<grid, dim3(32, BY), 0, L.stream>>>(L.g, w, L.lz, op);
+            return cudaGetLastError();
+        }
+    }
     stencil_kernel<T, 6, BY, NY, MB, false, Op><<<grid, dim3(32, BY), 0, L.stream>>>(L.g, w, L.lz, op);
     return cudaGetLastError();
 }
@@ -431,6 +517,13 @@ cudaError_t launch_stencil(const StencilLaunch &L, const Weights<T> &w, const Op
         return launch_stencil_var<T, 0>(L, w, op);
     }
     const dim3 grid = stencil_grid(L.g, BY * NY, L.lz);
+    if constexpr (DfOk<Op>::value) {
+        if (!L.exact) {
+            stencil_kernel<T, LSG_MAX_RADIUS, BY, NY, 1, true, Op, true>
+                <<<grid, dim3(32, BY), 0, L.stream>>>(L.g, w, L.lz, op);
+            return cudaGetLastError();
+        }
+    }
     stencil_kernel<T, LSG_MAX_RADIUS, BY, NY, 1, true, Op><<<grid, dim3(32, BY), 0, L.stream>>>(L.g, w, L.lz, op);
     return cudaGetLastError();
 }
@@ -443,7 +536,7 @@ static int rich_blocks_per_sm() {
                                          RichOp<T, RICH_AAR>>::type;
     int n = 0;
     const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &n, stencil_kernel<T, 6, Tl::BY, Tl::NY, Tl::MINB, false, Op>, 32 * Tl::BY, 0);
+        &n, stencil_kernel<T, 6, Tl::BY, Tl::NY, Tl::MINB, false, Op, DfOk<Op>::value>, 32 * Tl::BY, 0);
     if (e != cudaSuccess || n < 1) {
         cudaGetLastError();
         n = 1;

@@ -287,7 +287,8 @@ static int gmres_t(const lsg_operator *op, const lsg_params *prm, T *x, const T 
     const int sms = sm_count();
     const int rb = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4LL * sms));
     const int nchunk = (m + 1 + kDotChunk - 1) / kDotChunk;
-    const StencilLaunch L{g, choose_lz<T>(g, sms * Kernels<T>::stencil_blocks_per_sm()), s};
+    StencilLaunch L{g, choose_lz<T>(g, sms * Kernels<T>::stencil_blocks_per_sm()), s};
+    L.exact = fp64_exact_for(prm->tol);
     const long long sb = stencil_blocks<T>(g, L.lz);
     int dev = 0;
     cudaGetDevice(&dev);
@@ -329,6 +330,7 @@ static int gmres_t(const lsg_operator *op, const lsg_params *prm, T *x, const T 
     const double cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
     Weights<T> wcf = w;  // weights of cf A
     for (int p = 0; p <= op->radius; p++) wcf.w[p] = (T)(cf * (double)w.w[p]);
+    refresh_df_weights(wcf);
     const double acf = std::fabs(cf);
     long long launches = 0;
 
@@ -400,6 +402,7 @@ static int gmres_t(const lsg_operator *op, const lsg_params *prm, T *x, const T 
     r.rhs_norm = hc.rhs_norm;
     r.relres = hc.rhs_norm > 0 ? hc.relres / hc.rhs_norm : hc.relres;
     if (hc.status == LSG_NAN_DETECTED) r.status = LSG_NAN_DETECTED;
+    else if (hc.df_range) r.status = LSG_RANGE;
     else if (hc.done && !(hc.relres > hc.tol_abs)) r.status = LSG_OK;
     else r.status = LSG_NOT_CONVERGED;
     r.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count() - t0;

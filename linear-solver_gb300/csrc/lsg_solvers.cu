@@ -15,6 +15,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdarg>
 #include <cmath>
@@ -58,6 +59,16 @@ const char *last_error() { return t_last_error; }
             return set_error(e_ == cudaErrorMemoryAllocation ? LSG_NO_MEMORY : LSG_CUDA_ERROR, \
                              "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
+
+// ---------------------------------------------------------------- FP64 stencil arithmetic
+
+// 0: double-float sums on the FP32 pipe (default); 1: FP64 arithmetic.
+static std::atomic<int> g_fp64_arith{[] {
+    const char *e = getenv("LSG_FP64_ARITH");
+    return (e && e[0] == '1') ? 1 : 0;
+}()};
+int fp64_exact() { return g_fp64_arith.load(std::memory_order_relaxed); }
+int fp64_exact_for(double tol) { return (fp64_exact() || tol < kDfMinTol) ? 1 : 0; }
 
 // ---------------------------------------------------------------- device info
 
@@ -427,6 +438,7 @@ static void fill_result(lsg_result *res, const DevCtrl &c, int max_iter, double 
     res->rhs_norm = c.rhs_norm;
     res->relres = c.rhs_norm > 0 ? c.relres / c.rhs_norm : c.relres;
     if (c.status == LSG_NAN_DETECTED) res->status = LSG_NAN_DETECTED;
+    else if (c.df_range) res->status = LSG_RANGE;
     else if (c.status == LSG_TIMEOUT) res->status = LSG_TIMEOUT;
     else if (c.done && !c.stalled && !(c.relres > c.tol_abs)) res->status = LSG_OK;
     else res->status = (c.status == LSG_SVD_NO_CONVERGENCE) ? LSG_SVD_NO_CONVERGENCE : LSG_NOT_CONVERGED;
@@ -493,6 +505,7 @@ struct AarLoop {
         cf = jacobi_factor<T>(op);
         const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
         L = StencilLaunch{g, lz, R.s};  // paired -1: untuned
+        L.exact = fp64_exact_for(prm->tol);
         Lr = rich_launch<T>(op, L);      // a tuned shape sets paired to 0 (classic) or 1
         L.paired = 0;
         Lres = L;
@@ -649,7 +662,8 @@ int prich_core(Run &R, bool galerkin, const lsg_operator *op, const lsg_params *
     const Weights<T> w = make_weights<T>(op);
     const double cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
     const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
-    const StencilLaunch L{g, lz, R.s};
+    StencilLaunch L{g, lz, R.s};
+    L.exact = fp64_exact_for(prm->tol);
     StencilLaunch Lr = rich_launch<T>(op, L);
     if (Lr.paired >= 1) Lr = L;  // the paired march serves the AAR recurrence passes only
     Lr.paired = 0;
@@ -707,7 +721,8 @@ int cg_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const T
     const Weights<T> w = make_weights<T>(op);
     const double cf = op->precond ? 1.0 / jacobi_diag(op) : 1.0;
     const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
-    const StencilLaunch L{g, lz, R.s};
+    StencilLaunch L{g, lz, R.s};
+    L.exact = fp64_exact_for(prm->tol);
     const int sb = (int)stencil_blocks<T>(g, lz);
     const int rb = reduce_blocks(n, R.sms);
     T *r = (T *)ws->r0;
@@ -841,7 +856,8 @@ int solve_mixed_t(const lsg_operator *op, const lsg_params *prm, T64 *x, const T
     Run R(s, sm_count());
     const Weights<T64> w64 = make_weights<T64>(op);
     const int lz = choose_lz<T64>(g, stencil_slots<T64>(R.sms));
-    const StencilLaunch L64{g, lz, s};
+    StencilLaunch L64{g, lz, s};
+    L64.exact = fp64_exact_for(prm->tol);
     const int sb64 = (int)stencil_blocks<T64>(g, lz);
     const int rb = reduce_blocks(n, R.sms);
     DevCtrl *octrl = wo->ctrl;
@@ -890,6 +906,7 @@ int solve_mixed_t(const lsg_operator *op, const lsg_params *prm, T64 *x, const T
         LSG_CUDA(cudaStreamSynchronize(s));
         co = wo->hctrl[0];
         if (co.status == LSG_NAN_DETECTED) { status = LSG_NAN_DETECTED; break; }
+        if (co.df_range) { status = LSG_RANGE; break; }
         if (co.done) { status = LSG_OK; break; }
         if (it > prm->max_iter || replacements >= max_outer) break;
         // resume (or start) the FP32 iteration with its next pause target
@@ -1293,10 +1310,13 @@ const char *lsg_status_string(int st) {
     case LSG_UNSUPPORTED: return "unsupported";
     case LSG_NO_MEMORY: return "out of device memory";
     case LSG_SVD_NO_CONVERGENCE: return "SVD sweep limit reached";
+    case LSG_RANGE: return "value beyond the double-float stencil range";
     default: return "unknown status";
     }
 }
 
 const char *lsg_version(void) { return "lsg 0.1 (sm_103a)"; }
+
+int lsg_set_fp64_arith(int mode) { return lsg::g_fp64_arith.exchange(mode ? 1 : 0); }
 
 }  // extern "C"

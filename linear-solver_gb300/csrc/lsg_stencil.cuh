@@ -34,6 +34,7 @@
 #include "lsg_internal.cuh"
 #include "lsg_accum.cuh"
 #include "lsg_complex.cuh"
+#include "lsg_df.cuh"
 
 namespace lsg {
 
@@ -251,16 +252,237 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
     }
 }
 
-template <typename T, int RQ, int BY, int NY, int MINB, bool GENERIC, class Op>
+// ---------------------------------------------------------------- FP64 in double-float
+//
+// The march above for FP64 vectors with the sums evaluated in double-float
+// arithmetic on the FP32 pipe (lsg_df.cuh): the register ring and the staged
+// plane hold (hi, lo) float pairs, formed once per value with integer and
+// FP32 operations; Au is formed with error-free TwoSum / FMA two-product
+// steps.  Each point's sum is evaluated in the same order in every tile
+// shape, so results do not depend on the launch shape.  Functors opt in with
+// DF = true and carry the solve's control block (the split's scale 2^k comes
+// from its ||b||; a value beyond the float range sets its df_range flag).
+// The ring advances by register moves instead of a Q-fold unrolled march:
+// one double-float step is ~10x an FP32 step in code, and the unrolled march
+// overflows the instruction cache.
+
+template <class Op, class = void> struct DfOk { static constexpr bool value = false; };
+template <class Op> struct DfOk<Op, std::void_t<decltype(Op::DF)>> { static constexpr bool value = Op::DF; };
+
+template <class Op>
+__device__ __forceinline__ int df_shift_of(const Op &op) {
+    return op.ctrl ? df_shift_for(op.ctrl->rhs_norm) : 0;
+}
+
+// VALUE_DF: the functor forms u from its operands in double-float arithmetic
+// (value_df(raw, k, bad) -> the pair of u 2^k); the others return a double
+// that the march splits.
+template <class Op, class = void> struct HasValueDf { static constexpr bool value = false; };
+template <class Op>
+struct HasValueDf<Op, std::void_t<decltype(Op::VALUE_DF)>> { static constexpr bool value = Op::VALUE_DF; };
+
+template <class Op, class Raw>
+__device__ __forceinline__ float2 df_value(const Op &op, const Raw &v, int k, bool &bad) {
+    if constexpr (HasValueDf<Op>::value) return op.value_df(v, k, bad);
+    else return df_split(op.value(v), k, bad);
+}
+
+// STORE_DF: the functor's epilogue takes the centre u and Au as pairs scaled
+// by 2^k (store_df(idx, u, Au, ctr, k, acc)); the others get doubles.
+template <class Op, class = void> struct HasStoreDf { static constexpr bool value = false; };
+template <class Op>
+struct HasStoreDf<Op, std::void_t<decltype(Op::STORE_DF)>> { static constexpr bool value = Op::STORE_DF; };
+
+template <int RQ, int BY, int NY, bool GENERIC, class Op>
+__device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<double> &w, int lz, Op &op,
+                                                 double *smem0d, double *smem1d, int bx, int by, int bz,
+                                                 long long blk) {
+    using Raw = typename Op::Raw;
+    using Ctr = typename Op::Ctr;
+    constexpr int TX = 32;
+    constexpr int TY = BY * NY;
+    constexpr int FX = TX + 2 * RQ;
+    constexpr int NT = 32 * BY;
+    constexpr int H = 2 * RQ * TX + TY * 2 * RQ;  // halo cells of one plane (no corners)
+    constexpr int NH = (H + NT - 1) / NT;
+    constexpr int Q = 2 * RQ + 1;
+    constexpr int FY = TY + 2 * RQ;
+    const unsigned long long gn = (unsigned long long)g.n;
+    (void)gn;
+    float2 *const smem0 = reinterpret_cast<float2 *>(smem0d);
+    float2 *const smem1 = reinterpret_cast<float2 *>(smem1d);
+
+    const int radius = GENERIC ? w.radius : RQ;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * 32 + tx;
+    const int x0 = bx * TX, y0 = by * TY;
+    const int z0 = bz * lz;
+    const int z1 = min(z0 + lz, g.nz);
+    const int ks = df_shift_of(op);
+    bool bad = false;
+
+    const int gx = wrap_index(x0 + tx, g.nx);
+    int col[NY];
+    bool valid[NY];
+#pragma unroll
+    for (int k = 0; k < NY; k++) {
+        const int yy = y0 + ty * NY + k;
+        col[k] = gx + wrap_index(yy, g.ny) * g.nx;
+        valid[k] = (x0 + tx < g.nx) && (yy < g.ny);
+    }
+    int hs[NH], ho[NH];
+#pragma unroll
+    for (int s = 0; s < NH; s++) {
+        const int h = tid + s * NT;
+        hs[s] = -1;
+        ho[s] = 0;
+        if (h < H) {
+            int fy, fx;
+            if (h < RQ * TX) {
+                fy = h / TX; fx = RQ + h % TX;
+            } else if (h < 2 * RQ * TX) {
+                const int hh = h - RQ * TX;
+                fy = RQ + TY + hh / TX; fx = RQ + hh % TX;
+            } else {
+                const int hh = h - 2 * RQ * TX;
+                const int row = hh / (2 * RQ), c = hh % (2 * RQ);
+                fy = RQ + row;
+                fx = c < RQ ? c : TX + c;
+            }
+            hs[s] = fy * FX + fx;
+            ho[s] = wrap_index(x0 - RQ + fx, g.nx) + wrap_index(y0 - RQ + fy, g.ny) * g.nx;
+        }
+    }
+
+    Acc<double> acc[Op::NACC > 0 ? Op::NACC : 1];
+#pragma unroll
+    for (int a = 0; a < (Op::NACC > 0 ? Op::NACC : 1); a++) acc[a].zero();
+
+    // ring: q[k][j] holds plane z - RQ + j at the step of plane z
+    float2 q[NY][Q];
+    unsigned zl = (unsigned)wrap_index(z0 - RQ, g.nz);
+    const unsigned nxy = (unsigned)g.nxy, nz = (unsigned)g.nz;
+#pragma unroll
+    for (int s = 0; s < 2 * RQ; s++) {
+        const unsigned base = zl * nxy;
+#pragma unroll
+        for (int k = 0; k < NY; k++) q[k][s] = df_value(op, op.fetch(LSG_IX(base + col[k], gn)), ks, bad);
+        zl = (zl + 1 == nz) ? 0u : zl + 1;
+    }
+    Raw qn[NY], hn[NH];
+    Ctr cn[NY];
+    {
+        const unsigned lb = zl * nxy, zb = (unsigned)z0 * nxy;
+#pragma unroll
+        for (int k = 0; k < NY; k++) {
+            qn[k] = op.fetch(LSG_IX(lb + col[k], gn));
+            cn[k] = op.fetch_center(LSG_IX(zb + col[k], gn));
+        }
+#pragma unroll
+        for (int s = 0; s < NH; s++)
+            if (hs[s] >= 0) hn[s] = op.fetch(LSG_IX(zb + ho[s], gn));
+        zl = (zl + 1 == nz) ? 0u : zl + 1;
+    }
+
+    float2 *sm = smem0;
+#pragma unroll 1
+    for (int z = z0; z < z1; z++) {
+        constexpr int HEAD = Q - 1;
+        constexpr int CEN = RQ;
+        const unsigned zbase = (unsigned)z * nxy;
+#pragma unroll
+        for (int k = 0; k < NY; k++) {
+            q[k][HEAD] = df_value(op, qn[k], ks, bad);
+            sm[LSG_IX((RQ + ty * NY + k) * FX + RQ + tx, FX * FY)] = q[k][CEN];
+        }
+#pragma unroll
+        for (int s = 0; s < NH; s++)
+            if (hs[s] >= 0) sm[LSG_IX(hs[s], FX * FY)] = df_value(op, hn[s], ks, bad);
+        Ctr cc[NY];
+#pragma unroll
+        for (int k = 0; k < NY; k++) cc[k] = cn[k];
+        if (z + 1 < z1) {  // plane z+1's loads in flight while plane z is computed
+            const unsigned lb = zl * nxy, nb = zbase + nxy;
+#pragma unroll
+            for (int k = 0; k < NY; k++) {
+                qn[k] = op.fetch(LSG_IX(lb + col[k], gn));
+                cn[k] = op.fetch_center(LSG_IX(nb + col[k], gn));
+            }
+#pragma unroll
+            for (int s = 0; s < NH; s++)
+                if (hs[s] >= 0) hn[s] = op.fetch(LSG_IX(nb + ho[s], gn));
+            zl = (zl + 1 == nz) ? 0u : zl + 1;
+        }
+        __syncthreads();
+        const float2 *col0 = sm + (RQ + ty * NY) * FX + RQ + tx;
+        float2 yv[NY + 2 * RQ];
+#pragma unroll
+        for (int j = 0; j < RQ; j++) {
+            yv[j] = col0[(j - RQ) * FX];
+            yv[RQ + NY + j] = col0[(NY + j) * FX];
+        }
+#pragma unroll
+        for (int k = 0; k < NY; k++) yv[RQ + k] = q[k][CEN];
+#pragma unroll
+        for (int k = 0; k < NY; k++) {
+            const float2 *row = col0 + k * FX;
+            const float2 c = q[k][CEN];
+            float2 au;
+            au.x = __fmul_rn(c.x, w.wf[0]);
+            au.y = __fmaf_rn(c.x, w.wf[0], -au.x);
+            au.y = __fmaf_rn(c.x, w.wf[1], au.y);
+            au.y = __fmaf_rn(c.y, w.wf[0], au.y);
+            au.y = __fmaf_rn(c.x, w.wf[2], au.y);
+#pragma unroll
+            for (int p = 1; p <= RQ; p++) {
+                if (GENERIC && p > radius) break;
+                // the six neighbours at distance p, summed as a tree (depth 3)
+                const float2 sx = df_add2(row[-p], row[p]);
+                const float2 sy = df_add2(yv[RQ + k - p], yv[RQ + k + p]);
+                const float2 sz = df_add2(q[k][CEN - p], q[k][CEN + p]);
+                const float2 sp = df_add2(df_add2(sx, sy), sz);
+                df_fma_acc(au, sp.x, sp.y, w.wf[3 * p], w.wf[3 * p + 1], w.wf[3 * p + 2]);
+            }
+            if (valid[k] && LSG_IX_OK(zbase + col[k], gn)) {
+                if constexpr (HasStoreDf<Op>::value)
+                    op.store_df(zbase + col[k], c, au, cc[k], ks, acc);
+                else
+                    op.store(zbase + col[k], df_to_double(c, ks), df_to_double(au, ks), cc[k], acc);
+            }
+        }
+        sm = (sm == smem0) ? smem1 : smem0;
+        // advance the ring: planes z-RQ+1 .. z+RQ into slots 0 .. 2RQ-1
+#pragma unroll
+        for (int k = 0; k < NY; k++)
+#pragma unroll
+            for (int j = 0; j < 2 * RQ; j++) q[k][j] = q[k][j + 1];
+    }
+
+    if (__syncthreads_or(bad ? 1 : 0) && tid == 0 && op.ctrl)
+        atomicOr(&const_cast<DevCtrl *>(op.ctrl)->df_range, 1);
+    if (Op::NACC > 0) {
+        constexpr int NA = Op::NACC > 0 ? Op::NACC : 1;
+        __shared__ double red[NA * 32];
+        block_reduce_store<NA>(acc, red, op.partials + blk * Op::NACC);
+    }
+}
+
+// DFM: the FP64 march in double-float arithmetic (functors with DF set).
+template <typename T, int RQ, int BY, int NY, int MINB, bool GENERIC, class Op, bool DFM = false>
 __global__ void __launch_bounds__(32 * BY, MINB) stencil_kernel(Geom g, Weights<T> w, int lz, Op op) {
     constexpr int FX = 32 + 2 * RQ;
     constexpr int FY = BY * NY + 2 * RQ;
-    __shared__ T smem[2][FX * FY];
+    __shared__ __align__(16) T smem[2][FX * FY];
     if (op.skip()) return;
     op.init();
     const long long blk = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
-    stencil_march<T, RQ, BY, NY, GENERIC>(g, w, lz, op, smem[0], smem[1], blockIdx.x, blockIdx.y,
-                                          blockIdx.z, blk);
+    if constexpr (DFM && std::is_same<T, double>::value) {
+        stencil_march_df<RQ, BY, NY, GENERIC>(g, w, lz, op, smem[0], smem[1], blockIdx.x, blockIdx.y, blockIdx.z,
+                                              blk);
+    } else {
+        stencil_march<T, RQ, BY, NY, GENERIC>(g, w, lz, op, smem[0], smem[1], blockIdx.x, blockIdx.y,
+                                              blockIdx.z, blk);
+    }
 }
 
 // ---------------------------------------------------------------- two columns per lane

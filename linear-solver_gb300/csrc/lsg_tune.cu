@@ -65,6 +65,23 @@ template <> int dtype_of<float>() { return LSG_F32; }
 template <> int dtype_of<cplx<double>>() { return LSG_C128; }
 template <> int dtype_of<cplx<float>>() { return LSG_C64; }
 
+// Fills the tuner's scratch vectors with values in [-0.5, 0.5) (a hash of the
+// index), so the passes time the arithmetic of real data (zeros take the
+// double-float split's flush path).
+template <typename T>
+__global__ void tune_fill_kernel(T *v, long long n) {
+    using R = typename RealOf<T>::type;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        unsigned h = (unsigned)i * 2654435761u;
+        h ^= h >> 15;
+        h *= 2246822519u;
+        h ^= h >> 13;
+        const R a = (R)((double)h * (1.0 / 4294967296.0) - 0.5);
+        if constexpr (IsCplx<T>::value) v[i] = T(a, (R)0.25 * a);
+        else v[i] = a;
+    }
+}
+
 // Times `reps` launches of the Richardson pass in shape (tile, lz); ms per launch.
 // FP32 vectors time the lean recurrence pass (x left out), the form AAR uses
 // by default (p - 1 <= m).
@@ -118,6 +135,8 @@ static int tune_t(const lsg_operator *op, cudaStream_t s, TuneEntry *out, int *n
     cudaEventCreate(&e1);
     int rc = LSG_OK;
     if (cudaMemsetAsync(buf, 0, cb + 256, s) != cudaSuccess) rc = set_error(LSG_CUDA_ERROR, "autotune memset");
+    tune_fill_kernel<T><<<sms * 4, 256, 0, s>>>(v, 7 * n);
+    if (cudaGetLastError() != cudaSuccess) rc = set_error(LSG_CUDA_ERROR, "autotune fill");
     TuneEntry best;
     best.tile = 0;
     const int lz_default = choose_lz<T>(g, sms * Kernels<T>::stencil_blocks_per_sm(0));
@@ -136,6 +155,7 @@ static int tune_t(const lsg_operator *op, cudaStream_t s, TuneEntry *out, int *n
         for (int lz : cands) {
             if (lz < 1 || lz > g.nz) continue;
             StencilLaunch L{g, lz, s, var};
+            L.exact = fp64_exact();
             float ms = 0.f;
             rc = time_rich<T>(L, w, v, n, ctrl, e0, e1, &ms);
             if (rc != LSG_OK) break;

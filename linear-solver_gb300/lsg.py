@@ -28,7 +28,8 @@ A_REF = -1.0 / (4.0 * math.pi)  # operator scale of MPI_REAL/main.c:68
 
 F64, F32, C128, C64 = 0, 1, 2, 3
 STATUS = {0: "ok", 1: "not converged", 2: "NaN/Inf detected", 3: "bad argument", 4: "CUDA error",
-          5: "timeout", 6: "unsupported", 7: "out of memory", 8: "SVD sweep limit"}
+          5: "timeout", 6: "unsupported", 7: "out of memory", 8: "SVD sweep limit",
+          9: "value beyond the double-float stencil range"}
 
 
 class CudaLibraryError(RuntimeError):
@@ -98,7 +99,8 @@ EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "ls
            "lsg_profile", "lsg_profile_read", "lsg_set_compat_mode", "lsg_aar_mixed_c",
            "lsg_pinv_solve_noalloc", "lsg_aar_batched", "lsg_aar_mixed_batched", "lsg_autotune",
            "lsg_set_autotune", "lsg_autotune_save", "lsg_autotune_load", "lsg_gmres",
-           "lsg_aar_csr", "lsg_apply_csr", "lsg_register_operator_csr", "lsg_bounds_errors"]
+           "lsg_aar_csr", "lsg_apply_csr", "lsg_register_operator_csr", "lsg_bounds_errors",
+           "lsg_set_fp64_arith"]
 
 KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "unused"]
 
@@ -138,6 +140,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
                                                 C.POINTER(dp)]
         L.lsg_autotune.argtypes = [C.POINTER(_Operator), ip, C.POINTER(_TuneInfo), vp]
         L.lsg_set_autotune.argtypes = [ip]
+        L.lsg_set_fp64_arith.argtypes = [ip]
         L.lsg_autotune_save.argtypes = [C.c_char_p]
         L.lsg_autotune_load.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
         L.lsg_bounds_errors.argtypes = [C.POINTER(C.c_longlong)]
@@ -391,6 +394,13 @@ def autotune(op: Operator, dtype, stream=None) -> dict:
 def set_autotune(mode: int):
     """0: default launch shapes; 1: cached tuned shapes (default); 2: tune each new grid / batch."""
     _check(lib().lsg_set_autotune(int(mode)), "lsg_set_autotune", allow=(0,))
+
+
+def set_fp64_arith(mode: int) -> int:
+    """Arithmetic of the FP64 stencil passes in the solvers: 0 = double-float
+    sums on the FP32 pipe (default; tol < 1e-10 takes FP64 anyway), 1 = FP64
+    arithmetic.  Returns the previous mode."""
+    return int(lib().lsg_set_fp64_arith(int(mode)))
 
 
 def autotune_save(path: str):
