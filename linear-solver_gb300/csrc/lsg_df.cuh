@@ -116,21 +116,25 @@ __device__ __forceinline__ double df_to_double(float2 v, int k) {
         v.y = __fsub_rn(v.y, __fsub_rn(h, v.x));
         v.x = h;
     }
+    // every case as an integer bit pattern, one reinterpretation at the end
     const unsigned bh = __float_as_uint(v.x), bl = __float_as_uint(v.y);
     const unsigned ah = bh & 0x7fffffffu, al = bl & 0x7fffffffu;
-    if (ah < 0x00800000u) return df_f2d(v.y, k);  // hi zero (or denormal): lo alone
-    if (ah >= 0x7f800000u) return __hiloint2double(0x7ff80000, 0);
     const unsigned H = (ah >> 3) + ((unsigned)(896 - k) << 20);
-    const unsigned L = bh << 29;
     const int sh = (int)(al >> 23) - (int)(ah >> 23) + 29;  // lo's unit exponent minus the double's
     const unsigned ml = (al & 0x7fffffu) | 0x800000u;
     unsigned t = sh >= 0 ? (ml << (sh > 7 ? 7 : sh)) : (sh > -25 ? (ml >> -sh) : 0u);
-    if (al < 0x00800000u) t = 0u;
-    const bool opp = ((bh ^ bl) >> 31) != 0;
-    if (opp && (ah & 0x7fffffu) == 0u) t <<= 1;
-    unsigned long long P = ((unsigned long long)H << 32) | L;
-    P = opp ? P - t : P + t;
-    return __longlong_as_double((long long)(P | ((unsigned long long)(bh & 0x80000000u) << 32)));
+    t = al < 0x00800000u ? 0u : t;
+    const unsigned opp = (bh ^ bl) >> 31;
+    t = (opp && (ah & 0x7fffffu) == 0u) ? t << 1 : t;
+    const unsigned long long P = ((unsigned long long)H << 32) | (bh << 29);
+    unsigned long long R = (opp ? P - t : P + t) | ((unsigned long long)(bh & 0x80000000u) << 32);
+    // hi zero (or denormal): lo alone, as df_f2d forms it
+    const unsigned HL = al < 0x00800000u ? 0u : (al >> 3) + ((unsigned)(896 - k) << 20);
+    const unsigned LL = al < 0x00800000u ? 0u : bl << 29;
+    const unsigned long long RL = ((unsigned long long)(HL | (bl & 0x80000000u)) << 32) | LL;
+    R = ah < 0x00800000u ? RL : R;
+    R = ah >= 0x7f800000u ? 0x7ff8000000000000ull : R;
+    return __longlong_as_double((long long)R);
 }
 
 // Double-float pair of a double constant: hi = the float nearest w, lo = the

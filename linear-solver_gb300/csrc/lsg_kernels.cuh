@@ -650,11 +650,12 @@ __global__ void __launch_bounds__(kReduceThreads) gram_kernel(const T *__restric
 // chunk); block b takes chunks b, b + G, ..., so each thread visits the same
 // points in the same order as gram_block's grid-stride loop and the sums are
 // bit-identical to it.  Every wait is bounded: a copy that has not landed
-// after ~2 s sets LSG_TIMEOUT in the control block, the block waits (again
+// after `wait_cycles` SM clocks (a launch parameter: kWaitCycles, ~2 s, in
+// solves) sets LSG_TIMEOUT in the control block, the block waits (again
 // bounded) for its own copies in flight and returns.
 constexpr int kGramStages = 3;
 constexpr int kGramChunk = 4 * kReduceThreads;  // floats per column per stage
-constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
+constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz: the solves' limit
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(unsigned long long *b, unsigned count) {
@@ -682,21 +683,22 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *b, unsigned ph
         : "memory");
     return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *b, unsigned phase) {
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *b, unsigned phase, long long limit) {
     if (mbar_try_wait(b, phase)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(b, phase))
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > limit) return false;
     return true;
 }
 
 // extra_tx: bytes armed on each stage beyond the copies' (0; the failure
-// test arms more, so the waits run out and the timeout path is taken).
+// test arms more, so the waits run out and the timeout path is taken);
+// wait_cycles: the limit of every wait.
 template <int M>
 __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const float *__restrict__ df,
                                                                      const float *__restrict__ r, long long n,
                                                                      double *partials, DevCtrl *ctrl,
-                                                                     unsigned extra_tx) {
+                                                                     unsigned extra_tx, long long wait_cycles) {
     constexpr int NP = (M * (M + 1)) / 2;
     constexpr int NV = NP + M;
     constexpr int S = kGramStages, CH = kGramChunk, CV = CH / 4;
@@ -733,7 +735,7 @@ __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const floa
     long long k = 0;
     for (; k < mine; k++) {
         const int st = (int)(k % S);
-        if (!mbar_wait_bounded(&full[st], (unsigned)((k / S) & 1))) {
+        if (!mbar_wait_bounded(&full[st], (unsigned)((k / S) & 1), wait_cycles)) {
             abort_flag = 1;
         } else {
             const long long off = (first + k * step) * CH;
@@ -762,7 +764,7 @@ __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const floa
     if (abort_flag) {
         if (tid == 0) {
             for (long long kk = k; kk < k + S && kk < mine; kk++)
-                mbar_wait_bounded(&full[kk % S], (unsigned)((kk / S) & 1));
+                mbar_wait_bounded(&full[kk % S], (unsigned)((kk / S) & 1), wait_cycles);
             if (ctrl) {
                 ctrl->status = LSG_TIMEOUT;
                 ctrl->done = 1;
@@ -1153,23 +1155,28 @@ static cudaError_t gram_dispatch(int m, const T *dx, const T *df, const T *r, lo
         // the bulk-copy form: 16-byte aligned columns and residual, n % 4 == 0
         if (n % 4 == 0 && m >= 1 && m <= 8 && (((uintptr_t)df | (uintptr_t)r) & 15u) == 0) {
             DevCtrl *c = const_cast<DevCtrl *>(ctrl);
-            // LSG_FAULT_GRAM_TX=<bytes>: failure test of the bounded waits
+            // LSG_FAULT_GRAM_TX=<bytes>: failure test of the bounded waits, which
+            // then give up after LSG_GRAM_WAIT_CYCLES (default kWaitCycles)
             static const unsigned extra_tx = [] {
                 const char *e = getenv("LSG_FAULT_GRAM_TX");
                 const long v = e ? atol(e) : 0;
                 return (unsigned)(v > 0 && v < 65536 ? v : 0);
             }();
+            static const long long wait_cycles = [] {
+                const char *e = getenv("LSG_GRAM_WAIT_CYCLES");
+                const long long v = e ? atoll(e) : 0;
+                return v >= 1000000 && v <= kWaitCycles ? v : kWaitCycles;
+            }();
             switch (m) {
 #define LSG_GRAM_BULK(MM)                                                                                     \
     case MM: {                                                                                                \
-        static bool attr = false;                                                                             \
-        if (!attr) {                                                                                          \
-            cudaFuncSetAttribute(gram_bulk_kernel<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize,           \
-                                 (int)gram_bulk_smem<MM>());                                                  \
-            attr = true;                                                                                      \
-        }                                                                                                     \
+        /* the attribute is per device and context: set on every launch (a cheap host call) */               \
+        const cudaError_t ea = cudaFuncSetAttribute(gram_bulk_kernel<MM>,                                     \
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,              \
+                                                    (int)gram_bulk_smem<MM>());                               \
+        if (ea != cudaSuccess) return ea;                                                                     \
         gram_bulk_kernel<MM><<<blocks, kReduceThreads, gram_bulk_smem<MM>(), s>>>(df, r, n, partials, c,      \
-                                                                                  extra_tx);                  \
+                                                                                  extra_tx, wait_cycles);     \
         return cudaGetLastError();                                                                            \
     }
                 LSG_GRAM_BULK(1) LSG_GRAM_BULK(2) LSG_GRAM_BULK(3) LSG_GRAM_BULK(4)
@@ -1250,7 +1257,7 @@ template <typename T>
 cudaError_t Kernels<T>::aar_update_lean(int m, T *x, const T *r, const T *rs, const T *h, T *step,
                                         double beta, S cf, long long n, unsigned mask, const DevCtrl *ctrl,
                                         cudaStream_t s) {
-    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 8);
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, (long long)sm_count() * 8);
     if constexpr (!std::is_same<typename RealOf<T>::type, float>::value) {  // FP64 keeps the reference form
         (void)m, (void)x, (void)r, (void)rs, (void)h, (void)step, (void)beta, (void)cf, (void)mask, (void)ctrl,
             (void)s, (void)blocks;
@@ -1280,7 +1287,7 @@ cudaError_t Kernels<T>::aar_update_lean(int m, T *x, const T *r, const T *rs, co
 template <typename T>
 cudaError_t Kernels<T>::recur_fold(int m, T *x, const T *r, const T *rs, const T *h, double beta, S cf,
                                    long long n, unsigned mask, cudaStream_t s) {
-    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 8);
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, (long long)sm_count() * 8);
     if constexpr (!std::is_same<typename RealOf<T>::type, float>::value) {
         (void)m, (void)x, (void)r, (void)rs, (void)h, (void)beta, (void)cf, (void)mask, (void)s, (void)blocks;
         return cudaErrorInvalidValue;
@@ -1293,7 +1300,7 @@ cudaError_t Kernels<T>::recur_fold(int m, T *x, const T *r, const T *rs, const T
 template <typename T>
 cudaError_t Kernels<T>::aar_update(int m, T *x, const T *r, const T *h, T *step, double beta,
                                    S cf, long long n, const DevCtrl *ctrl, cudaStream_t s) {
-    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 8);
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, (long long)sm_count() * 8);
     if constexpr (IsCplx<T>::value) {
         aar_update_kernel<T, 0><<<blocks, kReduceThreads, 0, s>>>(m, x, r, h, step, T(beta), (T)cf, n, ctrl);
     } else {
@@ -1343,7 +1350,7 @@ cudaError_t Kernels<T>::norm2(const T *v, long long n, double *partials, int blo
 
 template <typename T>
 cudaError_t Kernels<T>::axpy(T *x, const T *y, double alpha, long long n, cudaStream_t s) {
-    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 8);
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, (long long)sm_count() * 8);
     axpy_kernel<T><<<blocks, kReduceThreads, 0, s>>>(x, y, (T)alpha, n);
     return cudaGetLastError();
 }
@@ -1405,7 +1412,7 @@ __global__ void __launch_bounds__(kReduceThreads) zero_check_kernel(const T64 *_
 
 template <typename T64>
 cudaError_t zero_check(const T64 *x, long long n, DevCtrl *ctrl, cudaStream_t s) {
-    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 4);
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, (long long)sm_count() * 4);
     zero_check_kernel<T64><<<blocks, kReduceThreads, 0, s>>>(x, n, ctrl);
     return cudaGetLastError();
 }
@@ -1482,7 +1489,7 @@ __global__ void __launch_bounds__(kReduceThreads) shift_kernel(T64 *__restrict__
 
 template <typename T64>
 cudaError_t rhs_mean(const T64 *b, long long n, double *partials, DevCtrl *ctrl, cudaStream_t s) {
-    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 4);
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, (long long)sm_count() * 4);
     mean_sum_kernel<T64><<<blocks, kReduceThreads, 0, s>>>(b, n, partials);
     mean_finalize_kernel<<<1, kReduceThreads, 0, s>>>(partials, blocks, n, ctrl, 0, 0.0, 0.0);
     return cudaGetLastError();
@@ -1491,7 +1498,7 @@ cudaError_t rhs_mean(const T64 *b, long long n, double *partials, DevCtrl *ctrl,
 template <typename T64>
 cudaError_t deflate_x(T64 *x, long long n, double *partials, DevCtrl *ctrl, double sig_re, double sig_im,
                       cudaStream_t s) {
-    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 4);
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, (long long)sm_count() * 4);
     mean_sum_kernel<T64><<<blocks, kReduceThreads, 0, s>>>(x, n, partials);
     mean_finalize_kernel<<<1, kReduceThreads, 0, s>>>(partials, blocks, n, ctrl, 1, sig_re, sig_im);
     shift_kernel<T64><<<blocks, kReduceThreads, 0, s>>>(x, n, ctrl);
@@ -1500,7 +1507,7 @@ cudaError_t deflate_x(T64 *x, long long n, double *partials, DevCtrl *ctrl, doub
 
 template <typename T64, typename T32>
 cudaError_t ir_correct(T64 *x, T32 *e, long long n, cudaStream_t s) {
-    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, 152 * 8);
+    const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, (long long)sm_count() * 8);
     ir_correct_kernel<T64, T32><<<blocks, kReduceThreads, 0, s>>>(x, e, n);
     return cudaGetLastError();
 }

@@ -29,6 +29,7 @@
 //   double *partials                      where the block writes NACC sums
 #pragma once
 
+#include <cstring>
 #include <type_traits>
 
 #include "lsg_internal.cuh"
@@ -293,6 +294,24 @@ template <class Op, class = void> struct HasStoreDf { static constexpr bool valu
 template <class Op>
 struct HasStoreDf<Op, std::void_t<decltype(Op::STORE_DF)>> { static constexpr bool value = Op::STORE_DF; };
 
+// Operands in flight across the march's loop are carried as integer words:
+// loop-carried double registers are copied through the FP64 pipe at the
+// loop's back edge, integer ones through the integer pipe.
+template <class V, bool BOX = (sizeof(V) % 8 == 0)> struct Bits { V v; };
+template <class V> struct Bits<V, true> { unsigned long long w[sizeof(V) / 8]; };
+template <class V>
+__device__ __forceinline__ Bits<V> to_bits(const V &v) {
+    Bits<V> b;
+    memcpy(&b, &v, sizeof(V));
+    return b;
+}
+template <class V>
+__device__ __forceinline__ V from_bits(const Bits<V> &b) {
+    V v;
+    memcpy(&v, &b, sizeof(V));
+    return v;
+}
+
 template <int RQ, int BY, int NY, bool GENERIC, class Op>
 __device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<double> &w, int lz, Op &op,
                                                  double *smem0d, double *smem1d, int bx, int by, int bz,
@@ -369,18 +388,18 @@ __device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<do
         for (int k = 0; k < NY; k++) q[k][s] = df_value(op, op.fetch(LSG_IX(base + col[k], gn)), ks, bad);
         zl = (zl + 1 == nz) ? 0u : zl + 1;
     }
-    Raw qn[NY], hn[NH];
-    Ctr cn[NY];
+    Bits<Raw> qn[NY], hn[NH];
+    Bits<Ctr> cn[NY];
     {
         const unsigned lb = zl * nxy, zb = (unsigned)z0 * nxy;
 #pragma unroll
         for (int k = 0; k < NY; k++) {
-            qn[k] = op.fetch(LSG_IX(lb + col[k], gn));
-            cn[k] = op.fetch_center(LSG_IX(zb + col[k], gn));
+            qn[k] = to_bits(op.fetch(LSG_IX(lb + col[k], gn)));
+            cn[k] = to_bits(op.fetch_center(LSG_IX(zb + col[k], gn)));
         }
 #pragma unroll
         for (int s = 0; s < NH; s++)
-            if (hs[s] >= 0) hn[s] = op.fetch(LSG_IX(zb + ho[s], gn));
+            if (hs[s] >= 0) hn[s] = to_bits(op.fetch(LSG_IX(zb + ho[s], gn)));
         zl = (zl + 1 == nz) ? 0u : zl + 1;
     }
 
@@ -392,25 +411,25 @@ __device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<do
         const unsigned zbase = (unsigned)z * nxy;
 #pragma unroll
         for (int k = 0; k < NY; k++) {
-            q[k][HEAD] = df_value(op, qn[k], ks, bad);
+            q[k][HEAD] = df_value(op, from_bits(qn[k]), ks, bad);
             sm[LSG_IX((RQ + ty * NY + k) * FX + RQ + tx, FX * FY)] = q[k][CEN];
         }
 #pragma unroll
         for (int s = 0; s < NH; s++)
-            if (hs[s] >= 0) sm[LSG_IX(hs[s], FX * FY)] = df_value(op, hn[s], ks, bad);
-        Ctr cc[NY];
+            if (hs[s] >= 0) sm[LSG_IX(hs[s], FX * FY)] = df_value(op, from_bits(hn[s]), ks, bad);
+        Bits<Ctr> cc[NY];
 #pragma unroll
         for (int k = 0; k < NY; k++) cc[k] = cn[k];
         if (z + 1 < z1) {  // plane z+1's loads in flight while plane z is computed
             const unsigned lb = zl * nxy, nb = zbase + nxy;
 #pragma unroll
             for (int k = 0; k < NY; k++) {
-                qn[k] = op.fetch(LSG_IX(lb + col[k], gn));
-                cn[k] = op.fetch_center(LSG_IX(nb + col[k], gn));
+                qn[k] = to_bits(op.fetch(LSG_IX(lb + col[k], gn)));
+                cn[k] = to_bits(op.fetch_center(LSG_IX(nb + col[k], gn)));
             }
 #pragma unroll
             for (int s = 0; s < NH; s++)
-                if (hs[s] >= 0) hn[s] = op.fetch(LSG_IX(nb + ho[s], gn));
+                if (hs[s] >= 0) hn[s] = to_bits(op.fetch(LSG_IX(nb + ho[s], gn)));
             zl = (zl + 1 == nz) ? 0u : zl + 1;
         }
         __syncthreads();
@@ -445,9 +464,9 @@ __device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<do
             }
             if (valid[k] && LSG_IX_OK(zbase + col[k], gn)) {
                 if constexpr (HasStoreDf<Op>::value)
-                    op.store_df(zbase + col[k], c, au, cc[k], ks, acc);
+                    op.store_df(zbase + col[k], c, au, from_bits(cc[k]), ks, acc);
                 else
-                    op.store(zbase + col[k], df_to_double(c, ks), df_to_double(au, ks), cc[k], acc);
+                    op.store(zbase + col[k], df_to_double(c, ks), df_to_double(au, ks), from_bits(cc[k]), acc);
             }
         }
         sm = (sm == smem0) ? smem1 : smem0;

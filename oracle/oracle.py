@@ -44,10 +44,23 @@ class ResultStruct(C.Structure):
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
 
+def reference_dir() -> str:
+    """Where the reference's MPI_REAL sources are: $LSG_REFERENCE_DIR, else the
+    Makefile's REF default (the recipe that compiles them names the path)."""
+    env = os.environ.get("LSG_REFERENCE_DIR")
+    if env:
+        return env
+    with open(os.path.join(HERE, "Makefile")) as f:
+        for line in f:
+            if line.startswith("REF ?="):
+                return line.split("?=", 1)[1].strip()
+    return ""
+
+
 def build(with_ref: bool | None = None) -> None:
     """Compile the oracle (and, where the reference checkout exists, the reference)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    ref_dir = os.environ.get("LSG_REFERENCE_DIR", "/root/reference/MPI_REAL")
+    ref_dir = reference_dir()
     if with_ref is None:
         with_ref = os.path.isdir(ref_dir)
     if with_ref:

@@ -9,7 +9,11 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("LSG_REFERENCE_DIR", "/root/reference/MPI_REAL")
+try:
+    from oracle.oracle import reference_dir
+    REF = reference_dir()
+except Exception:  # the checker's loader itself unavailable
+    REF = ""
 
 
 @pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "main.c")), reason="reference checkout absent")

@@ -5,7 +5,8 @@ The FP32 Gram streams the history through shared memory with bulk copies
 whose completion each stage's mbarrier waits for, with a time limit.  Setting
 LSG_FAULT_GRAM_TX arms every stage with more bytes than its copies deliver:
 all copies land, the barrier phase never completes, the waits give up after
-their limit (about 2 s), and the kernel sets LSG_TIMEOUT and stops the solve.
+their limit (LSG_GRAM_WAIT_CYCLES, here ~10 ms; solves use ~2 s), and the
+kernel sets LSG_TIMEOUT and stops the solve.
 The child process then runs an FP64 solve (no bulk-copy Gram) on the same
 context, which must converge as usual.
 """
@@ -36,7 +37,8 @@ print("FP64 status", r["status"], r["iters"])
 
 
 def test_gram_wait_timeout_reported_context_usable():
-    env = dict(os.environ, LSG_FAULT_GRAM_TX="16")
+    # each wait gives up after 2e7 SM clocks (~10 ms) instead of the solves' ~2 s
+    env = dict(os.environ, LSG_FAULT_GRAM_TX="16", LSG_GRAM_WAIT_CYCLES="20000000")
     out = subprocess.run([sys.executable, "-c", CHILD], cwd=ROOT, env=env, capture_output=True, text=True,
                          timeout=300)
     assert out.returncode == 0, out.stderr[-2000:]
