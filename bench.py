@@ -15,7 +15,13 @@ exchange on one GPU per rank), and the time is the max over ranks.
 --impl reference times the CPU implementation of the same path on the host
 cores: the C restatement of the reference solver (oracle/), run with every
 host thread on a bounded sample of iterations of the same problem and
-extrapolated to the iteration count the full solve needs.
+extrapolated to the iteration count the full solve needs.  --cpu-full runs
+one complete CPU solve instead (about 2.5 minutes on 16 cores) to check that
+extrapolation.
+
+Every solution on the line carries its error against the FFT diagonal solve
+of the periodic operator (an exact FP64 solve, mean removed), computed here
+with torch's FFT from the operator's coefficients.
 """
 from __future__ import annotations
 
@@ -46,9 +52,10 @@ WORKLOAD = ("256^3 periodic 12th-order FD Poisson (a = -1/(4 pi), FDn = 6, Jacob
 LARGE_GOLDEN = os.path.join(ROOT, "tests", "golden", "large_256.json")
 CPU_SAMPLE_ITERS = 24
 # DRAM bytes (read + write) of one launch of the dominant kernel at this
-# workload, from the ncu capture summarised in
-# profiles/richardson_f32_lean_256cube.md.
+# workload, from an ncu capture of that kernel on this workload (a constant:
+# the timed run is not captured).
 RICH32_TRAFFIC_BYTES = 224.2e6
+FP64_SOLVERS = ("aar", "pgr", "pl2r", "cg")
 
 
 def _peaks():
@@ -145,19 +152,20 @@ def _barrier(ws: int):
         dist.barrier()
 
 
-def _large_iters():
+def _large_iters(solver: str = "aar"):
     try:
         with open(LARGE_GOLDEN) as f:
-            return int(json.load(f)["aar"]["iters"])
+            return int(json.load(f)[solver]["iters"])
     except Exception:
         return None
 
 
-def cpu_sample(iters_full: int, threads: int | None = None):
-    """Times CPU_SAMPLE_ITERS iterations of the oracle AAR on the full workload
-    with every host thread; returns (seconds to solution, seconds/iter, threads)."""
-    import numpy as np
-
+def cpu_sample(iters_full: int, threads: int | None = None, solver: str = "aar", full: bool = False):
+    """Times CPU_SAMPLE_ITERS iterations (or, full=True, the whole solve) of
+    the oracle solver on the full workload with every host thread; returns
+    (seconds to solution, seconds/iter, threads, iterations timed).  The
+    oracle's work arrays are first-touched before its timer starts, so the
+    sample measures the steady state."""
     import workloads
     from oracle import oracle as O
 
@@ -165,10 +173,49 @@ def cpu_sample(iters_full: int, threads: int | None = None):
     threads = threads or O.lib().lsgo_max_threads()
     b = workloads.uniform_rhs(N_GRID, SEED)
     kw = dict(SOLVER_KW)
-    _, r = O.solve("aar", b, None, max_iter=CPU_SAMPLE_ITERS, threads=threads, **kw)
-    per_iter = r["seconds"] / CPU_SAMPLE_ITERS
-    del np
-    return per_iter * iters_full, per_iter, threads
+    if solver != "aar":
+        kw.pop("beta")
+    _, r = O.solve(solver, b, None, max_iter=100000 if full else CPU_SAMPLE_ITERS, threads=threads, **kw)
+    timed = r["iters"] if full else CPU_SAMPLE_ITERS
+    per_iter = r["seconds"] / max(timed, 1)
+    return (r["seconds"] if full else per_iter * iters_full), per_iter, threads, timed
+
+
+def fft_reference(b, op):
+    """The exact FP64 solution of the periodic operator (its DFT symbol is
+    a (3 c_0 + sum_p 2 c_p (cos 2 pi p kx/nx + cos .. ky + cos .. kz)) + sigma),
+    mean-free for the singular Poisson case; torch FFT on the device."""
+    import math
+
+    import torch
+    nz, ny, nx = b.shape
+    c = op.coeff
+
+    def axis(n):
+        k = torch.arange(n, dtype=torch.float64, device=b.device)
+        s = torch.zeros(n, dtype=torch.float64, device=b.device)
+        for p in range(1, op.radius + 1):
+            s += 2.0 * c[p] * torch.cos(2.0 * math.pi * p * k / n)
+        return s
+
+    lam = op.a * (3.0 * c[0] + axis(nz)[:, None, None] + axis(ny)[None, :, None] + axis(nx)[None, None, :])
+    lam = lam + op.sigma
+    bh = torch.fft.fftn(b)
+    singular = lam[0, 0, 0] == 0
+    lam[0, 0, 0] = 1.0 if singular else lam[0, 0, 0]
+    xh = bh / lam
+    if singular:
+        xh[0, 0, 0] = 0.0
+    x = torch.fft.ifftn(xh)
+    return x.real if not torch.is_complex(b) else x
+
+
+def err_vs_fft(x, xf, mean_free=True):
+    """Relative 2-norm error of x against the FFT solution (means removed for
+    the singular Poisson operator)."""
+    if mean_free:
+        x = x - x.mean()
+    return ((x - xf).norm() / xf.norm()).item()
 
 
 def run_reference(args):
@@ -183,19 +230,20 @@ def run_reference(args):
     samples = []
     threads = None
     for i in range(args.warmup + args.steps):
-        tts, per_iter, threads = cpu_sample(iters)
+        tts, per_iter, threads, _ = cpu_sample(iters)
         if i >= args.warmup:
             samples.append(tts)
     value = statistics.mean(samples)
-    sample = (f"{CPU_SAMPLE_ITERS} of {iters} AAR iterations at 256^3 per step, "
-              f"extrapolated by the iteration count; {threads} threads")
+    sample = (f"{CPU_SAMPLE_ITERS} of {iters} AAR iterations at 256^3 per step (work arrays "
+              f"first-touched before the timer), extrapolated by the iteration count; {threads} threads")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": {"workload": WORKLOAD, "n": N_GRID, "solver": "AAR FP64",
                                          "implementation": "C restatement of MPI_REAL AAR (oracle/), OpenMP"},
-        "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port", "sample": sample,
+                         "extrapolated_from": f"{CPU_SAMPLE_ITERS} iterations x {iters} / {CPU_SAMPLE_ITERS}"},
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -259,23 +307,51 @@ def run_lsg(args):
     ms = _max_over_ranks(ms, ws)
     value = ms / 1e3
     true_res = ((b - lsg.apply(op, x)).norm() / b.norm()).item()
+    xf = fft_reference(b, op)
+    err_mixed = err_vs_fft(x, xf)
 
-    # ---- FP64 AAR (the drop-in's arithmetic) on the same problem
-    x64, i64 = solve_fp64()
+    # ---- the four FP64 solvers (the drop-in's arithmetic: double-float
+    # stencil sums at this tolerance) and the FP64 AAR in FP64 arithmetic
+    def timed_solve(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        xs, inf = fn()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1) / 1e3, xs, inf
+
+    fp64 = {}
+    for s in FP64_SOLVERS:
+        kw = dict(SOLVER_KW)
+        if s != "aar":
+            kw.pop("beta")
+        secs, xs, inf = timed_solve(lambda: lsg.SOLVERS[s](op, b, **kw))
+        fp64[s] = {"seconds": secs, "iters": inf["iters"], "relres": inf["relres"],
+                   "true_relres": ((b - lsg.apply(op, xs)).norm() / b.norm()).item(),
+                   "err_vs_fft": err_vs_fft(xs, xf), "status": inf["status_name"],
+                   "updates_per_s": N * inf["iters"] / secs}
+        if s == "aar":
+            x64 = xs
+    fp64_s = fp64["aar"]["seconds"]
+    prev = lsg.set_fp64_arith(1)
+    secs, xs, inf = timed_solve(solve_fp64)
+    lsg.profile(True)
+    lsg.aar(op, b, max_iter=60, **SOLVER_KW)
     torch.cuda.synchronize()
-    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    t0.record(stream)
-    x64, i64 = solve_fp64()
-    t1.record(stream)
-    torch.cuda.synchronize()
-    fp64_s = t0.elapsed_time(t1) / 1e3
+    lsg.profile(False)
+    prof64x = lsg.profile_read()
+    lsg.set_fp64_arith(prev)
+    fp64_exact = {"seconds": secs, "iters": inf["iters"], "relres": inf["relres"],
+                  "err_vs_fft": err_vs_fft(xs, xf)}
+    del xs
     # per-kernel times of the FP64 iteration: 60 profiled iterations
     lsg.profile(True)
     lsg.aar(op, b, max_iter=60, **{k: v for k, v in SOLVER_KW.items()})
     torch.cuda.synchronize()
     lsg.profile(False)
     prof64 = lsg.profile_read()
-    true64 = ((b - lsg.apply(op, x64)).norm() / b.norm()).item()
 
     # ---- end to end: the reference-prototype AAR(POISSON*, ...) on pinned host
     # buffers (H2D of x0 and rhs, D2H of x inside the timed region), mixed mode
@@ -309,15 +385,32 @@ def run_lsg(args):
     total_ms = sum(v[1] for v in prof.values())
     r64l, r64ms = prof64["richardson"]
     rich64_ms = r64ms / max(r64l, 1)
+    r64xl, r64xms = prof64x["richardson"]
+    rich64x_ms = r64xms / max(r64xl, 1)
+    rich64_bytes = 7 * N * 8  # reads x, r, b; writes x', r', H, DF
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        iters_full = i64["iters"]
-        tts, per_iter, threads = cpu_sample(iters_full)
+        iters_full = fp64["aar"]["iters"]
+        tts, per_iter, threads, timed = cpu_sample(iters_full, full=args.cpu_full)
         cpu = {"value": tts, "unit": "s", "cores": threads, "kind": "port",
-               "sample": f"{CPU_SAMPLE_ITERS} of {iters_full} AAR iterations of the same 256^3 "
-                         f"workload on {threads} threads, extrapolated by the iteration count",
-               "seconds_per_iter": per_iter}
+               "sample": (f"one full {timed}-iteration AAR solve of the same 256^3 workload on {threads} threads"
+                          if args.cpu_full else
+                          f"{CPU_SAMPLE_ITERS} of {iters_full} AAR iterations of the same 256^3 workload on "
+                          f"{threads} threads (work arrays first-touched before the timer), extrapolated by the "
+                          f"iteration count"),
+               "measured": bool(args.cpu_full), "seconds_per_iter": per_iter}
+        # the other FP64 solvers: seconds per iteration on the same cores (bounded samples)
+        per = {}
+        for s in FP64_SOLVERS:
+            if s == "aar":
+                per[s] = per_iter
+                continue
+            _, pi, _, _ = cpu_sample(fp64[s]["iters"], threads=threads, solver=s)
+            per[s] = pi
+        for s in FP64_SOLVERS:
+            fp64[s]["cpu_seconds_per_iter"] = per[s]
+            fp64[s]["cpu_seconds_extrapolated"] = per[s] * fp64[s]["iters"]
 
     extra = other_workloads(dev) if (rank == 0 and not args.no_extra) else None
 
@@ -333,22 +426,33 @@ def run_lsg(args):
                                                                        "us_best", "us_default")}
                                             for k, v in tuned.items()}},
         "mixed": {"inner_iters": infos[-1]["inner_iters"], "outer_iters": infos[-1]["outer_iters"],
-                  "relres": infos[-1]["relres"], "true_relres_fp64": true_res},
-        "fp64": {"seconds": fp64_s, "iters": i64["iters"], "relres": i64["relres"],
-                 "true_relres": true64, "speedup_mixed_vs_fp64": fp64_s / value,
+                  "relres": infos[-1]["relres"], "true_relres_fp64": true_res, "err_vs_fft": err_mixed},
+        "fp64": {"seconds": fp64_s, "iters": fp64["aar"]["iters"], "relres": fp64["aar"]["relres"],
+                 "true_relres": fp64["aar"]["true_relres"], "err_vs_fft": fp64["aar"]["err_vs_fft"],
+                 "speedup_mixed_vs_fp64": fp64_s / value,
+                 "stencil_arith": "double-float sums on the FP32 pipe (FP64 storage and epilogue)",
                  "richardson_ms": rich64_ms,
-                 "richardson_gpts": N / (rich64_ms * 1e-3) / 1e9},
+                 "richardson_gpts": N / (rich64_ms * 1e-3) / 1e9,
+                 "fp64_arith": dict(fp64_exact, richardson_ms=rich64x_ms)},
+        "fp64_solvers": fp64,
+        "roofline_fp64": {"kernel": "stencil_kernel<double, RichOp, double-float> (fused FP64 Richardson step)",
+                          "bytes_per_launch": rich64_bytes, "avg_launch_ms": rich64_ms,
+                          "achieved": rich64_bytes / (rich64_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                          "frac": rich64_bytes / (rich64_ms * 1e-3) / 1e9 / peak,
+                          "frac_fp64_arith": rich64_bytes / (rich64x_ms * 1e-3) / 1e9 / peak,
+                          "bound": "issue (double-float arithmetic, ~950 instructions per point)"},
         "roofline": {"bound": "hbm",
                      "kernel": "stencil_x2_kernel<float, RichLeanOp> in the tuned paired shape (fused Richardson step, x left out)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
                      "traffic": RICH32_TRAFFIC_BYTES, "traffic_unit": "bytes per launch (ncu)",
+                     "traffic_source": "constant from an ncu capture of this kernel on this workload, not of this run",
                      "bytes_per_launch": rich_bytes, "avg_launch_ms": rich_ms,
                      "note": ("lean form: 4 vectors per launch (x left out; the x-carrying form moved 6 and ran "
                               "at a higher fraction but slower); latency-bound at 16 warps/SM, see the profile"),
                      "share_of_kernel_time": rms / total_ms if total_ms else None},
         "kernel_profile_ms": {k: round(v[1], 4) for k, v in prof.items() if v[0]},
-        "updates_per_s": {"mixed": N * infos[-1]["inner_iters"] / value, "fp64": N * i64["iters"] / fp64_s},
+        "updates_per_s": {"mixed": N * infos[-1]["inner_iters"] / value, "fp64": N * fp64["aar"]["iters"] / fp64_s},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 2 * N * 8,
                 "d2h_bytes_per_step": N * 8, "path": "AAR(POISSON*, ...) drop-in, mixed mode, pinned host buffers",
                 "converged": e2e_ok},
@@ -394,6 +498,8 @@ def other_workloads(dev):
     secs, (x, r) = timed(lambda: lsg.aar_mixed(op, b, tol=1e-10))
     res["blobs_384_mixed_1e-10"] = {"seconds": secs, "inner_iters": r["inner_iters"],
                                     "outer_iters": r["outer_iters"], "relres": r["relres"],
+                                    "true_relres_fp64": ((b - lsg.apply(op, x)).norm() / b.norm()).item(),
+                                    "err_vs_fft": err_vs_fft(x, fft_reference(b, op)),
                                     "updates_per_s": n ** 3 * r["inner_iters"] / secs}
     del b, x
     batch = workloads.helmholtz_batch(2024)
@@ -401,7 +507,8 @@ def other_workloads(dev):
     bs = [torch.from_numpy(v).to(dev) for _, _, v in batch]
     secs, (xs, rs) = timed(lambda: lsg.aar_batched(ops, bs, mixed=True, tol=1e-8))
     pts = sum(m ** 3 * r["iters"] for (m, _, _), r in zip(batch, rs))
-    res["helmholtz_48_batched"] = {"seconds": secs, "instances": len(batch),
+    errs = [err_vs_fft(xi, fft_reference(bi, oi), mean_free=False) for xi, bi, oi in zip(xs, bs, ops)]
+    res["helmholtz_48_batched"] = {"seconds": secs, "instances": len(batch), "err_vs_fft_max": max(errs),
                                    "converged": sum(r["status"] == 0 for r in rs),
                                    "iters_min": min(r["iters"] for r in rs),
                                    "iters_max": max(r["iters"] for r in rs),
@@ -482,6 +589,8 @@ def main():
     ap.add_argument("--impl", default="lsg", choices=["lsg", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-extra", action="store_true", help="skip the other measured workloads")
+    ap.add_argument("--cpu-full", action="store_true",
+                    help="time one complete CPU solve for the baseline instead of a bounded sample")
     ap.add_argument("--case", choices=["rich32", "rich64", "mixed", "fp64"],
                     help="run one short fixed invocation for a profiler and exit")
     args = ap.parse_args()

@@ -262,10 +262,22 @@ static int pinv_cut(const double *A, const double *b, double *x, int m, double c
     return status;
 }
 
+/* Zeroed work array, first touched by the OpenMP threads that will use it
+ * (so its pages are mapped -- and placed near those threads -- before a
+ * solver's timer starts: a bounded sample of iterations then measures the
+ * steady state, not the page faults of the first writes). */
 static void *xcalloc(long n, size_t sz)
 {
-    void *p = calloc((size_t)(n > 0 ? n : 1), sz);
+    const size_t bytes = (size_t)(n > 0 ? n : 1) * sz;
+    char *p = malloc(bytes);
+    long i;
+    const long chunks = (long)((bytes + 65535) / 65536);
     if (!p) abort();
+#pragma omp parallel for schedule(static)
+    for (i = 0; i < chunks; i++) {
+        const size_t off = (size_t)i * 65536;
+        memset(p + off, 0, bytes - off < 65536 ? bytes - off : 65536);
+    }
     return p;
 }
 

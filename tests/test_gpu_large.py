@@ -28,18 +28,59 @@ def _check(lsg, b, xf, x, r, tol):
     return true, err
 
 
-def test_aar_fp64_256(lsg, problem256, golden):
-    """Same iteration count as the CPU oracle's full run (tests/golden/large_256.json)."""
+def _pinned(name):
     import json
     import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "large_256.json")) as f:
+        return json.load(f)[name]
+
+
+def test_aar_fp64_256(lsg, problem256, golden):
+    """Same iteration count as the CPU oracle's full run (tests/golden/large_256.json).
+
+    The FP64 stencil passes run in double-float arithmetic (rounding ~2^-48 of
+    sum |w| |x| instead of FP64's ~2^-53), which moves the final residual of
+    this 1320-iteration trajectory by ~1% (9.52e-9 against the oracle's
+    9.43e-9); with FP64 arithmetic (lsg_set_fp64_arith(1)) it stays within
+    0.2%."""
     b, xf = problem256
+    pinned = _pinned("aar")
     x, r = lsg.aar(lsg.Operator(256), b)
     true, err = _check(lsg, b, xf, x, r, 1e-8)
     assert err < 1e-5
-    with open(os.path.join(os.path.dirname(__file__), "golden", "large_256.json")) as f:
-        pinned = json.load(f)["aar"]
+    assert r["iters"] == pinned["iters"]
+    assert r["relres"] == pytest.approx(pinned["relres"], rel=2e-2)
+    prev = lsg.set_fp64_arith(1)
+    try:
+        x, r = lsg.aar(lsg.Operator(256), b)
+    finally:
+        lsg.set_fp64_arith(prev)
+    _check(lsg, b, xf, x, r, 1e-8)
     assert r["iters"] == pinned["iters"]
     assert r["relres"] == pytest.approx(pinned["relres"], rel=5e-3)
+
+
+@pytest.mark.parametrize("solver", ["cg", "pgr", "pl2r"])
+def test_fp64_solvers_256(lsg, problem256, solver):
+    """The other FP64 solvers at 256^3 to 1e-8 against the oracle's full runs
+    (MPI_REAL/CG.c:57-153, PGR.c:90-142, PL2R.c:90-142 restated).
+
+    CG's count is stable under rounding and must match.  PGR and PL2R take
+    2500-3600 iterations whose projections amplify last-bit differences: the
+    oracle's own count moves with its OpenMP reduction order, and the GPU's
+    FP64-arithmetic and double-float runs land within a few periods of it
+    (PL2R: 2496 / 2520 against the oracle's 2508), so their counts are held
+    to 2%.  Every run must reach the FP64 residual and agree with the FFT
+    solve as well as the oracle's solution does (within 2x)."""
+    b, xf = problem256
+    pinned = _pinned(solver)
+    x, r = getattr(lsg, solver)(lsg.Operator(256), b)
+    true, err = _check(lsg, b, xf, x, r, 1e-8)
+    if solver == "cg":
+        assert r["iters"] == pinned["iters"]
+    else:
+        assert abs(r["iters"] - pinned["iters"]) <= 0.02 * pinned["iters"], (r["iters"], pinned)
+    assert err <= 2.0 * pinned["err_vs_fft"] + 1e-9, (err, pinned)
 
 
 def test_aar_mixed_256(lsg, problem256):
