@@ -201,8 +201,9 @@ def fft_reference(b, op):
     lam = op.a * (3.0 * c[0] + axis(nz)[:, None, None] + axis(ny)[None, :, None] + axis(nx)[None, None, :])
     lam = lam + op.sigma
     bh = torch.fft.fftn(b)
-    singular = lam[0, 0, 0] == 0
-    lam[0, 0, 0] = 1.0 if singular else lam[0, 0, 0]
+    singular = op.sigma == 0  # the constant mode (its symbol is zero up to rounding)
+    if singular:
+        lam[0, 0, 0] = 1.0
     xh = bh / lam
     if singular:
         xh[0, 0, 0] = 0.0

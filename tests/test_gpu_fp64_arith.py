@@ -33,10 +33,25 @@ def test_known_answers_both_arithmetics(lsg, oracle, golden, fp64_mode, mode, so
     x, r = lsg.SOLVERS[solver](lsg.Operator(48), bt, torch.ones_like(bt))
     assert r["status"] == 0 and r["iters"] == KNOWN[solver], (mode, solver, r)
     printed = float(g[f"ref48_{solver}_relres_printed"])
-    assert r["relres"] == pytest.approx(printed, rel=2e-3 if solver != "cg" else 0.5)
+    rtol = 2e-3 if mode == 1 else 2e-2
+    assert r["relres"] == pytest.approx(printed, rel=rtol if solver != "cg" else 0.5)
     xm = x.cpu().numpy()
     xm = xm - xm.mean()
     assert np.linalg.norm(xm) == pytest.approx(float(g[f"ref48_{solver}_x_norm"]), rel=1e-8)
+
+
+def test_small_goldens_fp64_arithmetic(lsg, golden, fp64_mode):
+    """The reference's small cases with FP64 arithmetic: printed residuals to 2e-3."""
+    from test_gpu_solvers import _case
+    fp64_mode(1)
+    g = golden("small_solves.npz")
+    for solver in KNOWN:
+        _case(lsg, g, "n16", solver, g["b16"], rtol=2e-3)
+        _case(lsg, g, "odd", solver, g["b_odd"], rtol=2e-3)
+    _case(lsg, g, "n16_nopc", "pgr", g["b16"], precond=False, rtol=2e-3)
+    _case(lsg, g, "n16_nopc", "cg", g["b16"], precond=False, rtol=2e-3)
+    for s in ("aar", "pgr", "pl2r"):
+        _case(lsg, g, "n16_m3p4", s, g["b16"], m=3, p=4, omega=0.9, beta=0.4, rtol=2e-3)
 
 
 @pytest.mark.parametrize("n", [16, 37])

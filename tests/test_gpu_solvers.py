@@ -1,10 +1,13 @@
 """Solver parity: the GPU solvers against the reference's own runs (golden
 fixtures from the unmodified MPI_REAL code) and the CPU oracle.
 
-FP64 bar: identical iteration counts, the reference's residual to 2e-3
-relative (rounding of the history Gram moves the last digits), and the
-solution (mean removed, since the periodic Poisson operator is singular) to
-1e-8 relative.
+FP64 bar: identical iteration counts, the reference's printed residual to
+2e-2 relative, and the solution (mean removed, since the periodic Poisson
+operator is singular) to 1e-8 relative.  The FP64 solvers' stencil sums run
+in double-float arithmetic by default (rounding ~2^-48 of sum |w| |x|, 30x
+FP64's), which moves the residual at the last check of a long trajectory by
+up to ~1.5% (PGR without preconditioning at 16^3); with FP64 arithmetic the
+same cases hold 2e-3 (tests/test_gpu_fp64_arith.py).
 
 CG's final residual is compared more loosely (within 50%, and below tol):
 the reference's CG restarts the residual every 50 steps but keeps the old
@@ -33,7 +36,7 @@ def _merr(x, xr):
     return np.linalg.norm(x - xr) / np.linalg.norm(xr)
 
 
-def _case(lsg, g, prefix, solver, b, x0=None, **kw):
+def _case(lsg, g, prefix, solver, b, x0=None, rtol=2e-2, **kw):
     op_kw = {k: kw.pop(k) for k in ("precond",) if k in kw}
     nz, ny, nx = b.shape
     op = lsg.Operator((nx, ny, nz), **op_kw)
@@ -41,7 +44,7 @@ def _case(lsg, g, prefix, solver, b, x0=None, **kw):
     x = x.cpu().numpy()
     assert r["iters"] == int(g[f"{prefix}_{solver}_iters"]), (prefix, solver, r)
     printed = float(g[f"{prefix}_{solver}_relres_printed"])
-    assert r["relres"] == pytest.approx(printed, rel=2e-3 if solver != "cg" else 0.5)
+    assert r["relres"] == pytest.approx(printed, rel=rtol if solver != "cg" else 0.5)
     if printed <= kw.get("tol", 1e-8):
         assert r["relres"] <= kw.get("tol", 1e-8)
     key = f"{prefix}_{solver}_x"
