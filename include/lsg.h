@@ -129,6 +129,23 @@ int lsg_pl2r(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x
 int lsg_cg(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
            const void *d_b, lsg_result *res, void *stream);    /* MPI_REAL/CG.c:33 */
 
+/* AAR (MPI_REAL/AAR.c:37-177) preconditioned with block-Jacobi ICC(0), the
+ * reference's pc = 1 (PETSC_REAL/AAR_Real.c:58-61: PCICC on each rank's
+ * diagonal block).  The blocks are the block[0] x block[1] x block[2] boxes
+ * tiling the grid (the subdomains of a Cartesian rank grid); couplings
+ * leaving a box, the periodic wrap included, are dropped.  Each side must
+ * divide the grid, a box holds at most 4096 points, radius <= 6.  FP64
+ * vectors; op->precond is ignored.  The factor is an incomplete L D L^T with
+ * zero fill, natural order, computed once per operator and box shape on the
+ * host (a diagonal shift 1e-3 * 2^k is added if a pivot is not positive). */
+int lsg_aar_icc(const lsg_operator *op, const lsg_params *prm, const int block[3], double *d_x,
+                const double *d_b, lsg_result *res, void *stream);
+/* The block ICC(0) factor lsg_aar_icc uses, on host arrays: L[i*18 + 6*axis +
+ * p-1] = l(i, i - p e_axis) (0 where that neighbour lies outside the box),
+ * d[i] the pivots, i = x + bx (y + by z); *shift the diagonal shift applied
+ * (may be NULL).  No GPU needed. */
+int lsg_icc_factor(const lsg_operator *op, const int block[3], double *L, double *d, double *shift);
+
 /* General sparse operator: A x = b for a caller's matrix in CSR form on the
  * device (square, n rows, 32-bit offsets and column indices, FP64 values).
  * The reference's AAR accepts any operator through its Lap_Vec_mult callback
@@ -252,6 +269,7 @@ enum lsg_kernel_class {
     LSG_K_SMALL = 4,      /* single-block finalize and m x m solve */
     LSG_K_CG = 5,         /* CG direction + operator stencil */
     LSG_K_REFINE = 6,     /* FP64 refinement residual and correction */
+    LSG_K_PRECOND = 7,    /* block ICC(0) preconditioner application */
     LSG_K_CLASSES = 8
 };
 typedef struct lsg_kernel_stats {

@@ -40,5 +40,9 @@ int solve_csr(const lsg_csr *A, const lsg_params *prm, double *x, const double *
 int gmres(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, const void *d_b, lsg_result *res,
           cudaStream_t s);
 int release_gmres_workspaces();
+// Block-Jacobi ICC(0) AAR (lsg_solvers.cu, kernels in lsg_icc.cu).
+int solve_icc(const lsg_operator *op, const lsg_params *prm, const int block[3], double *x, const double *b,
+              lsg_result *res, cudaStream_t s);
+void release_icc();
 
 }  // namespace lsg

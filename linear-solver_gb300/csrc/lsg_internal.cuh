@@ -654,6 +654,19 @@ cudaError_t csr_richardson(const CsrView &A, const double *x, const double *r, c
 cudaError_t csr_scale(const double *dinv, const double *r, double *f, long long n, int blocks,
                       const DevCtrl *ctrl, cudaStream_t s);
 
+// Block-Jacobi ICC(0) (lsg_icc.cu): the factor of one (bx, by, bz) box of
+// the operator (computed on the host, cached per device), its application
+// f = M^-1 r fused with the AAR history completion (hist: DF = f - f_old,
+// hc += beta DF), and the Richardson stencil pass with a materialised f
+// (x2 = x + omega f, r2 = b - A x2, hn = omega f).
+struct IccFactor;
+int icc_factor_host(const int block[3], const double *w, int radius, double shift, double *L, double *d);
+int icc_get(const lsg_operator *op, const int block[3], const IccFactor **out, double *shift);
+cudaError_t icc_apply(const IccFactor *F, const Geom &g, const double *r, double *f, const double *f_old,
+                      double *df, double *hc, double beta, int hist, const DevCtrl *ctrl, cudaStream_t s);
+cudaError_t rich_prec(const StencilLaunch &L, const Weights<double> &w, const double *x, const double *f,
+                      const double *b, double *x2, double *r2, double *hn, double omega, const DevCtrl *ctrl);
+
 // Number of Gram values per block for a kind and history depth.
 __host__ __device__ inline int gram_values(int kind, int m) {
     return kind == GRAM_SYM ? (m * (m + 1)) / 2 + m : m * m + m;

@@ -229,6 +229,7 @@ int release_workspaces() {
         g_ws.clear();
     }
     release_csr_extras();
+    release_icc();
     release_gmres_workspaces();
     return release_batch_workspaces();
 }
@@ -361,7 +362,7 @@ struct TraceRange {
     }
 };
 static const char *const kClassNames[LSG_K_CLASSES] = {"richardson", "residual", "gram",   "update",
-                                                       "small",      "cg",       "refine", "other"};
+                                                       "small",      "cg",       "refine", "precond"};
 
 #define LSG_KC(cls, call)                                                                    \
     do {                                                                                     \
@@ -965,6 +966,106 @@ int solve_mixed_c(const lsg_operator *op, const lsg_params *prm, void *x, const 
                                                     res, s);
 }
 
+// ---------------------------------------------------------------- block ICC(0) AAR
+
+// AAR.c:37-177 with f = M^-1 r, M the block ICC(0) factor (PETSC_REAL/AAR_Real.c
+// pc = 1).  f is materialised by the preconditioner pass, which also completes
+// the history column of the previous iteration (DF_c = f - f_old, H_c = step +
+// beta DF_c, c = (it-2) % m); a Richardson iteration is then one stencil pass
+// (x2 = x + omega f, r = b - A x2, the step into column (it-1) % m), an
+// Anderson iteration the Gram of (DF, f), the m x m solve, the update
+// x += beta f - sum H_j s_j (unit Jacobi factor) and the residual pass.
+int solve_icc(const lsg_operator *op, const lsg_params *prm, const int block[3], double *x, const double *b,
+              lsg_result *res, cudaStream_t s) {
+    TraceRange trace("lsg_aar_icc");
+    const double t0 = now_s();
+    int rc = check_operator(op);
+    if (rc) return rc;
+    rc = check_params(prm, true);
+    if (rc) return rc;
+    if (!x || !b || !block) return set_error(LSG_BAD_ARG, "NULL argument");
+    if (op->radius > 6) return set_error(LSG_UNSUPPORTED, "block ICC(0): radius %d > 6", op->radius);
+    for (int a = 0; a < 3; a++)
+        if (block[a] < 1 || block[a] > 255 || op->n[a] % block[a] != 0)
+            return set_error(LSG_BAD_ARG, "block ICC(0): box side %d does not divide the grid side %d", block[a],
+                             op->n[a]);
+    if ((long long)block[0] * block[1] * block[2] > 4096)
+        return set_error(LSG_BAD_ARG, "block ICC(0): a box holds at most 4096 points");
+    const Geom g = make_geom(op->n);
+    const long long n = g.n;
+    const int m = prm->m, p = prm->p;
+    Workspace *ws = nullptr;
+    std::unique_lock<std::mutex> lk;
+    rc = get_workspace(sizeof(double), n, m, false, g, &ws, &lk);
+    if (rc) return rc;
+    const IccFactor *F = nullptr;
+    rc = icc_get(op, block, &F, nullptr);
+    if (rc) return rc;
+    Run R(s, sm_count());
+    const Weights<double> w = make_weights<double>(op);
+    const int lz = choose_lz<double>(g, stencil_slots<double>(R.sms));
+    StencilLaunch L{g, lz, s};
+    L.exact = fp64_exact_for(prm->tol);
+    StencilLaunch Lr = rich_launch<double>(op, L);
+    if (Lr.paired >= 1) Lr = L;
+    Lr.paired = 0;
+    Lr.exact = L.exact;
+    const int sb = (int)stencil_blocks<double>(g, lz);
+    const int rb = reduce_blocks(n, R.sms);
+    const int gb = Kernels<double>::gram_grid(GRAM_SYM, m, n, R.sms);
+    double *X[2] = {x, (double *)ws->xalt};
+    double *r = (double *)ws->r0;
+    double *Fv[2] = {(double *)ws->r1, (double *)ws->rs};
+    double *H = (double *)ws->dx, *DF = (double *)ws->df;
+    DevCtrl *ctrl = ws->ctrl;
+    double *part = ws->partials;
+    ws->hctrl[0] = ctrl_init(prm->tol, 0);
+    LSG_CUDA(cudaMemcpyAsync(ctrl, ws->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, s));
+    LSG_CUDA(cudaMemsetAsync(H, 0, sizeof(double) * (size_t)n * m, s));
+    LSG_CUDA(cudaMemsetAsync(DF, 0, sizeof(double) * (size_t)n * m, s));
+    LSG_KC(LSG_K_UPDATE, Kernels<double>::norm2(b, n, part, rb, ctrl, s));
+    LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, s));
+    LSG_KC(LSG_K_RESIDUAL, Kernels<double>::residual(L, w, RES_INIT, x, b, r, nullptr, nullptr, 1.0, 0.0, part, ctrl));
+    int xc = 0, fc = 0;
+    auto is_anderson = [p](int it) { return it % p == 0 && it > 1; };
+    auto enqueue = [&](int it) -> int {
+        const int cprev = ((it - 2) % m + m) % m;
+        LSG_KC(LSG_K_PRECOND, icc_apply(F, g, r, Fv[fc ^ 1], Fv[fc], DF + (size_t)cprev * n, H + (size_t)cprev * n,
+                                        prm->beta, it > 1 ? 1 : 0, ctrl, s));
+        fc ^= 1;
+        const double *f = Fv[fc];
+        double *hcol = H + (size_t)((it - 1) % m) * n;
+        if (is_anderson(it)) {
+            LSG_KC(LSG_K_GRAM, Kernels<double>::gram(GRAM_SYM, m, H, DF, f, n, part, gb, ctrl, s));
+            LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, gb, GRAM_SYM, m, 1.0, ctrl, s));
+            LSG_KC(LSG_K_UPDATE, Kernels<double>::aar_update(m, X[xc], f, H, hcol, prm->beta, 1.0, n, ctrl, s));
+            LSG_KC(LSG_K_RESIDUAL, Kernels<double>::residual(L, w, RES_INIT, X[xc], b, r, nullptr, nullptr, 1.0, 0.0,
+                                                             part, ctrl));
+            LSG_KC(LSG_K_SMALL, finalize_norm(part, sb, ctrl, NF_CHECK, prm->tol, it, s));
+        } else {
+            LSG_KC(LSG_K_RICHARDSON, rich_prec(Lr, w, X[xc], f, b, X[xc ^ 1], r, hcol, prm->omega, ctrl));
+            xc ^= 1;
+        }
+        return LSG_OK;
+    };
+    rc = pipelined_loop(R, ws, 1, prm->max_iter, default_per_check(prm, n), enqueue, is_anderson);
+    if (rc != LSG_OK) return rc;
+    DevCtrl c;
+    LSG_CUDA(cudaMemcpy(&c, ctrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost));
+    const int last = c.done ? c.iters : prm->max_iter;
+    if (richardson_count(last, p) & 1)
+        LSG_CUDA(cudaMemcpyAsync(x, X[1], sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+    LSG_CUDA(cudaStreamSynchronize(s));
+    R.flush();
+    lsg_result tmp;
+    fill_result(&tmp, c, prm->max_iter, now_s() - t0, R.launches);
+    tmp.outer_iters = 0;
+    tmp.inner_iters = 0;
+    if (res) *res = tmp;
+    set_last_status(tmp.status);
+    return tmp.status;
+}
+
 int apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, cudaStream_t s) {
     int rc = check_operator(op);
     if (rc) return rc;
@@ -1267,6 +1368,10 @@ int lsg_pinv_solve(const double *d_A, const double *d_b, double *d_x, int m, voi
     return lsg::pinv(d_A, d_b, d_x, m, (cudaStream_t)stream);
 }
 int lsg_release_workspaces(void) { return lsg::release_workspaces(); }
+int lsg_aar_icc(const lsg_operator *op, const lsg_params *prm, const int block[3], double *d_x, const double *d_b,
+                lsg_result *res, void *stream) {
+    return lsg::solve_icc(op, prm, block, d_x, d_b, res, (cudaStream_t)stream);
+}
 
 int lsg_profile(int on) {
     std::lock_guard<std::mutex> g(lsg::g_prof_mu);

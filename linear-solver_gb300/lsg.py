@@ -100,9 +100,9 @@ EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "ls
            "lsg_pinv_solve_noalloc", "lsg_aar_batched", "lsg_aar_mixed_batched", "lsg_autotune",
            "lsg_set_autotune", "lsg_autotune_save", "lsg_autotune_load", "lsg_gmres",
            "lsg_aar_csr", "lsg_apply_csr", "lsg_register_operator_csr", "lsg_bounds_errors",
-           "lsg_set_fp64_arith"]
+           "lsg_set_fp64_arith", "lsg_aar_icc", "lsg_icc_factor"]
 
-KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "unused"]
+KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "precond"]
 
 
 def lib(build_if_missing: bool = True) -> C.CDLL:
@@ -141,6 +141,10 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
         L.lsg_autotune.argtypes = [C.POINTER(_Operator), ip, C.POINTER(_TuneInfo), vp]
         L.lsg_set_autotune.argtypes = [ip]
         L.lsg_set_fp64_arith.argtypes = [ip]
+        L.lsg_aar_icc.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), C.POINTER(ip), vp, vp,
+                                  C.POINTER(_Result), vp]
+        L.lsg_icc_factor.argtypes = [C.POINTER(_Operator), C.POINTER(ip), C.POINTER(dp), C.POINTER(dp),
+                                     C.POINTER(dp)]
         L.lsg_autotune_save.argtypes = [C.c_char_p]
         L.lsg_autotune_load.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
         L.lsg_bounds_errors.argtypes = [C.POINTER(C.c_longlong)]
@@ -318,6 +322,37 @@ def cg(op, b, x0=None, **kw):
     return _solve("lsg_cg", op, b, x0, **kw)
 
 
+def aar_icc(op, b, x0=None, block=(8, 8, 8), stream=None, **kw):
+    """AAR with block-Jacobi ICC(0) on (bx, by, bz) boxes, the reference's pc = 1
+    (PETSC_REAL/AAR_Real.c:58-61); FP64 vectors."""
+    import torch
+    _check_vec(b, op, "b")
+    if b.dtype != torch.float64:
+        raise TypeError("aar_icc: float64 vectors")
+    x = torch.zeros_like(b) if x0 is None else x0.clone()
+    res = _Result()
+    prm = _params(**kw)
+    blk = (C.c_int * 3)(*[int(v) for v in block])
+    rc = lib().lsg_aar_icc(C.byref(op._s), C.byref(prm), blk, C.c_void_p(x.data_ptr()),
+                           C.c_void_p(b.data_ptr()), C.byref(res), _stream_ptr(stream))
+    _check(rc, "lsg_aar_icc")
+    return x, _result(res)
+
+
+def icc_factor(op, block=(8, 8, 8)):
+    """The block ICC(0) factor on the host: (L (points x 18), d (points), shift)."""
+    import numpy as np
+    nb = int(block[0]) * int(block[1]) * int(block[2])
+    L = np.zeros(nb * 18)
+    d = np.zeros(nb)
+    sh = C.c_double(0.0)
+    blk = (C.c_int * 3)(*[int(v) for v in block])
+    dp = C.POINTER(C.c_double)
+    _check(lib().lsg_icc_factor(C.byref(op._s), blk, L.ctypes.data_as(dp), d.ctypes.data_as(dp), C.byref(sh)),
+           "lsg_icc_factor", allow=(0,))
+    return L.reshape(nb, 18), d, sh.value
+
+
 def gmres(op, b, x0=None, restart=30, **kw):
     """Restarted GMRES(restart), the reference's PETSc comparator (PETSC_REAL/main.c:84-122)."""
     kw = dict(kw)
@@ -491,7 +526,7 @@ def profile_read() -> dict:
     """{class: (launches, total_ms)} collected since profile(True)."""
     st = _KernelStats()
     lib().lsg_profile_read(C.byref(st))
-    return {KERNEL_CLASSES[i]: (st.launches[i], st.ms[i]) for i in range(7)}
+    return {KERNEL_CLASSES[i]: (st.launches[i], st.ms[i]) for i in range(8)}
 
 
 def set_compat_mode(mixed: bool):

@@ -349,11 +349,14 @@ def gmres(b: np.ndarray, x0=None, *, restart=30, tol=1e-8, max_iter=2000, radius
 
 # ----------------------------------------------------------------------------- AAR on any matrix
 
-def aar_general(matvec, dinv, b, x0=None, *, omega=0.6, beta=0.6, m=7, p=6, tol=1e-8, max_iter=100000):
+def aar_general(matvec, dinv, b, x0=None, *, omega=0.6, beta=0.6, m=7, p=6, tol=1e-8, max_iter=100000,
+                precond=None):
     """MPI_REAL/AAR.c:37-177 with any operator `matvec` and Jacobi factors
     `dinv` (1 / diag(A), or ones), in numpy (test infrastructure for the
-    general sparse operator path).  The m x m solve is the reference's
-    pseudo-inverse (`pinv_solve`).  Returns (x, dict(iters, relres))."""
+    general sparse operator path).  `precond(r)`, when given, replaces the
+    Jacobi scaling (the PCApply of PETSC_REAL/AAR_Real.c:100-103, e.g. the
+    block ICC(0) below).  The m x m solve is the reference's pseudo-inverse
+    (`pinv_solve`).  Returns (x, dict(iters, relres))."""
     b = np.asarray(b, dtype=np.float64).ravel()
     n = b.size
     x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64).ravel()
@@ -364,7 +367,7 @@ def aar_general(matvec, dinv, b, x0=None, *, omega=0.6, beta=0.6, m=7, p=6, tol=
     x_old = f_old = None
     it = 1
     while it <= max_iter and relres > tol_abs:        # AAR.c:91
-        f = dinv * r                                  # Precondition
+        f = dinv * r if precond is None else precond(r)  # Precondition
         if it > 1:                                    # AAR.c:96-102
             c = (it - 2) % m
             DX[c], DF[c] = x - x_old, f - f_old
@@ -380,3 +383,111 @@ def aar_general(matvec, dinv, b, x0=None, *, omega=0.6, beta=0.6, m=7, p=6, tol=
             r = b - matvec(x)
         it += 1
     return x, dict(iters=it - 1, relres=relres / np.linalg.norm(b), converged=bool(relres <= tol_abs))
+
+
+# ---------------------------------------------------------------- block ICC(0)
+# PETSC_REAL/AAR_Real.c:58-61 and PETSC_COMPLEX/AAR_Complex.c:63-66 (pc = 1):
+# PCICC on each rank's diagonal block of A (MatGetDiagonalBlock), i.e.
+# block-Jacobi with incomplete Cholesky, zero fill, on every block.  Here the
+# blocks are the (bx, by, bz) boxes tiling the periodic grid (the subdomains a
+# Cartesian rank grid would own); couplings that leave a box -- the periodic
+# wrap included -- are dropped.  The operator has constant coefficients, so
+# every box has the same block matrix and one factor serves all of them.
+
+
+def icc0_block_factor(block, weights, radius=6, shift=0.0):
+    """Incomplete LDL^T of the block matrix (natural order, x fastest; zero fill).
+
+    weights: w[0] (diagonal, 3 a c_0 + sigma) and w[1..radius] (a c_p).  The
+    lower neighbours of a point are the star points at distance p = 1..radius
+    below it along each axis that lie in the box; two such rows share lower
+    neighbours only along their common axis, so
+        l(i, i-p e) = (w_p - sum_{q>p} l(i, i-q e) l(i-p e, i-q e) d(i-q e)) / d(i-p e)
+        d(i)        = w_0 (1 + shift) - sum_{axis, p} l(i, i-p e)^2 d(i-p e).
+    Returns (L, d): L[i, 6 a + p - 1] = l(i, i - p e_a) (0 outside the box), or
+    None when a pivot is not positive."""
+    bx, by, bz = block
+    n = bx * by * bz
+    R = radius
+    L = np.zeros((n, 3 * 6))
+    d = np.zeros(n)
+    strides = (1, bx, bx * by)
+    for i in range(n):
+        c = (i % bx, (i // bx) % by, i // (bx * by))
+        acc = weights[0] * (1.0 + shift)
+        for a in range(3):
+            for p in range(R, 0, -1):          # farthest first: its terms feed the nearer ones
+                if c[a] < p:
+                    continue
+                k = i - p * strides[a]
+                t = weights[p]
+                for q in range(R, p, -1):
+                    if c[a] < q:
+                        continue
+                    tt = i - q * strides[a]
+                    t = t - L[i, 6 * a + q - 1] * L[k, 6 * a + (q - p) - 1] * d[tt]
+                L[i, 6 * a + p - 1] = t / d[k]
+        for a in range(3):
+            for p in range(1, R + 1):
+                if c[a] >= p:
+                    k = i - p * strides[a]
+                    acc = acc - L[i, 6 * a + p - 1] * L[i, 6 * a + p - 1] * d[k]
+        if not acc > 0.0:
+            return None
+        d[i] = acc
+    return L, d
+
+
+def icc0_factor_shifted(block, weights, radius=6):
+    """The factor of the first shift in 0, 1e-3, 2e-3, 4e-3, ... (a multiple of
+    the diagonal, Manteuffel's remedy for a non-positive pivot) that gives
+    positive pivots.  Returns (L, d, shift)."""
+    shift = 0.0
+    for _ in range(40):
+        f = icc0_block_factor(block, weights, radius, shift)
+        if f is not None:
+            return f[0], f[1], shift
+        shift = 1e-3 if shift == 0.0 else 2.0 * shift
+    raise RuntimeError("ICC(0): no positive factor")
+
+
+def icc0_apply(r, shape, block, L, d, radius=6):
+    """f = (L D L^T)^-1 r on every box of the (nz, ny, nx) grid: forward
+    solve with unit-diagonal L, division by D, backward solve with L^T; sums in
+    the fixed order axis x, y, z and p = 1..radius."""
+    nz, ny, nx = shape
+    bx, by, bz = block
+    n = bx * by * bz
+    R = radius
+    strides = (1, bx, bx * by)
+    rb = np.asarray(r, dtype=np.float64).reshape(nz // bz, bz, ny // by, by, nx // bx, bx)
+    rb = rb.transpose(0, 2, 4, 1, 3, 5).reshape(-1, n)      # (blocks, points in natural order)
+    y = np.zeros_like(rb)
+    coords = [(i % bx, (i // bx) % by, i // (bx * by)) for i in range(n)]
+    for i in range(n):
+        acc = rb[:, i].copy()
+        c = coords[i]
+        for a in range(3):
+            for p in range(1, R + 1):
+                if c[a] >= p:
+                    acc = acc - L[i, 6 * a + p - 1] * y[:, i - p * strides[a]]
+        y[:, i] = acc
+    z = y / d
+    x = np.zeros_like(rb)
+    for i in range(n - 1, -1, -1):
+        acc = z[:, i].copy()
+        c = coords[i]
+        dims = (bx, by, bz)
+        for a in range(3):
+            for p in range(1, R + 1):
+                if c[a] + p < dims[a]:
+                    j = i + p * strides[a]
+                    acc = acc - L[j, 6 * a + p - 1] * x[:, j]
+        x[:, i] = acc
+    x = x.reshape(nz // bz, ny // by, nx // bx, bz, by, bx).transpose(0, 3, 1, 4, 2, 5)
+    return x.reshape(nz, ny, nx)
+
+
+def stencil_weights(radius=6, a=A_REF, sigma=0.0):
+    c = coefficients(radius)
+    return [a * 3.0 * c[0] + sigma] + [a * c[p] for p in range(1, radius + 1)]
