@@ -86,6 +86,8 @@ struct IccFactor {
     double shift;
     double *L = nullptr;      // nb x 18
     double *dinv = nullptr;   // nb: 1 / d
+    float2 *Lf = nullptr;     // the same as double-float pairs (double-float apply)
+    float2 *dinvf = nullptr;
     int *order = nullptr;     // point indices sorted by level (natural order within a level)
     int *lev = nullptr;       // nlev + 1 offsets into order
     int *coord = nullptr;     // cx | cy << 8 | cz << 16
@@ -97,6 +99,7 @@ struct IccFactor {
 
 struct IccView {
     const double *L, *dinv;
+    const float2 *Lf, *dinvf;
     const int *order, *lev, *coord;
     int bx, by, bz, nb, nlev, radius;
 };
@@ -153,8 +156,12 @@ int icc_get(const lsg_operator *op, const int block[3], const IccFactor **out, d
     const size_t bL = (size_t)nb * kIccSlots * 8, bD = (size_t)nb * 8, bO = (size_t)nb * 4,
                  bV = (size_t)(nlev + 1) * 4, bC = (size_t)nb * 4;
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    std::vector<float2> Lf((size_t)nb * kIccSlots), dinvf(nb);
+    for (size_t i = 0; i < Lf.size(); i++) Lf[i] = df_weight(L[i]);
+    for (int i = 0; i < nb; i++) dinvf[i] = df_weight(dinv[i]);
     char *base = nullptr;
-    cudaError_t e = cudaMalloc(&base, al(bL) + al(bD) + al(bO) + al(bV) + al(bC));
+    const size_t oLf = al(bL) + al(bD) + al(bO) + al(bV) + al(bC), oDf = oLf + al(bL);
+    cudaError_t e = cudaMalloc(&base, oDf + al(bD));
     if (e != cudaSuccess) {
         cudaGetLastError();
         return set_error(LSG_NO_MEMORY, "block ICC(0) factor: %s", cudaGetErrorString(e));
@@ -165,11 +172,15 @@ int icc_get(const lsg_operator *op, const int block[3], const IccFactor **out, d
     F->order = (int *)(base + al(bL) + al(bD));
     F->lev = (int *)(base + al(bL) + al(bD) + al(bO));
     F->coord = (int *)(base + al(bL) + al(bD) + al(bO) + al(bV));
+    F->Lf = (float2 *)(base + oLf);
+    F->dinvf = (float2 *)(base + oDf);
     e = cudaMemcpy(F->L, L.data(), bL, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(F->dinv, dinv.data(), bD, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(F->order, order.data(), bO, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(F->lev, lev.data(), bV, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(F->coord, coord.data(), bC, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(F->Lf, Lf.data(), bL, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(F->dinvf, dinvf.data(), bD, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return set_error(LSG_CUDA_ERROR, "block ICC(0) upload: %s", cudaGetErrorString(e));
     F->bx = bx;
     F->by = by;
@@ -186,15 +197,103 @@ int icc_get(const lsg_operator *op, const int block[3], const IccFactor **out, d
 
 // ---------------------------------------------------------------- apply
 
+// acc - l y for double-float acc, l, y (l y by the FMA two-product; the lo
+// word left unnormalised until the point's sum is complete).
+__device__ __forceinline__ float2 df_fnms(float2 acc, float2 l, float2 y) {
+    const float p = __fmul_rn(l.x, y.x);
+    float e = __fmaf_rn(l.x, y.x, -p);
+    e = __fmaf_rn(l.x, y.y, e);
+    e = __fmaf_rn(l.y, y.x, e);
+    float s, t;
+    df_two_sum(acc.x, -p, s, t);
+    return make_float2(s, __fadd_rn(__fsub_rn(acc.y, e), t));
+}
+
+__device__ __forceinline__ float2 df_norm(float2 v) {
+    const float h = __fadd_rn(v.x, v.y);
+    return make_float2(h, __fsub_rn(v.y, __fsub_rn(h, v.x)));
+}
+
+__device__ __forceinline__ void icc_apply_df(const IccView &F, const Geom &g, const double *__restrict__ r,
+                                             double *__restrict__ f, const double *__restrict__ f_old,
+                                             double *__restrict__ df, double *__restrict__ hc, double beta,
+                                             int hist, const DevCtrl *ctrl, float2 *y) {
+    const int ks = ctrl ? df_shift_for(ctrl->rhs_norm) : 0;
+    bool bad = false;
+    const int nbx = g.nx / F.bx, nby = g.ny / F.by;
+    const int box = blockIdx.x;
+    const int ox = (box % nbx) * F.bx, oy = ((box / nbx) % nby) * F.by, oz = (box / (nbx * nby)) * F.bz;
+    const int st[3] = {1, F.bx, F.bx * F.by};
+    const int dim[3] = {F.bx, F.by, F.bz};
+    auto gidx = [&](int cw) -> long long {
+        return (long long)(ox + (cw & 0xff)) +
+               (long long)g.nx * ((oy + ((cw >> 8) & 0xff)) + (long long)g.ny * (oz + (cw >> 16)));
+    };
+    for (int i = threadIdx.x; i < F.nb; i += blockDim.x) y[i] = df_split(r[gidx(F.coord[i])], ks, bad);
+    __syncthreads();
+    for (int l = 0; l < F.nlev; l++) {
+        for (int t = F.lev[l] + threadIdx.x; t < F.lev[l + 1]; t += blockDim.x) {
+            const int i = F.order[t];
+            const int cw = F.coord[i];
+            const int c[3] = {cw & 0xff, (cw >> 8) & 0xff, cw >> 16};
+            const float2 *Li = F.Lf + (size_t)i * kIccSlots;
+            float2 acc = y[i];
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+                for (int p = 1; p <= F.radius; p++)
+                    if (c[a] >= p) acc = df_fnms(acc, Li[6 * a + p - 1], y[i - p * st[a]]);
+            y[i] = df_norm(acc);
+        }
+        __syncthreads();
+    }
+    for (int l = F.nlev - 1; l >= 0; l--) {
+        for (int t = F.lev[l] + threadIdx.x; t < F.lev[l + 1]; t += blockDim.x) {
+            const int i = F.order[t];
+            const int cw = F.coord[i];
+            const int c[3] = {cw & 0xff, (cw >> 8) & 0xff, cw >> 16};
+            float2 acc = df_mul(y[i], F.dinvf[i]);
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+                for (int p = 1; p <= F.radius; p++)
+                    if (c[a] + p < dim[a]) {
+                        const int j = i + p * st[a];
+                        acc = df_fnms(acc, F.Lf[(size_t)j * kIccSlots + 6 * a + p - 1], y[j]);
+                    }
+            y[i] = df_norm(acc);
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < F.nb; i += blockDim.x) {
+        const long long gi = gidx(F.coord[i]);
+        const double fv = df_to_double(y[i], ks);
+        f[gi] = fv;
+        if (hist) {
+            const double d = fv - f_old[gi];
+            df[gi] = d;
+            hc[gi] = fma(beta, d, hc[gi]);
+        }
+    }
+    if (__syncthreads_or(bad ? 1 : 0) && threadIdx.x == 0 && ctrl)
+        atomicOr(&const_cast<DevCtrl *>(ctrl)->df_range, 1);
+}
+
 // f = (L D L^T)^-1 r on box blockIdx.x; hist: also DF = f - f_old and
 // hc = hc + beta DF.  Sums in the fixed order axis x, y, z and p = 1..radius.
+// DFM: the solves in double-float arithmetic (the residual split into pairs
+// scaled by 2^k as in the stencil passes; f rounded to doubles once).
+template <bool DFM>
 __global__ void __launch_bounds__(kIccThreads) icc_apply_kernel(IccView F, Geom g, const double *__restrict__ r,
                                                                  double *__restrict__ f,
                                                                  const double *__restrict__ f_old,
                                                                  double *__restrict__ df, double *__restrict__ hc,
                                                                  double beta, int hist, const DevCtrl *ctrl) {
-    extern __shared__ double y[];
+    extern __shared__ double ysm[];
     if (solve_done(ctrl)) return;
+    if constexpr (DFM) {
+        icc_apply_df(F, g, r, f, f_old, df, hc, beta, hist, ctrl, reinterpret_cast<float2 *>(ysm));
+        return;
+    }
+    double *y = ysm;
     const int nbx = g.nx / F.bx, nby = g.ny / F.by;
     const int box = blockIdx.x;
     const int ox = (box % nbx) * F.bx, oy = ((box / nbx) % nby) * F.by, oz = (box / (nbx * nby)) * F.bz;
@@ -253,16 +352,15 @@ __global__ void __launch_bounds__(kIccThreads) icc_apply_kernel(IccView F, Geom 
 }
 
 cudaError_t icc_apply(const IccFactor *F, const Geom &g, const double *r, double *f, const double *f_old,
-                      double *df, double *hc, double beta, int hist, const DevCtrl *ctrl, cudaStream_t s) {
-    const IccView v{F->L, F->dinv, F->order, F->lev, F->coord, F->bx, F->by, F->bz, F->nb, F->nlev, F->radius};
+                      double *df, double *hc, double beta, int hist, const DevCtrl *ctrl, int exact, cudaStream_t s) {
+    const IccView v{F->L, F->dinv, F->Lf, F->dinvf, F->order, F->lev, F->coord, F->bx, F->by, F->bz, F->nb,
+                    F->nlev, F->radius};
     const long long boxes = (long long)(g.nx / F->bx) * (g.ny / F->by) * (g.nz / F->bz);
     const size_t smem = (size_t)F->nb * sizeof(double);
-    if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(icc_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)smem);
-        if (e != cudaSuccess) return e;
-    }
-    icc_apply_kernel<<<(unsigned)boxes, kIccThreads, smem, s>>>(v, g, r, f, f_old, df, hc, beta, hist, ctrl);
+    if (exact)
+        icc_apply_kernel<false><<<(unsigned)boxes, kIccThreads, smem, s>>>(v, g, r, f, f_old, df, hc, beta, hist, ctrl);
+    else
+        icc_apply_kernel<true><<<(unsigned)boxes, kIccThreads, smem, s>>>(v, g, r, f, f_old, df, hc, beta, hist, ctrl);
     return cudaGetLastError();
 }
 

@@ -663,7 +663,7 @@ struct IccFactor;
 int icc_factor_host(const int block[3], const double *w, int radius, double shift, double *L, double *d);
 int icc_get(const lsg_operator *op, const int block[3], const IccFactor **out, double *shift);
 cudaError_t icc_apply(const IccFactor *F, const Geom &g, const double *r, double *f, const double *f_old,
-                      double *df, double *hc, double beta, int hist, const DevCtrl *ctrl, cudaStream_t s);
+                      double *df, double *hc, double beta, int hist, const DevCtrl *ctrl, int exact, cudaStream_t s);
 cudaError_t rich_prec(const StencilLaunch &L, const Weights<double> &w, const double *x, const double *f,
                       const double *b, double *x2, double *r2, double *hn, double omega, const DevCtrl *ctrl);
 

@@ -1031,7 +1031,7 @@ int solve_icc(const lsg_operator *op, const lsg_params *prm, const int block[3],
     auto enqueue = [&](int it) -> int {
         const int cprev = ((it - 2) % m + m) % m;
         LSG_KC(LSG_K_PRECOND, icc_apply(F, g, r, Fv[fc ^ 1], Fv[fc], DF + (size_t)cprev * n, H + (size_t)cprev * n,
-                                        prm->beta, it > 1 ? 1 : 0, ctrl, s));
+                                        prm->beta, it > 1 ? 1 : 0, ctrl, L.exact, s));
         fc ^= 1;
         const double *f = Fv[fc];
         double *hcol = H + (size_t)((it - 1) % m) * n;
