@@ -477,6 +477,7 @@ def other_workloads(dev):
     / complex128 refinement, tol 1e-8); the differentiable batch of 16 real
     128^3 solves (mixed forward to 1e-9 + adjoint backward); GMRES(30), CG
     and AAR on the 256^3 workload at 1e-6."""
+    import numpy as np
     import torch
 
     import lsg
@@ -542,6 +543,31 @@ def other_workloads(dev):
         secs, (x, r) = timed(fn)
         cmp[name] = {"seconds": secs, "iters": r["iters"], "relres": r["relres"], "status": r["status_name"]}
     res["krylov_comparison_256_1e-6"] = cmp
+    # the complex comparison (PETSC_COMPLEX/main.c:47-175: AAR against GMRES and
+    # BiCG): one 96^3 shifted Helmholtz instance, sigma = 20 + 10i, complex128, 1e-6
+    n = 96
+    rng = np.random.default_rng(96)
+    bc = torch.from_numpy(rng.uniform(-0.5, 0.5, (n, n, n)) + 1j * rng.uniform(-0.5, 0.5, (n, n, n))).to(dev)
+    opc = lsg.Operator(n, a=-float(n * n), sigma=20 + 10j)
+    xfc = fft_reference(bc, opc)
+    ccmp = {}
+    for name, fn in (("aar", lambda: lsg.aar(opc, bc, tol=1e-6)),
+                     ("aar_mixed", lambda: lsg.aar_mixed(opc, bc, tol=1e-6)),
+                     ("gmres30", lambda: lsg.gmres(opc, bc, restart=30, tol=1e-6, max_iter=20000)),
+                     ("cocg", lambda: lsg.cocg(opc, bc, tol=1e-6))):
+        secs, (x, r) = timed(fn)
+        ccmp[name] = {"seconds": secs, "iters": r["iters"], "relres": r["relres"], "status": r["status_name"],
+                      "err_vs_fft": err_vs_fft(x, xfc, mean_free=False)}
+    res["helmholtz_krylov_comparison_96_1e-6"] = ccmp
+    # block-Jacobi ICC(0) AAR (the reference's pc = 1) against Jacobi on the 256^3 workload
+    op = lsg.Operator(N_GRID)
+    b = torch.from_numpy(workloads.uniform_rhs(N_GRID, SEED)).to(dev)
+    icc = {}
+    for name, fn in (("jacobi", lambda: lsg.aar(op, b, **SOLVER_KW)),
+                     ("icc0_8x8x8", lambda: lsg.aar_icc(op, b, block=(8, 8, 8), **SOLVER_KW))):
+        secs, (x, r) = timed(fn)
+        icc[name] = {"seconds": secs, "iters": r["iters"], "relres": r["relres"], "status": r["status_name"]}
+    res["aar_fp64_icc0_vs_jacobi_256"] = icc
     return res
 
 

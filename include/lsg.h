@@ -169,13 +169,25 @@ int lsg_aar_csr(const lsg_csr *A, const lsg_params *prm, double *d_x, const doub
 int lsg_apply_csr(const lsg_csr *A, const double *d_x, double *d_y, void *stream);
 
 /* Restarted GMRES(m), prm->m = restart length (the reference's comparator:
- * PETSc KSPGMRES, PETSC_REAL/main.c:84-122; PETSc's default restart is 30).
- * Left Jacobi preconditioning, classical Gram-Schmidt; stops when the GMRES
- * residual estimate reaches tol * ||M^-1 b|| and the true residual of the
- * restarted x confirms ||b - A x|| <= tol ||b||.  res->iters counts Arnoldi
- * steps.  dtype LSG_F64 or LSG_F32; omega, beta and p are unused. */
+ * PETSc KSPGMRES, PETSC_REAL/main.c:84-122 and, on the complex shifted
+ * operator, PETSC_COMPLEX/main.c:80-110; PETSc's default restart is 30).
+ * Left Jacobi preconditioning, classical Gram-Schmidt (Hermitian inner
+ * products and complex Givens rotations for complex vectors); stops when the
+ * GMRES residual estimate reaches tol * ||M^-1 b|| and the true residual of
+ * the restarted x confirms ||b - A x|| <= tol ||b||.  res->iters counts
+ * Arnoldi steps.  Any dtype; omega, beta and p are unused. */
 int lsg_gmres(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
               const void *d_b, lsg_result *res, void *stream);
+
+/* BiCG on the complex-symmetric shifted operator (the reference's KSPBICG,
+ * PETSC_COMPLEX/main.c:150-175), in its conjugate orthogonal CG form: with
+ * the shadow residual conj(r0) BiCG's shadow iterates are the conjugates of
+ * the primal ones, so one operator application per step suffices (van der
+ * Vorst & Melissen 1990).  Jacobi preconditioned; stops when ||b - A x|| <=
+ * tol ||b|| (checked every step).  dtype LSG_C128 or LSG_C64; m, omega, beta,
+ * p unused. */
+int lsg_cocg(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
+             const void *d_b, lsg_result *res, void *stream);
 
 /* Mixed precision: FP64 x and b (lsg_aar_mixed_c: complex128 x and b with a
  * complex64 inner iteration).  One FP32 AAR (FP32 vectors, history and

@@ -100,7 +100,7 @@ EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "ls
            "lsg_pinv_solve_noalloc", "lsg_aar_batched", "lsg_aar_mixed_batched", "lsg_autotune",
            "lsg_set_autotune", "lsg_autotune_save", "lsg_autotune_load", "lsg_gmres",
            "lsg_aar_csr", "lsg_apply_csr", "lsg_register_operator_csr", "lsg_bounds_errors",
-           "lsg_set_fp64_arith", "lsg_aar_icc", "lsg_icc_factor"]
+           "lsg_set_fp64_arith", "lsg_aar_icc", "lsg_icc_factor", "lsg_cocg"]
 
 KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "precond"]
 
@@ -126,7 +126,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
         L.lsg_params_default.argtypes = [C.POINTER(_Params)]
         L.lsg_params_default.restype = None
         L.lsg_apply.argtypes = [C.POINTER(_Operator), ip, vp, vp, vp]
-        for f in ("lsg_aar", "lsg_pgr", "lsg_pl2r", "lsg_cg", "lsg_gmres"):
+        for f in ("lsg_aar", "lsg_pgr", "lsg_pl2r", "lsg_cg", "lsg_gmres", "lsg_cocg"):
             getattr(L, f).argtypes = [C.POINTER(_Operator), C.POINTER(_Params), ip, vp, vp,
                                       C.POINTER(_Result), vp]
         L.lsg_aar_mixed.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), vp, vp,
@@ -360,7 +360,13 @@ def gmres(op, b, x0=None, restart=30, **kw):
     return _solve("lsg_gmres", op, b, x0, **kw)
 
 
-SOLVERS = {"aar": aar, "pgr": pgr, "pl2r": pl2r, "cg": cg, "gmres": gmres}
+def cocg(op, b, x0=None, **kw):
+    """BiCG on the complex-symmetric shifted operator in its COCG form (the
+    reference's KSPBICG, PETSC_COMPLEX/main.c:150-175); complex vectors."""
+    return _solve("lsg_cocg", op, b, x0, **kw)
+
+
+SOLVERS = {"aar": aar, "pgr": pgr, "pl2r": pl2r, "cg": cg, "gmres": gmres, "cocg": cocg}
 
 
 def aar_mixed(op, b, x0=None, stream=None, **kw):

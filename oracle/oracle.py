@@ -347,6 +347,105 @@ def gmres(b: np.ndarray, x0=None, *, restart=30, tol=1e-8, max_iter=2000, radius
         x = x + sum((y[i] * s[i]) * W[i] for i in range(k))
 
 
+def gmres_c(b: np.ndarray, x0=None, *, restart=30, tol=1e-8, max_iter=2000, radius=6, a=A_REF,
+            sigma=0.0, precond=True):
+    """Complex restarted GMRES(restart) for the complex-shifted operator
+    a*Lap + sigma (sigma complex), left Jacobi (cf = 1 / (3 a c_0 + sigma)),
+    classical Gram-Schmidt with Hermitian inner products, complex Givens
+    rotations G = [[c, s], [-conj(s), c]] (c = |h| / rho, s = (h / |h|) eta /
+    rho): the steps of lsg_gmres on complex vectors.  The reference runs
+    PETSc's KSPGMRES on its complex operator (PETSC_COMPLEX/main.c:80-110);
+    PETSc is absent, so this restates Saad & Schultz's algorithm."""
+    b = np.asarray(b, dtype=np.complex128)
+    x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.complex128, copy=True)
+    c = coefficients(radius)
+    sg = complex(sigma)
+    cf = 1.0 / (a * 3.0 * c[0] + sg) if precond else 1.0 + 0j
+    A = lambda v: apply_c(v, radius, a, sg)
+    bnorm = np.linalg.norm(b)
+    tol_abs = tol * bnorm
+    m = restart
+    iters = 0
+    acf = abs(cf)
+    while True:
+        r = b - A(x)
+        nr = np.linalg.norm(r)
+        if not nr > tol_abs or iters >= max_iter:
+            return x, dict(iters=iters, relres=nr / bnorm if bnorm > 0 else nr,
+                           converged=bool(not nr > tol_abs))
+        W = [r]
+        s = [(1.0 / nr) * (cf / acf)]
+        g = np.zeros(m + 1, dtype=np.complex128)
+        g[0] = acf * nr
+        H = np.zeros((m + 1, m), dtype=np.complex128)
+        cs, sn = np.zeros(m), np.zeros(m, dtype=np.complex128)
+        k = 0
+        for j in range(m):
+            z = cf * A(s[j] * W[j])
+            h = np.array([np.conj(s[i]) * np.vdot(W[i].ravel(), z.ravel()) for i in range(j + 1)])
+            H[:j + 1, j] = h
+            z = z - sum((h[i] * s[i]) * W[i] for i in range(j + 1))
+            eta = np.linalg.norm(z)
+            H[j + 1, j] = eta
+            W.append(z)
+            s.append(1.0 / eta if eta > 0 else 0.0)
+            for i in range(j):
+                t = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
+                H[i + 1, j] = cs[i] * H[i + 1, j] - np.conj(sn[i]) * H[i, j]
+                H[i, j] = t
+            aa = abs(H[j, j])
+            rr = np.hypot(aa, eta)
+            ph = H[j, j] / aa if aa > 0 else 1.0
+            cs[j], sn[j] = (aa / rr, (eta / rr) * ph) if rr > 0 else (1.0, 0.0)
+            H[j, j] = rr * ph
+            H[j + 1, j] = 0.0
+            g[j + 1] = -np.conj(sn[j]) * g[j]
+            g[j] = cs[j] * g[j]
+            k = j + 1
+            iters += 1
+            if abs(g[j + 1]) <= tol_abs * acf or iters >= max_iter or not eta > 0:
+                break
+        y = np.zeros(k, dtype=np.complex128)
+        for i in range(k - 1, -1, -1):
+            y[i] = (g[i] - H[i, i + 1:k] @ y[i + 1:k]) / H[i, i] if H[i, i] != 0 else 0.0
+        x = x + sum((y[i] * s[i]) * W[i] for i in range(k))
+
+
+def cocg(b: np.ndarray, x0=None, *, tol=1e-8, max_iter=100000, radius=6, a=A_REF, sigma=0.0, precond=True):
+    """Conjugate orthogonal CG (van der Vorst & Melissen 1990) for the
+    complex-symmetric operator a*Lap + sigma, Jacobi preconditioned: CG with
+    the bilinear form u^T v in place of u^H v.  It is BiCG (the reference's
+    KSPBICG, PETSC_COMPLEX/main.c:150-175) with the shadow residual conj(r0),
+    whose iterates then stay the conjugates of the primal ones, at one
+    operator application per step.  Convergence on ||r||_2 / ||b||_2."""
+    b = np.asarray(b, dtype=np.complex128)
+    x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.complex128, copy=True)
+    c = coefficients(radius)
+    sg = complex(sigma)
+    cf = 1.0 / (a * 3.0 * c[0] + sg) if precond else 1.0 + 0j
+    A = lambda v: apply_c(v, radius, a, sg)
+    bnorm = np.linalg.norm(b)
+    tol_abs = tol * bnorm
+    r = b - A(x)
+    rho = cf * np.sum(r * r)
+    d = np.zeros_like(b)
+    beta = 0.0
+    it = 0
+    nr = np.linalg.norm(r)
+    while nr > tol_abs and it < max_iter:
+        d = cf * r + beta * d
+        q = A(d)
+        alpha = rho / np.sum(d * q)
+        x = x + alpha * d
+        r = r - alpha * q
+        it += 1
+        rho_new = cf * np.sum(r * r)
+        beta = rho_new / rho
+        rho = rho_new
+        nr = np.linalg.norm(r)
+    return x, dict(iters=it, relres=nr / bnorm if bnorm > 0 else nr, converged=bool(not nr > tol_abs))
+
+
 # ----------------------------------------------------------------------------- AAR on any matrix
 
 def aar_general(matvec, dinv, b, x0=None, *, omega=0.6, beta=0.6, m=7, p=6, tol=1e-8, max_iter=100000,

@@ -80,3 +80,34 @@ def test_aar_mixed_complex(lsg, oracle, n, sigma):
     assert np.linalg.norm(x.cpu().numpy() - xf) <= kappa * 1e-8 * np.linalg.norm(xf)
     x32, r32 = lsg.aar(op, _t(b, torch.complex64), tol=1e-5)
     assert r32["status"] == 0
+
+
+def test_petsc_complex_driver_problem(lsg, oracle):
+    """PETSC_COMPLEX's own problem: 36^3 (system.c:26-28), A = -(1/(4 pi)) Lap_h
+    + Q with Q = -0.134992 - 0.070225i (system.c:217-220, 244), x0 = 1
+    (system.c:165), Jacobi (pc = 0), the README's run: tol 1e-6, m = 13, p = 11,
+    omega = 1.0, beta = 0.9, max_iter 2000 (main.c:51-52).  PETSc's random
+    generator is absent: b has real and imaginary parts U[0, 1) (VecSetRandom's
+    range) from seed 36.  The GPU complex AAR must take the restatement's
+    iteration count (99) and agree with it and with the FFT solve."""
+    import torch
+    n = 36
+    Q = complex(-0.134992, -0.070225)
+    rng = np.random.default_rng(36)
+    b = rng.uniform(0, 1, (n, n, n)) + 1j * rng.uniform(0, 1, (n, n, n))
+    x0 = np.ones((n, n, n), dtype=np.complex128)
+    kw = dict(omega=1.0, beta=0.9, m=13, p=11, tol=1e-6, max_iter=2000)
+    xo, ro = oracle.solve_c(b, x0, sigma=Q, **kw)
+    op = lsg.Operator(n, sigma=Q)
+    x, r = lsg.aar(op, torch.from_numpy(b).cuda(), torch.from_numpy(x0).cuda(), **kw)
+    assert ro["converged"] and r["status"] == 0
+    assert r["iters"] == ro["iters"], (r, ro)
+    assert r["relres"] == pytest.approx(ro["relres"], rel=2e-2)
+    xg = x.cpu().numpy()
+    assert np.linalg.norm(xg - xo) <= 1e-8 * np.linalg.norm(xo)
+    xf = oracle.fft_solve(b, sigma=Q)
+    lam = np.abs(oracle.symbol((n, n, n), sigma=Q))
+    assert np.linalg.norm(xg - xf) <= (lam.max() / lam.min()) * 1e-6 * np.linalg.norm(xf)
+    # complex64 inner iteration with complex128 refinement reaches the same tolerance
+    xm, rm = lsg.aar_mixed(op, torch.from_numpy(b).cuda(), torch.from_numpy(x0).cuda(), **kw)
+    assert rm["status"] == 0 and rm["relres"] <= 1e-6

@@ -1,0 +1,84 @@
+"""The reference's complex Krylov comparators (PETSC_COMPLEX/main.c:80-175:
+KSPGMRES and KSPBICG on the complex-shifted Helmholtz operator; PETSc is
+absent, so the oracle restates Saad & Schultz's GMRES with Hermitian inner
+products and complex Givens rotations, and BiCG in its conjugate orthogonal
+CG form for the complex-symmetric operator).  CPU: the restatements against
+the FFT solve.  GPU (through the C ABI): against the restatements -- Arnoldi /
+COCG step counts within 1, solutions to 1e-6 -- and complex64 runs."""
+import numpy as np
+import pytest
+
+
+def _problem(n, seed):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(-0.5, 0.5, (n, n, n)) + 1j * rng.uniform(-0.5, 0.5, (n, n, n))
+
+
+@pytest.mark.parametrize("sigma", [20 + 10j, 3 + 40j])
+def test_restatements_solve(oracle, sigma):
+    n = 12
+    b = _problem(n, 3)
+    a = -float(n * n)
+    xf = oracle.fft_solve(b, a=a, sigma=sigma)
+    for fn, kw in ((oracle.gmres_c, dict(restart=30, max_iter=5000)), (oracle.cocg, {})):
+        x, r = fn(b, a=a, sigma=sigma, tol=1e-10, **kw)
+        assert r["converged"], (fn.__name__, r)
+        assert np.linalg.norm(x - xf) <= 1e-7 * np.linalg.norm(xf), fn.__name__
+
+
+def test_complex_gmres_on_real_data_is_real_gmres(oracle):
+    n = 10
+    b = np.random.default_rng(5).uniform(-0.5, 0.5, (n, n, n))
+    b -= b.mean()
+    x1, r1 = oracle.gmres(b, tol=1e-8)
+    x2, r2 = oracle.gmres_c(b + 0j, tol=1e-8)
+    assert r1["iters"] == r2["iters"]
+    assert np.abs(x1 - x2.real).max() <= 1e-12 * np.abs(x1).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,sigma,restart", [(16, 20 + 10j, 30), (20, 3 + 40j, 10), ((24, 16, 12), 8 + 2j, 30)])
+def test_gpu_complex_gmres_matches_restatement(lsg, oracle, n, sigma, restart):
+    import torch
+    nx, ny, nz = (n, n, n) if isinstance(n, int) else n
+    rng = np.random.default_rng(nx + restart)
+    b = rng.uniform(-0.5, 0.5, (nz, ny, nx)) + 1j * rng.uniform(-0.5, 0.5, (nz, ny, nx))
+    a = -float(nx * nx)
+    xo, ro = oracle.gmres_c(b, restart=restart, tol=1e-9, a=a, sigma=sigma, max_iter=4000)
+    op = lsg.Operator((nx, ny, nz), a=a, sigma=sigma)
+    x, r = lsg.gmres(op, torch.from_numpy(b).cuda(), restart=restart, tol=1e-9, max_iter=4000)
+    assert r["status"] == 0 and ro["converged"]
+    assert abs(r["iters"] - ro["iters"]) <= 1, (r, ro)
+    x = x.cpu().numpy()
+    assert np.linalg.norm(x - xo) <= 1e-6 * np.linalg.norm(xo)
+    x64, r64 = lsg.gmres(op, torch.from_numpy(b).to(torch.complex64).cuda(), restart=restart, tol=1e-5,
+                         max_iter=4000)
+    assert r64["status"] == 0 and r64["relres"] <= 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,sigma", [(16, 20 + 10j), (20, 3 + 40j), ((24, 16, 12), 8 + 2j)])
+def test_gpu_cocg_matches_restatement(lsg, oracle, n, sigma):
+    import torch
+    nx, ny, nz = (n, n, n) if isinstance(n, int) else n
+    rng = np.random.default_rng(nx + 1)
+    b = rng.uniform(-0.5, 0.5, (nz, ny, nx)) + 1j * rng.uniform(-0.5, 0.5, (nz, ny, nx))
+    a = -float(nx * nx)
+    xo, ro = oracle.cocg(b, tol=1e-9, a=a, sigma=sigma)
+    op = lsg.Operator((nx, ny, nz), a=a, sigma=sigma)
+    x, r = lsg.cocg(op, torch.from_numpy(b).cuda(), tol=1e-9)
+    assert r["status"] == 0 and ro["converged"]
+    assert abs(r["iters"] - ro["iters"]) <= 1, (r, ro)
+    assert np.linalg.norm(x.cpu().numpy() - xo) <= 1e-6 * np.linalg.norm(xo)
+    xf = oracle.fft_solve(b, a=a, sigma=sigma)
+    assert np.linalg.norm(x.cpu().numpy() - xf) <= 1e-6 * np.linalg.norm(xf)
+    x64, r64 = lsg.cocg(op, torch.from_numpy(b).to(torch.complex64).cuda(), tol=1e-5)
+    assert r64["status"] == 0 and r64["relres"] <= 1e-5
+
+
+@pytest.mark.gpu
+def test_gpu_cocg_rejects_real(lsg):
+    import torch
+    b = torch.zeros((8, 8, 8), dtype=torch.float64, device="cuda")
+    with pytest.raises(lsg.CudaLibraryError):
+        lsg.cocg(lsg.Operator(8), b)
