@@ -1146,6 +1146,41 @@ __global__ void __launch_bounds__(kReduceThreads) gram_c_kernel(const cplx<R> *_
     gram_c_block<R, M>(df, r, n, partials + (long long)blockIdx.x * 2 * NV, blockIdx.x, gridDim.x);
 }
 
+// Generic Hermitian Gram for complex vectors, m > 8: one value per
+// (block, value slot), G(a,j) = DF_a^H DF_j (a <= j) or h_j = DF_j^H r, the
+// columns re-read per value from L2; partials laid out as gram_c_block's
+// (2 reals per value, nv values per block).
+template <typename R>
+__global__ void __launch_bounds__(kReduceThreads) gram_generic_c_kernel(int m, const cplx<R> *__restrict__ df,
+                                                                        const cplx<R> *__restrict__ r, long long n,
+                                                                        int nv, double *partials,
+                                                                        const DevCtrl *ctrl) {
+    __shared__ double red[(kReduceThreads / 32) * 2];
+    __shared__ double out[2];
+    if (solve_done(ctrl)) return;
+    const int v = blockIdx.y;
+    const int np = (m * (m + 1)) / 2;
+    const cplx<R> *u, *w;
+    if (v < np) {
+        int j = 0;
+        while ((j + 1) * (j + 2) / 2 <= v) j++;
+        const int a = v - j * (j + 1) / 2;
+        u = df + (long long)a * n;
+        w = df + (long long)j * n;
+    } else {
+        u = df + (long long)(v - np) * n;
+        w = r;
+    }
+    Acc<cplx<R>> acc[1];
+    acc[0].zero();
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        acc[0].add_prod(ldg(u + i), ldg(w + i));
+    block_reduce_store<1>(acc, red, out);
+    __syncthreads();
+    if (threadIdx.x < 2) partials[((long long)blockIdx.x * nv + v) * 2 + threadIdx.x] = out[threadIdx.x];
+}
+
 template <typename T, int KIND>
 static cudaError_t gram_dispatch(int m, const T *dx, const T *df, const T *r, long long n,
                                  double *partials, int blocks, const DevCtrl *ctrl,
@@ -1244,7 +1279,11 @@ cudaError_t Kernels<T>::gram(int kind, int m, const T *dx, const T *df, const T 
             LSG_GRAMC_CASE(1) LSG_GRAMC_CASE(2) LSG_GRAMC_CASE(3) LSG_GRAMC_CASE(4)
             LSG_GRAMC_CASE(5) LSG_GRAMC_CASE(6) LSG_GRAMC_CASE(7) LSG_GRAMC_CASE(8)
 #undef LSG_GRAMC_CASE
-        default: return cudaErrorInvalidValue;
+        default: {
+            if (m < 1 || 2 * m > LSG_MAX_M) return cudaErrorInvalidValue;
+            const int nv = (m * (m + 1)) / 2 + m;
+            gram_generic_c_kernel<R><<<dim3(blocks, nv), kReduceThreads, 0, s>>>(m, df, r, n, nv, partials, ctrl);
+        }
         }
         return cudaGetLastError();
     } else {

@@ -406,7 +406,7 @@ static int gmres_t(const lsg_operator *op, const lsg_params *prm, T *x, const T 
     };
 #define LSG_GK(call) do { int rc_ = chk(call); if (rc_) return rc_; } while (0)
     LSG_GK(Kernels<T>::norm2(b, n, part, rb, ctrl, s));
-    LSG_GK(finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, s));
+    LSG_GK(finalize_norm(part, rb, ctrl, NF_RHS, prm->tol, 0, s, AccWidth<T>::value));
     auto restart = [&]() -> int {
         LSG_GK(Kernels<T>::residual(L, w, RES_INIT, x, b, V, nullptr, nullptr, 1.0, 0.0, part, ctrl));
         gmres_restart_kernel<S><<<1, 256, 0, s>>>(part, (int)sb, cf, prm->max_iter, st, ctrl);
