@@ -53,8 +53,15 @@ LARGE_GOLDEN = os.path.join(ROOT, "tests", "golden", "large_256.json")
 CPU_SAMPLE_ITERS = 24
 # DRAM bytes (read + write) of one launch of the dominant kernel at this
 # workload, from an ncu capture of that kernel on this workload (a constant:
-# the timed run is not captured).
-RICH32_TRAFFIC_BYTES = 224.2e6
+# the timed run is not captured); keyed by "residual ring in use".
+RICH32_TRAFFIC_BYTES = {False: 224.2e6, True: None}
+
+
+def aar_form_in_use(lsg):
+    """The FP32 AAR form the library will run (0 ring, 1 lean, 2 x-carrying)."""
+    f = lsg.set_aar_form(0)
+    lsg.set_aar_form(f)
+    return f
 FP64_SOLVERS = ("aar", "pgr", "pl2r", "cg")
 
 
@@ -379,9 +386,11 @@ def run_lsg(args):
     peak, peak_kind = _peaks()
     rl, rms = prof["richardson"]
     rich_ms = rms / max(rl, 1)
-    # the FP32 inner solver's fused step in residual-recurrence form, x left
-    # out: reads r (stencil); writes r', the H column and the DF column
-    rich_bytes = 4 * N * 4
+    # the FP32 inner solver's Richardson pass: in the residual-ring form it
+    # reads r_{k-1} (stencil) and writes r_k; the lean form also writes the H
+    # and DF columns
+    ring = aar_form_in_use(lsg) == 0
+    rich_bytes = (2 if ring else 4) * N * 4
     achieved = rich_bytes / (rich_ms * 1e-3) / 1e9
     total_ms = sum(v[1] for v in prof.values())
     r64l, r64ms = prof64["richardson"]
@@ -443,14 +452,19 @@ def run_lsg(args):
                           "frac_fp64_arith": rich64_bytes / (rich64x_ms * 1e-3) / 1e9 / peak,
                           "bound": "issue (double-float arithmetic, ~950 instructions per point)"},
         "roofline": {"bound": "hbm",
-                     "kernel": "stencil_x2_kernel<float, RichLeanOp> in the tuned paired shape (fused Richardson step, x left out)",
+                     "kernel": ("stencil_x2_kernel<float, RichRingOp> in the tuned paired shape (Richardson step of "
+                                "the residual ring: r_k only)" if ring else
+                                "stencil_x2_kernel<float, RichLeanOp> in the tuned paired shape (fused Richardson "
+                                "step, x left out)"),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
-                     "traffic": RICH32_TRAFFIC_BYTES, "traffic_unit": "bytes per launch (ncu)",
+                     "traffic": RICH32_TRAFFIC_BYTES[ring], "traffic_unit": "bytes per launch (ncu)",
                      "traffic_source": "constant from an ncu capture of this kernel on this workload, not of this run",
                      "bytes_per_launch": rich_bytes, "avg_launch_ms": rich_ms,
-                     "note": ("lean form: 4 vectors per launch (x left out; the x-carrying form moved 6 and ran "
-                              "at a higher fraction but slower); latency-bound at 16 warps/SM, see the profile"),
+                     "note": ("residual ring: 2 vectors per launch (the H and DF columns are rebuilt from "
+                              "consecutive residuals by the Gram and update kernels; the lean form moved 4, the "
+                              "x-carrying form 6)" if ring else
+                              "lean form: 4 vectors per launch (x left out; the x-carrying form moved 6)"),
                      "share_of_kernel_time": rms / total_ms if total_ms else None},
         "kernel_profile_ms": {k: round(v[1], 4) for k, v in prof.items() if v[0]},
         "updates_per_s": {"mixed": N * infos[-1]["inner_iters"] / value, "fp64": N * fp64["aar"]["iters"] / fp64_s},

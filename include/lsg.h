@@ -115,6 +115,18 @@ void lsg_params_default(lsg_params *prm);
  * always uses FP64 arithmetic. */
 int lsg_set_fp64_arith(int mode);
 
+/* Form of the FP32 (and mixed-precision inner) AAR's Richardson passes, all
+ * giving the same residuals, history columns and extrapolation steps bit for
+ * bit.  0 (default): the residual ring -- a pass reads r_{k-1} and writes r_k
+ * only, into a ring of m + 1 residuals from which the Gram and update kernels
+ * rebuild DF_k = (r_k - r_{k-1}) cf and H_k = c r_{k-1} + beta DF_k (m <= 8,
+ * p - 1 <= m, grid size a multiple of 4, 16-byte aligned x; otherwise 1).
+ * 1: the lean form (r', H, DF stored; x rebuilt at each extrapolation).
+ * 2: the x-carrying recurrence (x, r', H, DF stored), whose iterates form 0
+ * reproduces bit for bit.  LSG_AAR_FORM sets the value at load.  Returns the
+ * previous form, or -1 for a form outside 0..2. */
+int lsg_set_aar_form(int form);
+
 /* y = A x on the device (replaces MPI_REAL/system.c:80-213). */
 int lsg_apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, void *stream);
 

@@ -73,8 +73,10 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // (FP64) to out[0..NV).  `scratch` is NV * 32 doubles of shared memory.
 // FP32 accumulators are reduced as double-float pairs with FP32 instructions;
 // only the NV final conversions to double touch the (slow) FP64 pipe.
+// perm (optional, shared memory): total k goes to out[perm[k]].
 template <int NV, typename T>
-__device__ __forceinline__ void block_reduce_store(Acc<T> (&acc)[NV], double *scratch, double *out) {
+__device__ __forceinline__ void block_reduce_store(Acc<T> (&acc)[NV], double *scratch, double *out,
+                                                   const int *perm = nullptr) {
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     const int lane = tid & 31, warp = tid >> 5;
     const int nwarps = (blockDim.x * blockDim.y) >> 5;
@@ -88,7 +90,7 @@ __device__ __forceinline__ void block_reduce_store(Acc<T> (&acc)[NV], double *sc
         for (int k = warp; k < NV; k += nwarps) {
             double s = lane < nwarps ? scratch[k * nwarps + lane] : 0.0;
             s = warp_sum_d(s);
-            if (lane == 0) out[k] = s;
+            if (lane == 0) out[perm ? perm[k] : k] = s;
         }
     } else {
         float2 *sf = reinterpret_cast<float2 *>(scratch);
@@ -103,7 +105,7 @@ __device__ __forceinline__ void block_reduce_store(Acc<T> (&acc)[NV], double *sc
             float hi = 0.f, lo = 0.f;
             if (lane < nwarps) { const float2 v = sf[k * nwarps + lane]; hi = v.x; lo = v.y; }
             df_warp_sum(hi, lo);
-            if (lane == 0) out[k] = (double)hi + (double)lo;
+            if (lane == 0) out[perm ? perm[k] : k] = (double)hi + (double)lo;
         }
     }
 }

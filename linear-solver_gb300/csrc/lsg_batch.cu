@@ -504,7 +504,8 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
         memset((void *)&I, 0, sizeof(I));
         I.g = geo[i];
         constexpr int VN = IsCplx<T>::value ? 0 : (int)(16 / sizeof(T));
-        I.vec = VN > 0 && geo[i].n % VN == 0;
+        // x is the caller's vector (the rest are work arrays): 16-byte loads only when it is aligned
+        I.vec = VN > 0 && geo[i].n % VN == 0 && (((uintptr_t)xs[i]) & 15u) == 0;
         I.w = make_weights<T>(&ops[i]);
         I.w64 = make_weights<TW>(&ops[i]);
         const typename ScalarOf<T>::type cf = jacobi_factor<T>(&ops[i]);

@@ -177,6 +177,8 @@ int fp64_exact();
 // the FP64-arithmetic march.
 constexpr double kDfMinTol = 1e-10;
 int fp64_exact_for(double tol);
+// Form of the FP32 AAR's Richardson passes (lsg_set_aar_form): 0 ring, 1 lean, 2 x-carrying.
+int aar_form();
 int check_params(const lsg_params *prm, bool history);
 // Initial control block: relres = tol + 1 (AAR.c:76), stall rule off (0) or on.
 DevCtrl ctrl_init(double tol, int stall_limit);
@@ -240,6 +242,28 @@ enum RichMode {
 enum GramKind {
     GRAM_SYM = 0,     // G(i,j) = DF_i.DF_j (i <= j, symmetrised), h(j) = DF_j.r * hscale
     GRAM_GALERKIN = 1 // G(i,j) = DX_i.DF_j (all i,j), h(j) = DX_j.r * hscale
+};
+
+// The residual ring of the FP32 AAR.  The Richardson passes keep only the
+// residual sequence: r_k (after iteration k) lives in ring slot k mod (m + 1),
+// and history column k (written at iteration k, column (k - 1) mod m) is
+//   DF_k = (r_k - r_{k-1}) cf,   H_k = c r_{k-1} + beta DF_k   (c = omega cf),
+// rebuilt from two ring slots, with the arithmetic the x-carrying pass uses,
+// wherever it is read.  Extrapolation columns (H_k = step + beta DF_k) keep H
+// in the history array; a column whose r_k is later overwritten (the FP64
+// residual replacement of a mixed solve) has DF (and H) stored first.
+// RingWindow is one extrapolation's view: time t = 0..m-1 is the column of
+// iteration k = it - m + t, column (s0 + t) mod m, read from slot[t] (r_{k-1})
+// and slot[t + 1] (r_k); slot[m] holds the current residual r_{it-1}.
+constexpr int kRingMaxM = 8;
+struct RingWindow {
+    int slot[kRingMaxM + 1];
+    int s0;
+    unsigned valid;  // bit t: the column exists (k >= 1)
+    unsigned hmem;   // bit t: H stored in the history array
+    unsigned dfmem;  // bit t: DF stored in the history array
+    unsigned cyc;    // bit t: a Richardson step of the current cycle not yet added to x
+    int e0, e1;      // times of the first two H-stored columns (-1: none)
 };
 
 struct StencilLaunch {
@@ -389,6 +413,29 @@ struct Kernels {
     static cudaError_t residual_recur(const StencilLaunch &L, const Weights<T> &w, const T *step,
                                       T *r, T *df, T *hc, S cf, double hb, double *partials,
                                       const DevCtrl *ctrl);
+    // ---- residual ring (FP32 only; other types return cudaErrorInvalidValue)
+    // Richardson pass: r2 = r - c A r (nothing else is stored).
+    static cudaError_t ring_richardson(const StencilLaunch &L, const Weights<T> &w, const T *r, T *r2, S c,
+                                       const DevCtrl *ctrl);
+    // Extrapolation-step residual: r2 = r - A step, H column hc = step + hb (r2 - r) cf, ||r2||^2.
+    static cudaError_t ring_residual(const StencilLaunch &L, const Weights<T> &w, const T *step, const T *r,
+                                     T *r2, T *hc, S cf, double hb, double *partials, const DevCtrl *ctrl);
+    // Gram partials of the window's columns (column order, as gram() writes them).
+    static cudaError_t ring_gram(int m, const RingWindow &rw, const T *ring, long long ss, const T *df, S cf,
+                                 long long n, double *partials, int blocks, DevCtrl *ctrl, cudaStream_t s);
+    // Extrapolation: x += the cycle's Richardson steps c r_{k-1} (in order),
+    // step = beta cf r - sum_j H_j s_j, x += step.
+    static cudaError_t ring_update(int m, const RingWindow &rw, const T *ring, long long ss, const T *h, T *x,
+                                   T *step, S c, double beta, S cf, long long n, const DevCtrl *ctrl,
+                                   cudaStream_t s);
+    // x += the cycle's Richardson steps (a solve stopped between extrapolations).
+    static cudaError_t ring_fold(int m, const RingWindow &rw, const T *ring, long long ss, T *x, S c, long long n,
+                                 cudaStream_t s);
+    // df = (rk - rk1) cf; h (if not null) = c rk1 + hb df.
+    static cudaError_t ring_store_column(const T *rk1, const T *rk, T *df, T *h, S c, double hb, S cf,
+                                         long long n, cudaStream_t s);
+    // Paired-march z depth and block count of the ring passes (0 when T has none).
+    static long long ring_paired_plan(const Geom &g, int *lz);
     // Grid of one Gram launch (one wave); partials written = grid * values.
     static int gram_grid(int kind, int m, long long n, int sms);
     // Gram partials over the history (point-local, grid-stride).  Complex

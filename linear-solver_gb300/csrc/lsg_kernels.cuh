@@ -404,6 +404,81 @@ struct IrResidualOp {
     }
 };
 
+// Richardson step of the residual ring: r2 = r - c A r and nothing else (two
+// vectors per pass); the column's DF and H are rebuilt from r and r2 where
+// they are read (RingWindow).  r2 is RichLeanOp's r2 bit for bit.
+template <typename T>
+struct RichRingOp {
+    static constexpr int NACC = 0;
+    using Raw = T;
+    using Ctr = NoCtr;
+    const T *r;
+    T *r2;
+    T c;  // omega * cf
+    double *partials;
+    const DevCtrl *ctrl;
+    __device__ bool skip() const { return solve_done(ctrl); }
+    __device__ void init() {}
+    __device__ __forceinline__ Raw fetch(unsigned i) const { return ldg(r + i); }
+    __device__ __forceinline__ T value(const Raw &v) const { return v; }
+    __device__ __forceinline__ Ctr fetch_center(unsigned) const { return NoCtr{}; }
+    __device__ __forceinline__ void store(unsigned i, T rc, T ar, const Ctr &, Acc<T> *) const {
+        r2[i] = fma(-c, ar, rc);
+    }
+    static constexpr bool PAIRED = true;
+    static constexpr bool PACKED = false;  // packed sums spill here
+    __host__ __device__ const void *pair_ptrs_or() const { return (const void *)((uintptr_t)r | (uintptr_t)r2); }
+    __device__ __forceinline__ Two<T> fetch_pair(unsigned i) const { return ld_pair(r + i); }
+    __device__ __forceinline__ Two<T> center_pair(unsigned) const { return Two<T>{T(0), T(0)}; }
+    __device__ __forceinline__ void store_pair(unsigned i, Two<T> rc, Two<T> ar, Two<T>, Acc<T> *) const {
+        st_pair(r2 + i, fma(-c, ar.a, rc.a), fma(-c, ar.b, rc.b));
+    }
+};
+
+// Extrapolation-step residual of the residual ring: r2 = r - A step into the
+// next ring slot (r stays), H_col = step + beta DF_col stored, ||r2||^2; DF_col
+// is rebuilt from r and r2.  The arithmetic of ResRecurOp.
+template <typename T>
+struct ResRingOp {
+    static constexpr int NACC = 1;
+    using Raw = T;
+    using Ctr = T;  // r at the centre
+    const T *stp;
+    const T *r;
+    T *r2;
+    T *hc;
+    T cf;
+    T hb;
+    double *partials;
+    const DevCtrl *ctrl;
+    __device__ bool skip() const { return solve_done(ctrl); }
+    __device__ void init() {}
+    __device__ __forceinline__ Raw fetch(unsigned i) const { return ldg(stp + i); }
+    __device__ __forceinline__ T value(const Raw &v) const { return v; }
+    __device__ __forceinline__ Ctr fetch_center(unsigned i) const { return ldg(r + i); }
+    __device__ __forceinline__ void store(unsigned i, T step, T au, const Ctr &ro, Acc<T> *acc) const {
+        const T rn = ro - au;
+        const T dfv = (rn - ro) * cf;
+        hc[i] = fma(hb, dfv, step);
+        r2[i] = rn;
+        acc[0].add_prod(rn, rn);
+    }
+    static constexpr bool PAIRED = true;
+    __host__ __device__ const void *pair_ptrs_or() const {
+        return (const void *)((uintptr_t)stp | (uintptr_t)r | (uintptr_t)r2 | (uintptr_t)hc);
+    }
+    __device__ __forceinline__ Two<T> fetch_pair(unsigned i) const { return ld_pair(stp + i); }
+    __device__ __forceinline__ Two<T> center_pair(unsigned i) const { return ld_pair(r + i); }
+    __device__ __forceinline__ void store_pair(unsigned i, Two<T> st, Two<T> au, Two<T> ro, Acc<T> *acc) const {
+        const T rna = ro.a - au.a, rnb = ro.b - au.b;
+        const T dfa = (rna - ro.a) * cf, dfb = (rnb - ro.b) * cf;
+        st_pair(hc + i, fma(hb, dfa, st.a), fma(hb, dfb, st.b));
+        st_pair(r2 + i, rna, rnb);
+        acc[0].add_prod(rna, rna);
+        acc[0].add_prod(rnb, rnb);
+    }
+};
+
 // ---------------------------------------------------------------- stencil dispatch
 
 template <class Op, class = void> struct IsPaired { static constexpr bool value = false; };
@@ -557,6 +632,12 @@ int Kernels<T>::stencil_blocks_per_sm(int var) {
 // points per thread and step (one 16-byte load per vector).  FP32 vectors:
 // the VEC products of a step are summed in FP32 and folded into a
 // double-float accumulator (lsg_accum.cuh); FP64 vectors: FP64 FMAs.
+// True when every pointer is 16-byte aligned (nullptr counts as aligned).
+template <typename... P>
+inline bool aligned16(const P *...p) {
+    return ((((uintptr_t)p) | ... | (uintptr_t)0) & 15u) == 0;
+}
+
 template <typename T> struct Vec4;
 template <> struct Vec4<float> { using type = float4; static constexpr int N = 4; };
 template <> struct Vec4<double> { using type = double2; static constexpr int N = 2; };
@@ -694,11 +775,19 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *b, unsigne
 // extra_tx: bytes armed on each stage beyond the copies' (0; the failure
 // test arms more, so the waits run out and the timeout path is taken);
 // wait_cycles: the limit of every wait.
-template <int M>
+// RING: the columns come from the residual ring (RingWindow rw, slots ss
+// floats apart): the stage holds r_{it-m-1} .. r_{it-1} in time order, the
+// block rebuilds DF_t = (r_t+1 - r_t) cf (stored columns, rw.dfmem, straight
+// from df), accumulates in time order and writes each sum at its column-order
+// place, so the partials equal gram()'s over the same columns bit for bit.
+template <int M, bool RING = false>
 __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const float *__restrict__ df,
                                                                      const float *__restrict__ r, long long n,
                                                                      double *partials, DevCtrl *ctrl,
-                                                                     unsigned extra_tx, long long wait_cycles) {
+                                                                     unsigned extra_tx, long long wait_cycles,
+                                                                     const float *__restrict__ ring = nullptr,
+                                                                     long long ss = 0, RingWindow rw = {},
+                                                                     float cf = 1.f) {
     constexpr int NP = (M * (M + 1)) / 2;
     constexpr int NV = NP + M;
     constexpr int S = kGramStages, CH = kGramChunk, CV = CH / 4;
@@ -706,6 +795,7 @@ __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const floa
     __shared__ __align__(8) unsigned long long full[S];
     __shared__ double red[NV * (kReduceThreads / 32)];
     __shared__ int abort_flag;
+    __shared__ int perm[RING ? NV : 1];
     if (solve_done(ctrl)) return;
     const int tid = threadIdx.x;
     const long long nchunk = (n + CH - 1) / CH;
@@ -716,6 +806,22 @@ __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const floa
         abort_flag = 0;
         mbar_init_fence();
     }
+    if constexpr (RING) {
+        if (tid < NV) {  // time-order sum -> column-order place
+            int o;
+            if (tid < NP) {
+                int tj = 0;
+                while ((tj + 1) * (tj + 2) / 2 <= tid) tj++;
+                const int ta = tid - tj * (tj + 1) / 2;
+                const int ca = (rw.s0 + ta) % M, cj = (rw.s0 + tj) % M;
+                const int lo = ca < cj ? ca : cj, hi = ca < cj ? cj : ca;
+                o = hi * (hi + 1) / 2 + lo;
+            } else {
+                o = NP + (rw.s0 + tid - NP) % M;
+            }
+            perm[tid] = o;
+        }
+    }
     __syncthreads();
     auto issue = [&](long long k) {  // the block's k-th chunk into stage k % S (thread 0)
         const long long off = (first + k * step) * CH;
@@ -723,9 +829,14 @@ __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const floa
         unsigned long long *bar = &full[k % S];
         float *dst = gsm + (size_t)(k % S) * (M + 1) * CH;
         mbar_expect_tx(bar, bytes * (M + 1) + extra_tx);
+        if constexpr (RING) {
 #pragma unroll
-        for (int v = 0; v < M; v++) bulk_g2s(dst + v * CH, df + (long long)v * n + off, bytes, bar);
-        bulk_g2s(dst + M * CH, r + off, bytes, bar);
+            for (int v = 0; v <= M; v++) bulk_g2s(dst + v * CH, ring + (long long)rw.slot[v] * ss + off, bytes, bar);
+        } else {
+#pragma unroll
+            for (int v = 0; v < M; v++) bulk_g2s(dst + v * CH, df + (long long)v * n + off, bytes, bar);
+            bulk_g2s(dst + M * CH, r + off, bytes, bar);
+        }
     };
     if (tid == 0)
         for (long long k = 0; k < S && k < mine; k++) issue(k);
@@ -742,9 +853,31 @@ __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const floa
             if (off + 4 * tid < n) {
                 const float4 *src = reinterpret_cast<const float4 *>(gsm + (size_t)st * (M + 1) * CH);
                 float4 f[M];
+                float4 rv;
+                if constexpr (RING) {
+                    float4 u[M + 1];
 #pragma unroll
-                for (int v = 0; v < M; v++) f[v] = src[v * CV + tid];
-                const float4 rv = src[M * CV + tid];
+                    for (int v = 0; v <= M; v++) u[v] = src[v * CV + tid];
+#pragma unroll
+                    for (int t = 0; t < M; t++) {
+                        float4 d;
+                        if ((rw.dfmem >> t) & 1u) {
+                            d = ldg(reinterpret_cast<const float4 *>(df + (long long)((rw.s0 + t) % M) * n + off) + tid);
+                        } else {
+                            d.x = (u[t + 1].x - u[t].x) * cf;
+                            d.y = (u[t + 1].y - u[t].y) * cf;
+                            d.z = (u[t + 1].z - u[t].z) * cf;
+                            d.w = (u[t + 1].w - u[t].w) * cf;
+                        }
+                        if (!((rw.valid >> t) & 1u)) d = make_float4(0.f, 0.f, 0.f, 0.f);
+                        f[t] = d;
+                    }
+                    rv = u[M];
+                } else {
+#pragma unroll
+                    for (int v = 0; v < M; v++) f[v] = src[v * CV + tid];
+                    rv = src[M * CV + tid];
+                }
                 int q = 0;
 #pragma unroll
                 for (int j = 0; j < M; j++)
@@ -772,7 +905,7 @@ __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const floa
         }
         return;
     }
-    block_reduce_store<NV>(acc, red, partials + (long long)blockIdx.x * NV);
+    block_reduce_store<NV>(acc, red, partials + (long long)blockIdx.x * NV, RING ? perm : nullptr);
 }
 
 template <int M>
@@ -942,6 +1075,130 @@ __global__ void __launch_bounds__(kReduceThreads) aar_update_lean_kernel(int m, 
     aar_update_block<T, M, (M > 0), true>(m, x, r, h, step, beta, cf, n, ctrl, blockIdx.x, gridDim.x, rs, mask);
 }
 
+// ---- residual-ring extrapolation (FP32, RingWindow).  Per point: the m + 1
+// ring residuals r_{it-m-1} .. r_{it-1}, the stored H columns (rw.hmem) and x;
+// the other columns' H_t = c r_t + beta (r_t+1 - r_t) cf as the Richardson
+// pass rounds it; am = sum_j H_j s_j summed in column order j = 0..m-1 (the
+// window's time order rotated by s0, a template parameter), so the step equals
+// aar_update's over the same columns bit for bit; x first takes the cycle's
+// Richardson steps x = fma(c, r_{k-1}, x) in iteration order, as the
+// x-carrying pass applies them.
+template <int M, int ROT>
+__device__ __forceinline__ void ring_update_loop(const float *__restrict__ ring, long long ss, const RingWindow &rw,
+                                                 const float *__restrict__ hm, float *__restrict__ x,
+                                                 float *__restrict__ step, float c, float beta, float cf,
+                                                 long long n, const float *sj) {
+    // one float4 per thread (no grid-stride loop: nothing loop-invariant to keep in registers)
+    const long long nv = n / 4;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const float4 *r4 = reinterpret_cast<const float4 *>(ring);
+    const long long ss4 = ss / 4;
+    const float4 *h4 = reinterpret_cast<const float4 *>(hm);
+    float4 *x4 = reinterpret_cast<float4 *>(x);
+    float4 *s4 = reinterpret_cast<float4 *>(step);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    {
+        float4 u[M + 1];
+#pragma unroll
+        for (int t = 0; t <= M; t++) u[t] = ldg(r4 + rw.slot[t] * ss4 + i);
+        // the first two stored H columns are loaded with the ring (more only when p is small)
+        const float4 hx0 = rw.e0 >= 0 ? ldg(h4 + (long long)((ROT + rw.e0) % M) * nv + i) : zero;
+        const float4 hx1 = rw.e1 >= 0 ? ldg(h4 + (long long)((ROT + rw.e1) % M) * nv + i) : zero;
+        float4 xo = x4[i];
+#pragma unroll
+        for (int t = 0; t < M; t++)
+            if ((rw.cyc >> t) & 1u) {
+                xo.x = fma(c, u[t].x, xo.x);
+                xo.y = fma(c, u[t].y, xo.y);
+                xo.z = fma(c, u[t].z, xo.z);
+                xo.w = fma(c, u[t].w, xo.w);
+            }
+        float4 am = zero;
+#pragma unroll
+        for (int j = 0; j < M; j++) {
+            const int t = (j + M - ROT) % M;  // the column's time in the window
+            float4 h;
+            if (t == rw.e0) {
+                h = hx0;
+            } else if (t == rw.e1) {
+                h = hx1;
+            } else if ((rw.hmem >> t) & 1u) {
+                h = ldg(h4 + (long long)j * nv + i);
+            } else {
+                h.x = fma(beta, (u[t + 1].x - u[t].x) * cf, c * u[t].x);
+                h.y = fma(beta, (u[t + 1].y - u[t].y) * cf, c * u[t].y);
+                h.z = fma(beta, (u[t + 1].z - u[t].z) * cf, c * u[t].z);
+                h.w = fma(beta, (u[t + 1].w - u[t].w) * cf, c * u[t].w);
+            }
+            if (!((rw.valid >> t) & 1u)) h = zero;
+            am.x = fma(h.x, sj[j], am.x);
+            am.y = fma(h.y, sj[j], am.y);
+            am.z = fma(h.z, sj[j], am.z);
+            am.w = fma(h.w, sj[j], am.w);
+        }
+        float4 xn, st;
+        update_point<float, false>(xo.x, u[M].x, u[M].x, am.x, 0.f, beta, cf, xn.x, st.x);
+        update_point<float, false>(xo.y, u[M].y, u[M].y, am.y, 0.f, beta, cf, xn.y, st.y);
+        update_point<float, false>(xo.z, u[M].z, u[M].z, am.z, 0.f, beta, cf, xn.z, st.z);
+        update_point<float, false>(xo.w, u[M].w, u[M].w, am.w, 0.f, beta, cf, xn.w, st.w);
+        x4[i] = xn;
+        s4[i] = st;
+    }
+}
+
+template <int M>
+__global__ void __launch_bounds__(kReduceThreads) aar_update_ring_kernel(const float *__restrict__ ring, long long ss,
+                                                                         RingWindow rw, const float *__restrict__ hm,
+                                                                         float *__restrict__ x,
+                                                                         float *__restrict__ step, float c,
+                                                                         float beta, float cf, long long n,
+                                                                         const DevCtrl *ctrl) {
+    __shared__ float s[M];
+    if (solve_done(ctrl)) return;
+    if (threadIdx.x < M) s[threadIdx.x] = ctrl_s<float>(ctrl, threadIdx.x);
+    __syncthreads();
+    float sj[M];
+#pragma unroll
+    for (int j = 0; j < M; j++) sj[j] = s[j];
+    switch (rw.s0) {
+#define LSG_RING_ROT(R) \
+    case R: if constexpr (R < M) ring_update_loop<M, R>(ring, ss, rw, hm, x, step, c, beta, cf, n, sj); break;
+        LSG_RING_ROT(0) LSG_RING_ROT(1) LSG_RING_ROT(2) LSG_RING_ROT(3)
+        LSG_RING_ROT(4) LSG_RING_ROT(5) LSG_RING_ROT(6) LSG_RING_ROT(7)
+#undef LSG_RING_ROT
+    default: break;
+    }
+}
+
+// x += the cycle's Richardson steps, x = fma(c, r_{k-1}, x) in iteration order.
+static __global__ void __launch_bounds__(kReduceThreads) ring_fold_kernel(int m, const float *__restrict__ ring,
+                                                                   long long ss, RingWindow rw,
+                                                                   float *__restrict__ x, float c, long long n) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        float xo = x[i];
+        for (int t = 0; t < m; t++)
+            if ((rw.cyc >> t) & 1u) xo = fma(c, ldg(ring + (long long)rw.slot[t] * ss + i), xo);
+        x[i] = xo;
+    }
+}
+
+// One history column from two consecutive residuals: df = (rk - rk1) cf and,
+// when h is set, h = c rk1 + hb df (the Richardson pass's rounding).
+static __global__ void __launch_bounds__(kReduceThreads) ring_column_kernel(const float *__restrict__ rk1,
+                                                                     const float *__restrict__ rk,
+                                                                     float *__restrict__ df, float *__restrict__ h,
+                                                                     float c, float hb, float cf, long long n) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float a = rk1[i];
+        const float dfv = (rk[i] - a) * cf;
+        df[i] = dfv;
+        if (h) h[i] = fma(hb, dfv, c * a);
+    }
+}
+
 // x += sum_mask H_j - beta cf (r - rs): the iterate of a lean FP32 solve that
 // stopped between extrapolations (its Richardson passes left x out).
 template <typename T>
@@ -1099,6 +1356,58 @@ cudaError_t Kernels<T>::richardson_lean(const StencilLaunch &L, const Weights<T>
 }
 
 template <typename T>
+cudaError_t Kernels<T>::ring_richardson(const StencilLaunch &L, const Weights<T> &w, const T *r, T *r2, S c,
+                                        const DevCtrl *ctrl) {
+    if constexpr (std::is_same<T, float>::value) {
+        RichRingOp<T> op{r, r2, (T)c, nullptr, ctrl};
+        return launch_stencil<T>(L, w, op);
+    } else {
+        (void)L, (void)w, (void)r, (void)r2, (void)c, (void)ctrl;
+        return cudaErrorInvalidValue;
+    }
+}
+
+template <typename T>
+cudaError_t Kernels<T>::ring_residual(const StencilLaunch &L, const Weights<T> &w, const T *step, const T *r,
+                                      T *r2, T *hc, S cf, double hb, double *partials, const DevCtrl *ctrl) {
+    if constexpr (std::is_same<T, float>::value) {
+        ResRingOp<T> op{step, r, r2, hc, (T)cf, T(hb), partials, ctrl};
+        return launch_stencil<T>(L, w, op);
+    } else {
+        (void)L, (void)w, (void)step, (void)r, (void)r2, (void)hc, (void)cf, (void)hb, (void)partials, (void)ctrl;
+        return cudaErrorInvalidValue;
+    }
+}
+
+template <typename T>
+long long Kernels<T>::ring_paired_plan(const Geom &g, int *lz) {
+    if constexpr (std::is_same<T, float>::value) {
+        static int slots = 0;
+        if (slots == 0) {
+            int occ = 0, dev = 0, sms = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &occ, stencil_x2_kernel<T, kPairBY, kPairNY, kPairMINB, RichRingOp<T>>, 32 * kPairBY, 0) !=
+                    cudaSuccess ||
+                occ < 1) {
+                cudaGetLastError();
+                occ = 1;
+            }
+            slots = std::max(1, sms) * occ;
+        }
+        const int z = balanced_lz(g, kPairBY * kPairNY, slots, FillCost<T>::value, 64);
+        if (lz) *lz = z;
+        return (long long)((g.nx + 63) / 64) * ((g.ny + kPairBY * kPairNY - 1) / (kPairBY * kPairNY)) *
+               ((g.nz + z - 1) / z);
+    } else {
+        (void)g;
+        if (lz) *lz = 0;
+        return 0;
+    }
+}
+
+template <typename T>
 cudaError_t Kernels<T>::residual_recur(const StencilLaunch &L, const Weights<T> &w, const T *step,
                                        T *r, T *df, T *hc, S cf, double hb, double *partials,
                                        const DevCtrl *ctrl) {
@@ -1221,7 +1530,7 @@ static cudaError_t gram_dispatch(int m, const T *dx, const T *df, const T *r, lo
             }
         }
     }
-    switch (n % vn == 0 ? m : 0) {
+    switch (n % vn == 0 && aligned16(dx, df, r) ? m : 0) {
 #define LSG_GRAM_CASE(MM) \
     case MM: gram_kernel<T, KIND, MM><<<blocks, kReduceThreads, 0, s>>>(dx, df, r, n, partials, ctrl); break;
         LSG_GRAM_CASE(1) LSG_GRAM_CASE(2) LSG_GRAM_CASE(3) LSG_GRAM_CASE(4)
@@ -1305,7 +1614,7 @@ cudaError_t Kernels<T>::aar_update_lean(int m, T *x, const T *r, const T *rs, co
         aar_update_lean_kernel<T, 0><<<blocks, kReduceThreads, 0, s>>>(m, x, r, rs, h, step, T(beta), (T)cf, n,
                                                                       mask, ctrl);
     } else {
-        const bool vec = n % Vec4<T>::N == 0;
+        const bool vec = n % Vec4<T>::N == 0 && aligned16(x, r, rs, h, step);
         switch (vec ? m : 0) {
 #define LSG_UPD_CASE(MM)                                                                                      \
     case MM:                                                                                                  \
@@ -1321,6 +1630,96 @@ cudaError_t Kernels<T>::aar_update_lean(int m, T *x, const T *r, const T *rs, co
         }
     }
     return cudaGetLastError();
+}
+
+// The ring kernels need m <= 8, n % 4 == 0 and 16-byte aligned ring, x, step and history.
+template <typename T>
+cudaError_t Kernels<T>::ring_gram(int m, const RingWindow &rw, const T *ring, long long ss, const T *df, S cf,
+                                  long long n, double *partials, int blocks, DevCtrl *ctrl, cudaStream_t s) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (m < 1 || m > kRingMaxM || n % 4 != 0 || ss % 4 != 0 || !aligned16(ring, df))
+            return cudaErrorInvalidValue;
+        static const long long wait_cycles = [] {
+            const char *e = getenv("LSG_GRAM_WAIT_CYCLES");
+            const long long v = e ? atoll(e) : 0;
+            return v >= 1000000 && v <= kWaitCycles ? v : kWaitCycles;
+        }();
+        switch (m) {
+#define LSG_GRAM_RING(MM)                                                                                   \
+    case MM: {                                                                                              \
+        const cudaError_t ea = cudaFuncSetAttribute(gram_bulk_kernel<MM, true>,                             \
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,            \
+                                                    (int)gram_bulk_smem<MM>());                             \
+        if (ea != cudaSuccess) return ea;                                                                   \
+        gram_bulk_kernel<MM, true><<<blocks, kReduceThreads, gram_bulk_smem<MM>(), s>>>(                    \
+            df, nullptr, n, partials, ctrl, 0u, wait_cycles, ring, ss, rw, (float)cf);                      \
+        return cudaGetLastError();                                                                          \
+    }
+            LSG_GRAM_RING(1) LSG_GRAM_RING(2) LSG_GRAM_RING(3) LSG_GRAM_RING(4)
+            LSG_GRAM_RING(5) LSG_GRAM_RING(6) LSG_GRAM_RING(7) LSG_GRAM_RING(8)
+#undef LSG_GRAM_RING
+        default: return cudaErrorInvalidValue;
+        }
+    } else {
+        (void)m, (void)rw, (void)ring, (void)ss, (void)df, (void)cf, (void)n, (void)partials, (void)blocks,
+            (void)ctrl, (void)s;
+        return cudaErrorInvalidValue;
+    }
+}
+
+template <typename T>
+cudaError_t Kernels<T>::ring_update(int m, const RingWindow &rw, const T *ring, long long ss, const T *h, T *x,
+                                    T *step, S c, double beta, S cf, long long n, const DevCtrl *ctrl,
+                                    cudaStream_t s) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (m < 1 || m > kRingMaxM || n % 4 != 0 || ss % 4 != 0 || !aligned16(ring, h, x, step))
+            return cudaErrorInvalidValue;
+        const long long nb = (n / 4 + kReduceThreads - 1) / kReduceThreads;  // one float4 per thread
+        if (nb > 0x7fffffffLL) return cudaErrorInvalidValue;
+        const unsigned blocks = (unsigned)nb;
+        switch (m) {
+#define LSG_UPD_RING(MM)                                                                                     \
+    case MM:                                                                                                 \
+        aar_update_ring_kernel<MM><<<blocks, kReduceThreads, 0, s>>>(ring, ss, rw, h, x, step, (float)c,     \
+                                                                     (float)beta, (float)cf, n, ctrl);       \
+        break;
+            LSG_UPD_RING(1) LSG_UPD_RING(2) LSG_UPD_RING(3) LSG_UPD_RING(4)
+            LSG_UPD_RING(5) LSG_UPD_RING(6) LSG_UPD_RING(7) LSG_UPD_RING(8)
+#undef LSG_UPD_RING
+        default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    } else {
+        (void)m, (void)rw, (void)ring, (void)ss, (void)h, (void)x, (void)step, (void)c, (void)beta, (void)cf, (void)n,
+            (void)ctrl, (void)s;
+        return cudaErrorInvalidValue;
+    }
+}
+
+template <typename T>
+cudaError_t Kernels<T>::ring_fold(int m, const RingWindow &rw, const T *ring, long long ss, T *x, S c, long long n,
+                                  cudaStream_t s) {
+    if constexpr (std::is_same<T, float>::value) {
+        const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, (long long)sm_count() * 8);
+        ring_fold_kernel<<<blocks, kReduceThreads, 0, s>>>(m, ring, ss, rw, x, (float)c, n);
+        return cudaGetLastError();
+    } else {
+        (void)m, (void)rw, (void)ring, (void)ss, (void)x, (void)c, (void)n, (void)s;
+        return cudaErrorInvalidValue;
+    }
+}
+
+template <typename T>
+cudaError_t Kernels<T>::ring_store_column(const T *rk1, const T *rk, T *df, T *h, S c, double hb, S cf,
+                                          long long n, cudaStream_t s) {
+    if constexpr (std::is_same<T, float>::value) {
+        const int blocks = (int)std::min<long long>((n + kReduceThreads - 1) / kReduceThreads, (long long)sm_count() * 8);
+        ring_column_kernel<<<blocks, kReduceThreads, 0, s>>>(rk1, rk, df, h, (float)c, (float)hb, (float)cf, n);
+        return cudaGetLastError();
+    } else {
+        (void)rk1, (void)rk, (void)df, (void)h, (void)c, (void)hb, (void)cf, (void)n, (void)s;
+        return cudaErrorInvalidValue;
+    }
 }
 
 template <typename T>
@@ -1343,7 +1742,8 @@ cudaError_t Kernels<T>::aar_update(int m, T *x, const T *r, const T *h, T *step,
     if constexpr (IsCplx<T>::value) {
         aar_update_kernel<T, 0><<<blocks, kReduceThreads, 0, s>>>(m, x, r, h, step, T(beta), (T)cf, n, ctrl);
     } else {
-        const bool vec = n % Vec4<T>::N == 0;
+        // 16-byte loads need every vector 16-byte aligned (x may be a view at an element offset)
+        const bool vec = n % Vec4<T>::N == 0 && aligned16(x, r, h, step);
         switch (vec ? m : 0) {
 #define LSG_UPD_CASE(MM) \
     case MM: aar_update_kernel<T, MM><<<blocks, kReduceThreads, 0, s>>>(m, x, r, h, step, (T)beta, (T)cf, n, ctrl); break;

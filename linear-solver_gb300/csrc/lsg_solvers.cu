@@ -68,6 +68,16 @@ static std::atomic<int> g_fp64_arith{[] {
     return (e && e[0] == '1') ? 1 : 0;
 }()};
 int fp64_exact() { return g_fp64_arith.load(std::memory_order_relaxed); }
+
+// Form of the FP32 AAR's Richardson passes: 0 = the residual ring where it
+// applies, 1 = the lean form (three residual buffers, H and DF stored),
+// 2 = the x-carrying recurrence.  LSG_AAR_FORM sets the initial value.
+static std::atomic<int> g_aar_form{[] {
+    const char *e = getenv("LSG_AAR_FORM");
+    const int v = e ? atoi(e) : 0;
+    return v >= 0 && v <= 2 ? v : 0;
+}()};
+int aar_form() { return g_aar_form.load(std::memory_order_relaxed); }
 int fp64_exact_for(double tol) { return (fp64_exact() || tol < kDfMinTol) ? 1 : 0; }
 
 // ---------------------------------------------------------------- device info
@@ -100,6 +110,7 @@ static int stencil_slots(int sms) {
 //   xalt, r0, r1, rs             four vectors (ping-pong partners; rs: the
 //                                cycle-start residual of the lean FP32 AAR)
 //   dx[m], df[m]                 the history, column j at offset j*n
+//   ring[m + 1]                  FP32 keys with m <= 8: the residual ring of the AAR
 //   partials                     per-block FP64 sums
 //   ctrl                         DevCtrl
 // The mixed solver adds r32 / e32 (float) on an FP64 key.
@@ -111,6 +122,8 @@ struct Workspace {
     int m = 0;
     char *base = nullptr;
     void *xalt = nullptr, *r0 = nullptr, *r1 = nullptr, *rs = nullptr, *dx = nullptr, *df = nullptr;
+    void *ring = nullptr;     // FP32 keys: the residual ring, m + 1 slots ring_ss elements apart
+    long long ring_ss = 0;
     float *r32 = nullptr, *e32 = nullptr;
     double *partials = nullptr;
     long long partials_cap = 0;
@@ -175,6 +188,9 @@ static int get_workspace(size_t es, long long n, int m, bool mixed, const Geom &
     const size_t o_rs = bytes; bytes += vec;
     const size_t o_dx = bytes; bytes += align_up((size_t)n * es * (size_t)m);
     const size_t o_df = bytes; bytes += align_up((size_t)n * es * (size_t)m);
+    size_t o_ring = 0;
+    const bool with_ring = es == 4 && !mixed && m >= 1 && m <= kRingMaxM;
+    if (with_ring) { o_ring = bytes; bytes += vec * (size_t)(m + 1); }
     size_t o_r32 = 0, o_e32 = 0;
     if (mixed) {  // FP32 (or complex64) correction, half the outer element size
         o_r32 = bytes; bytes += align_up((size_t)n * (es / 2));
@@ -206,6 +222,10 @@ static int get_workspace(size_t es, long long n, int m, bool mixed, const Geom &
     ws->rs = base + o_rs;
     ws->dx = base + o_dx;
     ws->df = base + o_df;
+    if (with_ring) {
+        ws->ring = base + o_ring;
+        ws->ring_ss = (long long)(vec / es);
+    }
     if (mixed) {
         ws->r32 = (float *)(base + o_r32);
         ws->e32 = (float *)(base + o_e32);
@@ -494,6 +514,12 @@ struct AarLoop {
     double *part;
     bool lean = false;
     int xc = 0, rc = 0, rsc = 0;  // rsc: buffer of the cycle-start residual (lean)
+    // residual ring (RingWindow): r_k in slot k mod (m + 1) of RG
+    bool ring = false;
+    T *RG = nullptr;
+    long long rss = 0;
+    std::vector<int> replaced;  // iterations whose residual a mixed solve overwrote
+    int fold_it = 0;            // x holds the Richardson steps up to this iteration
 
     AarLoop(Run &R_, const lsg_operator *op, const lsg_params *prm_, T *x, const T *b_, Workspace *ws_)
         : R(R_), prm(prm_), ws(ws_), b(b_) {
@@ -501,7 +527,11 @@ struct AarLoop {
         n = g.n;
         m = prm->m;
         p = prm->p;
-        lean = recur && m <= 32 && p - 1 <= m;
+        const int form = aar_form();
+        lean = recur && m <= 32 && p - 1 <= m && form != 2;
+        if constexpr (std::is_same<T, float>::value)
+            ring = lean && form == 0 && ws->ring && m <= kRingMaxM && n % 4 == 0 && ws->ring_ss % 4 == 0 &&
+                   (((uintptr_t)x | (uintptr_t)ws->xalt | (uintptr_t)ws->dx | (uintptr_t)ws->df) & 15u) == 0;
         w = make_weights<T>(op);
         cf = jacobi_factor<T>(op);
         const int lz = choose_lz<T>(g, stencil_slots<T>(R.sms));
@@ -523,6 +553,7 @@ struct AarLoop {
             if (Lr.paired == -1) {  // untuned: the paired march
                 Lr.paired = 1;
                 Lr.lz = plz;
+                if (ring) Kernels<T>::ring_paired_plan(g, &Lr.lz);
             }
             Lres.paired = 1;
             Lres.lz = plz;
@@ -542,8 +573,62 @@ struct AarLoop {
         DF = (T *)ws->df;
         ctrl = ws->ctrl;
         part = ws->partials;
+        if (ring) {
+            RG = (T *)ws->ring;
+            rss = ws->ring_ss;
+        }
     }
     bool is_anderson(int it) const { return it % p == 0 && it > 1; }
+    T *slot_ptr(int k) const { return RG + (size_t)(k % (m + 1)) * (size_t)rss; }
+    bool was_replaced(int k) const { return std::find(replaced.begin(), replaced.end(), k) != replaced.end(); }
+    // The ring's view at extrapolation iteration `it` (or, for a fold after
+    // iteration it - 1, of the columns up to it - 1).
+    RingWindow window(int it) const {
+        RingWindow rw{};
+        const int M1 = m + 1;
+        for (int t = 0; t <= m; t++) {
+            const int k = it - m - 1 + t;
+            rw.slot[t] = ((k % M1) + M1) % M1;
+        }
+        rw.s0 = (it - 1) % m;
+        int la = 0;  // the last extrapolation before it
+        for (int k = it - 1; k >= 1; k--)
+            if (is_anderson(k)) { la = k; break; }
+        for (int t = 0; t < m; t++) {
+            const int k = it - m + t;
+            if (k < 1) continue;
+            const bool ext = is_anderson(k), rep = was_replaced(k);
+            rw.valid |= 1u << t;
+            if (ext || rep) rw.hmem |= 1u << t;
+            if (rep) rw.dfmem |= 1u << t;
+            if (!ext && k > la && k > fold_it) rw.cyc |= 1u << t;
+        }
+        rw.e0 = rw.e1 = -1;
+        for (int t = 0; t < m; t++)
+            if ((rw.hmem >> t) & 1u) {
+                if (rw.e0 < 0) rw.e0 = t;
+                else if (rw.e1 < 0) rw.e1 = t;
+            }
+        return rw;
+    }
+    // The residual the iteration continues from after iterations 1..last (a
+    // mixed solve replaces it with the FP64 residual).
+    T *residual_after(int last) {
+        if (ring) return slot_ptr(last);
+        sync_parity(last);
+        return Rv[rc];
+    }
+    // Before that residual is overwritten, the ring keeps its column: DF (and,
+    // for a Richardson column, H) go to the history arrays.
+    int prepare_replace(int last) {
+        if (!ring || last < 1 || was_replaced(last)) return LSG_OK;
+        const size_t col = (size_t)((last - 1) % m) * (size_t)n;
+        LSG_KC(LSG_K_REFINE, Kernels<T>::ring_store_column(slot_ptr(last - 1), slot_ptr(last), DF + col,
+                                                           is_anderson(last) ? nullptr : DX + col,
+                                                           prm->omega * cf, prm->beta, cf, n, R.s));
+        replaced.push_back(last);
+        return LSG_OK;
+    }
     // r buffers holding the residual (and, lean, the cycle-start residual)
     // after iteration `last`
     void sync_parity(int last) {
@@ -561,6 +646,12 @@ struct AarLoop {
     // added that cycle's steps to x yet: fold them in.
     int finish(int last) {
         if (!lean || last < 1 || is_anderson(last)) return LSG_OK;
+        if (ring) {
+            if (last <= fold_it) return LSG_OK;
+            LSG_KC(LSG_K_UPDATE, Kernels<T>::ring_fold(m, window(last + 1), RG, rss, X[0], prm->omega * cf, n, R.s));
+            fold_it = last;
+            return LSG_OK;
+        }
         sync_parity(last);
         LSG_KC(LSG_K_UPDATE, Kernels<T>::recur_fold(m, X[0], Rv[rc], Rv[rsc], DX, prm->beta, cf, n,
                                                     cycle_mask(last), R.s));
@@ -574,6 +665,25 @@ struct AarLoop {
     int enqueue(int it) {
         const int col = (it - 1) % m;  // the reference writes this column at iteration it+1
         T *dxc = DX + (size_t)col * n, *dfc = DF + (size_t)col * n;
+        if constexpr (std::is_same<T, float>::value) {
+          if (ring) {
+            if (is_anderson(it)) {
+                const RingWindow rw = window(it);
+                LSG_KC(LSG_K_GRAM, Kernels<T>::ring_gram(m, rw, RG, rss, DF, cf, n, part, gb, ctrl, R.s));
+                LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, gb, GRAM_SYM, m, cf, ctrl, R.s));
+                T *step = (T *)ws->xalt;  // the residual pass reads it as its stencil input
+                LSG_KC(LSG_K_UPDATE, Kernels<T>::ring_update(m, rw, RG, rss, DX, X[0], step, prm->omega * cf,
+                                                             prm->beta, cf, n, ctrl, R.s));
+                LSG_KC(LSG_K_RESIDUAL, Kernels<T>::ring_residual(Lres, w, step, slot_ptr(it - 1), slot_ptr(it), dxc,
+                                                                 cf, prm->beta, part, ctrl));
+                LSG_KC(LSG_K_SMALL, finalize_norm(part, sbr, ctrl, NF_CHECK, prm->tol, it, R.s, W));
+            } else {
+                LSG_KC(LSG_K_RICHARDSON, Kernels<T>::ring_richardson(Lr, w, slot_ptr(it - 1), slot_ptr(it),
+                                                                     prm->omega * cf, ctrl));
+            }
+            return LSG_OK;
+          }
+        }
         if (is_anderson(it)) {
             LSG_KC(LSG_K_GRAM, Kernels<T>::gram(GRAM_SYM, m, DX, DF, Rv[rc], n, part, gb, ctrl, R.s));
             if constexpr (IsCplx<T>::value)
@@ -633,8 +743,8 @@ int aar_core(Run &R, const lsg_operator *op, const lsg_params *prm, T *x, const 
     // ||b|| and tol *= ||b|| (AAR.c:78-79); f = b - A x (AAR.c:80-82).
     LSG_KC(LSG_K_UPDATE, Kernels<T>::norm2(b, A.n, A.part, A.rb, A.ctrl, R.s));
     LSG_KC(LSG_K_SMALL, finalize_norm(A.part, A.rb, A.ctrl, NF_RHS, prm->tol, 0, R.s, AarLoop<T>::W));
-    LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(A.L, A.w, RES_INIT, x, b, A.Rv[0], nullptr, nullptr, A.cf, 0.0,
-                                                A.part, A.ctrl));
+    LSG_KC(LSG_K_RESIDUAL, Kernels<T>::residual(A.L, A.w, RES_INIT, x, b, A.residual_after(0), nullptr, nullptr,
+                                                A.cf, 0.0, A.part, A.ctrl));
     rc = A.run(1);
     if (rc != LSG_OK) return rc;
     DevCtrl c;
@@ -892,16 +1002,17 @@ int solve_mixed_t(const lsg_operator *op, const lsg_params *prm, T64 *x, const T
     DevCtrl co, ci;
     for (;;) {
         // r = b - A x64 in FP64, stored as the FP32 residual the iteration continues from
-        A.sync_parity(it - 1);
+        rc = A.prepare_replace(it - 1);
+        if (rc != LSG_OK) return rc;
+        T32 *r32 = A.residual_after(it - 1);
         if (deflate) {
             LSG_KC(LSG_K_REFINE, deflate_x<T64>(x, n, opart, octrl, sig_re, sig_im, s));
             R.launches += 2;  // sum + finalize + shift
         }
         const int first = it == 1 ? 1 : 0;
-        LSG_KC(LSG_K_REFINE, (ir_residual<T64, T32>(L64, w64, x, b, A.Rv[A.rc], opart, octrl, first)));
+        LSG_KC(LSG_K_REFINE, (ir_residual<T64, T32>(L64, w64, x, b, r32, opart, octrl, first)));
         if (first)
-            LSG_KC(LSG_K_REFINE, (ir_residual_const<T64, T32>(b, A.Rv[A.rc], n, opart, sb64, octrl, sig_re, sig_im,
-                                                             s)));
+            LSG_KC(LSG_K_REFINE, (ir_residual_const<T64, T32>(b, r32, n, opart, sb64, octrl, sig_re, sig_im, s)));
         LSG_KC(LSG_K_SMALL, finalize_norm(opart, sb64, octrl, NF_CHECK, prm->tol, it - 1, s, W));
         LSG_CUDA(cudaMemcpyAsync(&wo->hctrl[0], octrl, sizeof(DevCtrl), cudaMemcpyDeviceToHost, s));
         LSG_CUDA(cudaStreamSynchronize(s));
@@ -1423,5 +1534,10 @@ const char *lsg_status_string(int st) {
 const char *lsg_version(void) { return "lsg 0.1 (sm_103a)"; }
 
 int lsg_set_fp64_arith(int mode) { return lsg::g_fp64_arith.exchange(mode ? 1 : 0); }
+
+int lsg_set_aar_form(int form) {
+    if (form < 0 || form > 2) return -1;
+    return lsg::g_aar_form.exchange(form);
+}
 
 }  // extern "C"

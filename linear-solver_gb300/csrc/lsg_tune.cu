@@ -83,8 +83,8 @@ __global__ void tune_fill_kernel(T *v, long long n) {
 }
 
 // Times `reps` launches of the Richardson pass in shape (tile, lz); ms per launch.
-// FP32 vectors time the lean recurrence pass (x left out), the form AAR uses
-// by default (p - 1 <= m).
+// FP32 vectors time the pass of the AAR form in use: the residual ring's
+// (r' only) by default, else the lean recurrence pass (x left out).
 template <typename T>
 static int time_rich(const StencilLaunch &L, const Weights<T> &w, T *v, long long n, const DevCtrl *ctrl,
                      cudaEvent_t e0, cudaEvent_t e1, float *ms) {
@@ -94,6 +94,8 @@ static int time_rich(const StencilLaunch &L, const Weights<T> &w, T *v, long lon
     T *x = v, *r = v + n, *r2 = v + 2 * n, *dx = v + 3 * n, *df = v + 4 * n, *x2 = v + 5 * n;
     const T *b = v + 6 * n;
     auto launch = [&]() -> cudaError_t {
+        if constexpr (std::is_same<T, float>::value)
+            if (aar_form() == 0) return Kernels<T>::ring_richardson(L, w, r, r2, c, ctrl);
         if (recur) return Kernels<T>::richardson_lean(L, w, r, r2, dx, df, c, cf, 0.5, ctrl);
         return Kernels<T>::richardson(L, w, RICH_AAR, x, r, b, x2, r2, dx, df, c, cf, 0.5, ctrl);
     };

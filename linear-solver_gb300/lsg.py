@@ -100,7 +100,7 @@ EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "ls
            "lsg_pinv_solve_noalloc", "lsg_aar_batched", "lsg_aar_mixed_batched", "lsg_autotune",
            "lsg_set_autotune", "lsg_autotune_save", "lsg_autotune_load", "lsg_gmres",
            "lsg_aar_csr", "lsg_apply_csr", "lsg_register_operator_csr", "lsg_bounds_errors",
-           "lsg_set_fp64_arith", "lsg_aar_icc", "lsg_icc_factor", "lsg_cocg"]
+           "lsg_set_fp64_arith", "lsg_aar_icc", "lsg_icc_factor", "lsg_cocg", "lsg_set_aar_form"]
 
 KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "precond"]
 
@@ -141,6 +141,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
         L.lsg_autotune.argtypes = [C.POINTER(_Operator), ip, C.POINTER(_TuneInfo), vp]
         L.lsg_set_autotune.argtypes = [ip]
         L.lsg_set_fp64_arith.argtypes = [ip]
+        L.lsg_set_aar_form.argtypes = [ip]
         L.lsg_aar_icc.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), C.POINTER(ip), vp, vp,
                                   C.POINTER(_Result), vp]
         L.lsg_icc_factor.argtypes = [C.POINTER(_Operator), C.POINTER(ip), C.POINTER(dp), C.POINTER(dp),
@@ -442,6 +443,16 @@ def set_fp64_arith(mode: int) -> int:
     sums on the FP32 pipe (default; tol < 1e-10 takes FP64 anyway), 1 = FP64
     arithmetic.  Returns the previous mode."""
     return int(lib().lsg_set_fp64_arith(int(mode)))
+
+
+def set_aar_form(form: int) -> int:
+    """Form of the FP32 AAR's Richardson passes: 0 = residual ring (default
+    where it applies), 1 = lean (r', H, DF stored), 2 = x-carrying recurrence.
+    All give the same residuals and steps bit for bit.  Returns the previous form."""
+    prev = int(lib().lsg_set_aar_form(int(form)))
+    if prev < 0:
+        raise ValueError(f"AAR form {form} outside 0..2")
+    return prev
 
 
 def autotune_save(path: str):
