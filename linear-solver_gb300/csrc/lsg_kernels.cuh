@@ -426,7 +426,7 @@ struct RichRingOp {
         r2[i] = fma(-c, ar, rc);
     }
     static constexpr bool PAIRED = true;
-    static constexpr bool PACKED = false;  // packed sums spill here
+    static constexpr bool PACKED = false;  // packed sums spill here and ran 5% slower
     __host__ __device__ const void *pair_ptrs_or() const { return (const void *)((uintptr_t)r | (uintptr_t)r2); }
     __device__ __forceinline__ Two<T> fetch_pair(unsigned i) const { return ld_pair(r + i); }
     __device__ __forceinline__ Two<T> center_pair(unsigned) const { return Two<T>{T(0), T(0)}; }

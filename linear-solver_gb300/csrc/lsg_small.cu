@@ -374,6 +374,55 @@ __device__ int warp_pinv_any(double *G, double *V, const double *b, double *x, i
     return warp_pinv(G, V, b, x, m, cut);
 }
 
+// Sums nv values over nparts block partials (row k: values of block k): value
+// v = warp + q * nwarps is one warp's, lanes striding over the rows, each lane
+// adding its rows in increasing order, then a warp sum.  A warp keeps its
+// (up to kSumVals) values' loads in flight together, two rows at a time,
+// since the partials are L2-resident and the loop is latency-bound.
+constexpr int kSumVals = 6;
+__device__ __forceinline__ void block_sum_partials(const double *__restrict__ partials, int nparts, int nv,
+                                                   double *vals, int *bad) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int v0 = warp; v0 < nv; v0 += nw * kSumVals) {
+        double t[kSumVals];
+#pragma unroll
+        for (int q = 0; q < kSumVals; q++) t[q] = 0.0;
+        int k = lane;
+        for (; k + 32 < nparts; k += 64) {
+            const double *ra = partials + (long long)k * nv, *rb = ra + 32LL * nv;
+            double a[kSumVals], b[kSumVals];
+#pragma unroll
+            for (int q = 0; q < kSumVals; q++) {
+                const int v = v0 + q * nw;
+                a[q] = v < nv ? __ldcg(ra + v) : 0.0;
+                b[q] = v < nv ? __ldcg(rb + v) : 0.0;
+            }
+#pragma unroll
+            for (int q = 0; q < kSumVals; q++) {
+                t[q] += a[q];
+                t[q] += b[q];
+            }
+        }
+        if (k < nparts) {
+            const double *ra = partials + (long long)k * nv;
+#pragma unroll
+            for (int q = 0; q < kSumVals; q++) {
+                const int v = v0 + q * nw;
+                if (v < nv) t[q] += __ldcg(ra + v);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kSumVals; q++) {
+            const int v = v0 + q * nw;
+            const double tv = warp_sum(t[q]);
+            if (lane == 0 && v < nv) {
+                vals[v] = tv;
+                if (!isfinite(tv)) *bad = 1;
+            }
+        }
+    }
+}
+
 __device__ void gram_solve_body(const double *partials, int nparts, int kind, int m, double hscale,
                                 DevCtrl *ctrl) {
     __shared__ double vals[LSG_MAX_M * LSG_MAX_M + LSG_MAX_M];
@@ -385,19 +434,7 @@ __device__ void gram_solve_body(const double *partials, int nparts, int kind, in
     const int np = nv - m;
     if (threadIdx.x == 0) bad = 0;
     __syncthreads();
-    {
-        // One warp per Gram value, lanes striding over the block partials.
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        for (int v = warp; v < nv; v += nw) {
-            double t = 0.0;
-            for (int k = lane; k < nparts; k += 32) t += partials[(long long)k * nv + v];
-            t = warp_sum(t);
-            if (lane == 0) {
-                vals[v] = t;
-                if (!isfinite(t)) bad = 1;
-            }
-        }
-    }
+    block_sum_partials(partials, nparts, nv, vals, &bad);
     __syncthreads();
     if (threadIdx.x < 32) {
         // Assemble G (row-major) and h.
@@ -456,18 +493,7 @@ __device__ void gram_solve_c_body(const double *partials, int nparts, int m, dou
     const int m2 = 2 * m;
     if (threadIdx.x == 0) bad = 0;
     __syncthreads();
-    {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        for (int v = warp; v < nvr; v += nw) {
-            double t = 0.0;
-            for (int k = lane; k < nparts; k += 32) t += partials[(long long)k * nvr + v];
-            t = warp_sum(t);
-            if (lane == 0) {
-                vals[v] = t;
-                if (!isfinite(t)) bad = 1;
-            }
-        }
-    }
+    block_sum_partials(partials, nparts, nvr, vals, &bad);
     __syncthreads();
     if (threadIdx.x < 32) {
         for (int k = threadIdx.x; k < np; k += 32) {
