@@ -54,7 +54,7 @@ CPU_SAMPLE_ITERS = 24
 # DRAM bytes (read + write) of one launch of the dominant kernel at this
 # workload, from an ncu capture of that kernel on this workload (a constant:
 # the timed run is not captured); keyed by "residual ring in use".
-RICH32_TRAFFIC_BYTES = {False: 224.2e6, True: None}
+RICH32_TRAFFIC_BYTES = {False: 224.2e6, True: 101.0e6}
 
 
 def aar_form_in_use(lsg):

@@ -127,6 +127,16 @@ int lsg_set_fp64_arith(int mode);
  * previous form, or -1 for a form outside 0..2. */
 int lsg_set_aar_form(int form);
 
+/* Batched inner products kept on the device: d_out[k] = sum_i conj(x_k[i]) y_k[i]
+ * (real dtypes: sum x y; complex: Re, Im at d_out[2k], d_out[2k+1]) for count
+ * vectors of n values stored back to back in d_x and d_y, accumulated in FP64
+ * (double-float for F32 / C64) in a fixed order, enqueued on `stream` without
+ * a host synchronisation.  d_scratch: device doubles, count * lsg_dot_blocks(n)
+ * * (2 for complex dtypes, else 1). */
+int lsg_dot_blocks(long long n);
+int lsg_dot(int dtype, int count, long long n, const void *d_x, const void *d_y, double *d_out,
+            double *d_scratch, void *stream);
+
 /* y = A x on the device (replaces MPI_REAL/system.c:80-213). */
 int lsg_apply(const lsg_operator *op, int dtype, const void *d_x, void *d_y, void *stream);
 

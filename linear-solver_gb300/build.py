@@ -34,7 +34,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "-diag-suppress", "177", f"-I{os.path.join(ROOT, 'include')}"] + (["-DLSG_BOUNDS"] if BOUNDS else [])
 SOURCES = ["lsg_kernels_f64.cu", "lsg_kernels_f32.cu", "lsg_kernels_c128.cu", "lsg_kernels_c64.cu",
            "lsg_batch_f64.cu", "lsg_batch_f32.cu", "lsg_batch_c128.cu", "lsg_batch_c64.cu",
-           "lsg_small.cu", "lsg_solvers.cu", "lsg_batch.cu", "lsg_tune.cu", "lsg_krylov.cu", "lsg_csr.cu", "lsg_icc.cu", "lsg_compat.cpp"]
+           "lsg_small.cu", "lsg_solvers.cu", "lsg_batch.cu", "lsg_tune.cu", "lsg_krylov.cu", "lsg_csr.cu", "lsg_icc.cu", "lsg_dot.cu", "lsg_compat.cpp"]
 
 
 def _nvcc() -> str:

@@ -380,8 +380,8 @@ __device__ int warp_pinv_any(double *G, double *V, const double *b, double *x, i
 // (up to kSumVals) values' loads in flight together, two rows at a time,
 // since the partials are L2-resident and the loop is latency-bound.
 constexpr int kSumVals = 6;
-__device__ __forceinline__ void block_sum_partials(const double *__restrict__ partials, int nparts, int nv,
-                                                   double *vals, int *bad) {
+__device__ __forceinline__ void sum_gram_partials(const double *__restrict__ partials, int nparts, int nv,
+                                                  double *vals, int *bad) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int v0 = warp; v0 < nv; v0 += nw * kSumVals) {
         double t[kSumVals];
@@ -434,7 +434,7 @@ __device__ void gram_solve_body(const double *partials, int nparts, int kind, in
     const int np = nv - m;
     if (threadIdx.x == 0) bad = 0;
     __syncthreads();
-    block_sum_partials(partials, nparts, nv, vals, &bad);
+    sum_gram_partials(partials, nparts, nv, vals, &bad);
     __syncthreads();
     if (threadIdx.x < 32) {
         // Assemble G (row-major) and h.
@@ -493,7 +493,7 @@ __device__ void gram_solve_c_body(const double *partials, int nparts, int m, dou
     const int m2 = 2 * m;
     if (threadIdx.x == 0) bad = 0;
     __syncthreads();
-    block_sum_partials(partials, nparts, nvr, vals, &bad);
+    sum_gram_partials(partials, nparts, nvr, vals, &bad);
     __syncthreads();
     if (threadIdx.x < 32) {
         for (int k = threadIdx.x; k < np; k += 32) {

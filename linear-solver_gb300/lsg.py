@@ -100,7 +100,7 @@ EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "ls
            "lsg_pinv_solve_noalloc", "lsg_aar_batched", "lsg_aar_mixed_batched", "lsg_autotune",
            "lsg_set_autotune", "lsg_autotune_save", "lsg_autotune_load", "lsg_gmres",
            "lsg_aar_csr", "lsg_apply_csr", "lsg_register_operator_csr", "lsg_bounds_errors",
-           "lsg_set_fp64_arith", "lsg_aar_icc", "lsg_icc_factor", "lsg_cocg", "lsg_set_aar_form"]
+           "lsg_set_fp64_arith", "lsg_aar_icc", "lsg_icc_factor", "lsg_cocg", "lsg_set_aar_form", "lsg_dot", "lsg_dot_blocks"]
 
 KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "precond"]
 
@@ -142,6 +142,8 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
         L.lsg_set_autotune.argtypes = [ip]
         L.lsg_set_fp64_arith.argtypes = [ip]
         L.lsg_set_aar_form.argtypes = [ip]
+        L.lsg_dot_blocks.argtypes = [C.c_longlong]
+        L.lsg_dot.argtypes = [ip, ip, C.c_longlong, vp, vp, vp, vp, vp]
         L.lsg_aar_icc.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), C.POINTER(ip), vp, vp,
                                   C.POINTER(_Result), vp]
         L.lsg_icc_factor.argtypes = [C.POINTER(_Operator), C.POINTER(ip), C.POINTER(dp), C.POINTER(dp),
@@ -445,6 +447,28 @@ def set_fp64_arith(mode: int) -> int:
     return int(lib().lsg_set_fp64_arith(int(mode)))
 
 
+def dot(x, y, batched: bool = False, stream=None):
+    """conj(x) . y on the device (FP64 accumulation, fixed order, no host sync).
+
+    batched: x and y are (B, ...) and the result has one value per leading
+    index.  Returns a float64 (real inputs) or complex128 tensor on x's device."""
+    import torch
+    if x.dtype != y.dtype or x.shape != y.shape or not (x.is_cuda and y.is_cuda):
+        raise TypeError("dot: x and y must be CUDA tensors of one dtype and shape")
+    x, y = x.contiguous(), y.contiguous()
+    count = x.shape[0] if batched else 1
+    n = x.numel() // count
+    w = 2 if x.is_complex() else 1
+    nblk = int(lib().lsg_dot_blocks(n))
+    scratch = torch.empty(count * nblk * w, dtype=torch.float64, device=x.device)
+    out = torch.empty(count * w, dtype=torch.float64, device=x.device)
+    _check(lib().lsg_dot(_dtype_code(x), count, n, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
+                         C.c_void_p(out.data_ptr()), C.c_void_p(scratch.data_ptr()), _stream_ptr(stream)), "lsg_dot")
+    if w == 2:
+        out = torch.view_as_complex(out.view(count, 2))
+    return out if batched else out.reshape(())
+
+
 def set_aar_form(form: int) -> int:
     """Form of the FP32 AAR's Richardson passes: 0 = residual ring (default
     where it applies), 1 = lean (r', H, DF stored), 2 = x-carrying recurrence.
@@ -697,6 +721,9 @@ class _ShiftedSolve:
             def forward(ctx, b, sigma, grid, radius, a, precision, kw):
                 batched = b.dim() == 4
                 if torch.is_tensor(sigma):
+                    # the shifts are operator coefficients on the host: a CUDA
+                    # sigma costs one device-to-host copy here (pass a CPU
+                    # tensor or numbers to avoid the synchronisation)
                     raw = sigma.detach().cpu().reshape(-1).tolist()
                 elif isinstance(sigma, (list, tuple)):
                     raw = list(sigma)
@@ -736,9 +763,8 @@ class _ShiftedSolve:
                 lam = lam.to(x.dtype)
                 gsig = None
                 if ctx.sigma_is_tensor and ctx.needs_input_grad[1]:
-                    hp = torch.complex128 if x.is_complex() else torch.float64
-                    prod = -(x.to(hp).conj() * lam.to(hp))
-                    g = prod.reshape(prod.shape[0], -1).sum(1) if ctx.batched else prod.sum()
+                    # dL/dsigma = -x^H lambda, one device reduction per instance
+                    g = -dot(x, lam, batched=ctx.batched)
                     if not ctx.sigma_dtype.is_complex:
                         g = g.real
                     nsig = 1
