@@ -127,6 +127,12 @@ int lsg_set_fp64_arith(int mode);
  * previous form, or -1 for a form outside 0..2. */
 int lsg_set_aar_form(int form);
 
+/* Stencil march of the FP32 batched Richardson passes: 1 (default) the paired
+ * march (two columns per lane, 64-wide tiles) when every grid has an even nx
+ * and every x is 8-byte aligned, 0 the one-column march.  Both give the same
+ * results bit for bit.  Returns the previous setting. */
+int lsg_set_batch_march(int paired);
+
 /* Batched inner products kept on the device: d_out[k] = sum_i conj(x_k[i]) y_k[i]
  * (real dtypes: sum x y; complex: Re, Im at d_out[2k], d_out[2k+1]) for count
  * vectors of n values stored back to back in d_x and d_y, accumulated in FP64

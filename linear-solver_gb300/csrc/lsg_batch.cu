@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -38,7 +39,8 @@ namespace lsg {
     do {                                                                                     \
         cudaError_t e_ = (call);                                                             \
         if (e_ != cudaSuccess)                                                               \
-            return set_error(e_ == cudaErrorMemoryAllocation ? LSG_NO_MEMORY : LSG_CUDA_ERROR, \
+            return cudaGetLastError(), /* clear it for later launches */                     \
+                   set_error(e_ == cudaErrorMemoryAllocation ? LSG_NO_MEMORY : LSG_CUDA_ERROR, \
                              "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
 
@@ -49,6 +51,7 @@ struct BPlan {
     std::vector<int> act;     // active instances
     int var = 0;              // tile variant of the stencil passes
     int sgrid = 0, ugrid = 0;
+    int pgrid = 0;            // paired-march Richardson blocks (0: the one-column march)
     long long points = 0;     // grid points of the active instances
 };
 
@@ -63,11 +66,13 @@ struct BatchWs {
     void *d_inst = nullptr, *h_inst = nullptr;
     int *d_smap = nullptr, *h_smap = nullptr;
     int *d_umap = nullptr, *h_umap = nullptr;
+    int *d_pmap = nullptr, *h_pmap = nullptr;  // FP32: paired-march Richardson blocks
     int *d_amap = nullptr, *h_amap = nullptr;
     BClock *d_clk = nullptr, *h_clk = nullptr;  // BClock + count done flags; host: 2 slots
     DevCtrl *d_ctrl = nullptr, *h_ctrl = nullptr;  // 2 per instance: ctrl, octrl
     size_t clk_bytes = 0;
-    long long smap_cap = 0, umap_cap = 0;
+    long long smap_cap = 0, umap_cap = 0, pmap_cap = 0;
+    int paired = 0;               // this solve's Richardson passes run the paired march
     std::vector<char *> vec;      // per instance: xalt r0 r1 dx[m] df[m] (e) (FP32: rs)
     std::vector<double *> part;
     std::vector<long long> part_cap;
@@ -113,7 +118,24 @@ static long long max_sblocks(const Geom &g, int ty) {
     return (long long)tx * tyn * ((g.nz + lzmin - 1) / lzmin);
 }
 
-static const int kUcapPerSm = 8;  // point-local blocks (256 threads) per SM over the batch
+// Paired-march tiles of one instance (64 columns x kPairBY * kPairNY rows)
+// and their upper bound over all plans.
+static void ptiles_of(const Geom &g, int *tx, int *tyn) {
+    *tx = (g.nx + 63) / 64;
+    *tyn = (g.ny + kPairBY * kPairNY - 1) / (kPairBY * kPairNY);
+}
+static long long max_pblocks(const Geom &g) {
+    int tx, tyn;
+    ptiles_of(g, &tx, &tyn);
+    const int lzmin = std::min(8, g.nz);
+    return (long long)tx * tyn * ((g.nz + lzmin - 1) / lzmin);
+}
+
+static const int kUcapPerSm = 8;
+
+// lsg_set_batch_march: 1 (default) lets FP32 batches run the paired march.
+static std::atomic<int> g_batch_paired{1};
+static bool batch_paired_enabled() { return g_batch_paired.load(std::memory_order_relaxed) != 0; }  // point-local blocks (256 threads) per SM over the batch
 
 template <typename T>
 static int batch_ws_get(const std::vector<Geom> &geo, int m, bool mixed, bool generic, BatchWs **out,
@@ -145,8 +167,9 @@ static int batch_ws_get(const std::vector<Geom> &geo, int m, bool mixed, bool ge
     size_t bytes = 0;
     std::vector<size_t> o_vec(count), o_part(count);
     ws->part_cap.resize(count);
-    long long smap_cap = 0;
+    long long smap_cap = 0, pmap_cap = 0;
     for (int i = 0; i < count; i++) {
+        if (std::is_same<T, float>::value) pmap_cap += max_pblocks(geo[i]);
         o_vec[i] = bytes;
         bytes += (size_t)nvec * al256((size_t)geo[i].n * es);
         const long long sb = max_sblocks(geo[i], ty);
@@ -159,6 +182,7 @@ static int batch_ws_get(const std::vector<Geom> &geo, int m, bool mixed, bool ge
         bytes += al256((size_t)ws->part_cap[i] * 8);
     }
     ws->smap_cap = smap_cap;
+    ws->pmap_cap = pmap_cap;
     ws->umap_cap = ucap + count;
     ws->inst_bytes = sizeof(BInst<T>) * count;
     ws->clk_bytes = al256(sizeof(BClock) + sizeof(int) * count);
@@ -167,6 +191,7 @@ static int batch_ws_get(const std::vector<Geom> &geo, int m, bool mixed, bool ge
     const size_t o_inst = bytes; bytes += al256(ws->inst_bytes);
     const size_t o_smap = bytes; bytes += al256(sizeof(int) * smap_cap);
     const size_t o_umap = bytes; bytes += al256(sizeof(int) * ws->umap_cap);
+    const size_t o_pmap = bytes; bytes += al256(sizeof(int) * pmap_cap);
     const size_t o_amap = bytes; bytes += al256(sizeof(int) * count);
     const size_t o_clk = bytes; bytes += ws->clk_bytes;
     cudaError_t e = cudaMalloc(&ws->base, bytes);
@@ -183,6 +208,7 @@ static int batch_ws_get(const std::vector<Geom> &geo, int m, bool mixed, bool ge
     const size_t hb_inst = hbytes; hbytes += al256(ws->inst_bytes);
     const size_t hb_smap = hbytes; hbytes += al256(sizeof(int) * smap_cap);
     const size_t hb_umap = hbytes; hbytes += al256(sizeof(int) * ws->umap_cap);
+    const size_t hb_pmap = hbytes; hbytes += al256(sizeof(int) * pmap_cap);
     const size_t hb_amap = hbytes; hbytes += al256(sizeof(int) * count);
     const size_t hb_clk = hbytes; hbytes += 2 * ws->clk_bytes;
     e = cudaMallocHost(&ws->host, hbytes);
@@ -205,6 +231,7 @@ static int batch_ws_get(const std::vector<Geom> &geo, int m, bool mixed, bool ge
     ws->d_inst = ws->base + o_inst;
     ws->d_smap = (int *)(ws->base + o_smap);
     ws->d_umap = (int *)(ws->base + o_umap);
+    ws->d_pmap = (int *)(ws->base + o_pmap);
     ws->d_amap = (int *)(ws->base + o_amap);
     ws->d_clk = (BClock *)(ws->base + o_clk);
     ws->h_ctrl = (DevCtrl *)(ws->host + hb_ctrl);
@@ -212,6 +239,7 @@ static int batch_ws_get(const std::vector<Geom> &geo, int m, bool mixed, bool ge
     ws->h_inst = ws->host + hb_inst;
     ws->h_smap = (int *)(ws->host + hb_smap);
     ws->h_umap = (int *)(ws->host + hb_umap);
+    ws->h_pmap = (int *)(ws->host + hb_pmap);
     ws->h_amap = (int *)(ws->host + hb_amap);
     ws->h_clk = (BClock *)(ws->host + hb_clk);
     LSG_BCUDA(cudaStreamCreateWithFlags(&ws->stream, cudaStreamNonBlocking));
@@ -274,6 +302,43 @@ static void make_plan(BatchWs *ws, const std::vector<Geom> &geo, const std::vect
         sb0 += nb;
     }
     plan->sgrid = sb0;
+    // FP32 Richardson passes: the paired march's own tile grid, its z depth
+    // chosen by the same one-wave rule
+    plan->pgrid = 0;
+    if (ws->paired) {
+        const int pslots = sms * std::max(1, BatchKernels<T>::paired_blocks_per_sm());
+        long long pxy = 0, pcols = 0;
+        for (int i : act) {
+            ptiles_of(geo[i], &hi[i].ptx, &hi[i].pty);
+            pxy += (long long)hi[i].ptx * hi[i].pty;
+            pcols += (long long)hi[i].ptx * hi[i].pty * geo[i].nz;
+        }
+        int Lp = maxnz;
+        if (pxy < pslots) {
+            Lp = (int)std::max<long long>(8, (pcols + pslots - 1) / pslots);
+            auto pblocks_at = [&](int l) {
+                long long b = 0;
+                for (int i : act) {
+                    const int lz = std::min(l, geo[i].nz);
+                    b += (long long)hi[i].ptx * hi[i].pty * ((geo[i].nz + lz - 1) / lz);
+                }
+                return b;
+            };
+            while (Lp < maxnz && pblocks_at(Lp) > pslots) Lp++;
+            Lp = std::max(8, std::min(maxnz, (int)(Lp * lscale + 0.5)));
+        }
+        int pb0 = 0;
+        for (int i : act) {
+            const int lz = std::min(Lp, geo[i].nz);
+            hi[i].plz = lz;
+            const int nb = hi[i].ptx * hi[i].pty * ((geo[i].nz + lz - 1) / lz);
+            ws->h_ctl[i].pblk0 = pb0;
+            ws->h_ctl[i].pblocks = nb;
+            for (int b = 0; b < nb; b++) ws->h_pmap[pb0 + b] = i;
+            pb0 += nb;
+        }
+        plan->pgrid = pb0;
+    }
     long long need = 0;
     for (int i : act) need += (geo[i].n + 255) / 256;
     const long long U = std::min<long long>(need, (long long)kUcapPerSm * sms);
@@ -299,6 +364,8 @@ static int upload_tables(BatchWs *ws, const BPlan &plan) {
         LSG_BCUDA(cudaMemcpyAsync(ws->d_smap, ws->h_smap, sizeof(int) * plan.sgrid, cudaMemcpyHostToDevice, s));
     if (plan.ugrid > 0)
         LSG_BCUDA(cudaMemcpyAsync(ws->d_umap, ws->h_umap, sizeof(int) * plan.ugrid, cudaMemcpyHostToDevice, s));
+    if (plan.pgrid > 0)
+        LSG_BCUDA(cudaMemcpyAsync(ws->d_pmap, ws->h_pmap, sizeof(int) * plan.pgrid, cudaMemcpyHostToDevice, s));
     if (!plan.act.empty())
         LSG_BCUDA(cudaMemcpyAsync(ws->d_amap, ws->h_amap, sizeof(int) * plan.act.size(), cudaMemcpyHostToDevice, s));
     return LSG_OK;
@@ -360,7 +427,10 @@ struct BatchRun {
         return LSG_OK;
     }
     int richardson(int k) {
-        LSG_BL(BatchKernels<T>::richardson(tab(), args(ws->d_smap, k), plan.sgrid, generic, plan.var, ws->stream));
+        if (plan.pgrid > 0)
+            LSG_BL(BatchKernels<T>::richardson_paired(tab(), args(ws->d_pmap, k), plan.pgrid, ws->stream));
+        else
+            LSG_BL(BatchKernels<T>::richardson(tab(), args(ws->d_smap, k), plan.sgrid, generic, plan.var, ws->stream));
         return LSG_OK;
     }
     // One extrapolation cycle (iterations it0+1 .. it0+p) and the clock tick.
@@ -552,6 +622,7 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
     LSG_BCUDA(cudaStreamWaitEvent(s, ws->join, 0));
     std::vector<int> act(count);
     for (int i = 0; i < count; i++) act[i] = i;
+    ws->paired = 0;  // the tuner times the one-column march
     if (!generic && !ws->tuned && tune_mode() == 2) {
         rc = tune_batch<T>(ws, geo, act, prm, mixed);
         if (rc) return rc;
@@ -562,6 +633,14 @@ static int batch_solve(const lsg_operator *ops, int count, const lsg_params *prm
         const size_t vb = al256((size_t)geo[i].n * es);
         LSG_BCUDA(cudaMemsetAsync(hi[i].dx, 0, 2 * (size_t)m * vb, s));  // dx, df contiguous
         if (mixed) LSG_BCUDA(cudaMemsetAsync(hi[i].x, 0, vb, s));
+    }
+    // FP32: the Richardson passes take the paired march when every grid has an
+    // even nx (its pairs never straddle the wrap) and the vectors it touches
+    // are 8-byte aligned (the work arrays are; x is the caller's)
+    if constexpr (std::is_same<T, float>::value) {
+        bool ok = !generic && batch_paired_enabled();
+        for (int i = 0; i < count && ok; i++) ok = geo[i].nx % 2 == 0 && (((uintptr_t)hi[i].x) & 7u) == 0;
+        ws->paired = ok ? 1 : 0;
     }
     const int var = generic ? 0 : ws->tvar;
     const double lscale = generic ? 1.0 : ws->tscale;
@@ -734,6 +813,8 @@ int solve_mixed_batched(const lsg_operator *ops, int count, const lsg_params *pr
 }  // namespace lsg
 
 extern "C" {
+
+int lsg_set_batch_march(int paired) { return lsg::g_batch_paired.exchange(paired ? 1 : 0); }
 
 int lsg_aar_batched(const lsg_operator *ops, int count, const lsg_params *prm, int dtype, void *const *d_x,
                     const void *const *d_b, lsg_result *res, void *stream) {

@@ -183,6 +183,28 @@ __global__ void __launch_bounds__(32 * BY, MINB) batch_stencil_kernel(const BIns
     }
 }
 
+// The paired march (two columns per lane, 64-wide tiles) of one batched pass
+// whose functor has one (the FP32 Richardson passes); a.map is the paired
+// block map, the instance's paired tile grid is (ptx, pty) x z chunks of plz.
+// Results equal the one-column march's bit for bit.
+template <typename T, int BY, int NY, int MINB, class Pass>
+__global__ void __launch_bounds__(32 * BY, MINB) batch_stencil_x2_kernel(const BInst<T> *tab, BArgs a) {
+    constexpr int FX = 64 + 12;
+    constexpr int FY = BY * NY + 12;
+    __shared__ __align__(16) T smem[2][FX * FY];
+    const int i = a.map[blockIdx.x];
+    const BCtl &C = a.ctl[i];
+    const BInst<T> &I = tab[i];
+    typename Pass::Op op;
+    if (!Pass::make(I, C, a, op)) return;
+    if (op.skip()) return;
+    op.init();
+    const int lb = blockIdx.x - C.pblk0;
+    const int t = lb / I.ptx;
+    stencil_march_x2<T, BY, NY>(I.g, Pass::weights(I), I.plz, op, smem[0], smem[1], lb - t * I.ptx, t % I.pty,
+                                t / I.pty, lb);
+}
+
 // Batched stencil tile: tile variant V of the vector type (the refinement
 // pass keeps its own launch bounds); the generic-radius path uses variant 0
 // with one row per thread (NY = 1) so the widest staged plane stays in 48 KB.
@@ -475,6 +497,40 @@ cudaError_t BatchKernels<T>::richardson(const BInst<T> *tab, const BArgs &a, int
         return launch_batch_stencil<T, PassRichRecur<T>>(tab, a, grid, generic, var, s);
     } else {
         return launch_batch_stencil<T, PassRich<T>>(tab, a, grid, generic, var, s);
+    }
+}
+
+template <typename T>
+cudaError_t BatchKernels<T>::richardson_paired(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (grid <= 0) return cudaSuccess;
+        if (a.lean)
+            batch_stencil_x2_kernel<T, kPairBY, kPairNY, kPairMINB, PassRichLean<T>>
+                <<<grid, dim3(32, kPairBY), 0, s>>>(tab, a);
+        else
+            batch_stencil_x2_kernel<T, kPairBY, kPairNY, kPairMINB, PassRichRecur<T>>
+                <<<grid, dim3(32, kPairBY), 0, s>>>(tab, a);
+        return cudaGetLastError();
+    } else {
+        (void)tab, (void)a, (void)grid, (void)s;
+        return cudaErrorInvalidValue;
+    }
+}
+
+template <typename T>
+int BatchKernels<T>::paired_blocks_per_sm() {
+    if constexpr (std::is_same<T, float>::value) {
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &occ, batch_stencil_x2_kernel<T, kPairBY, kPairNY, kPairMINB, PassRichLean<T>>, 32 * kPairBY, 0) !=
+                cudaSuccess ||
+            occ < 1) {
+            cudaGetLastError();
+            occ = 1;
+        }
+        return occ;
+    } else {
+        return 0;
     }
 }
 

@@ -593,6 +593,7 @@ struct BCtl {
     double *part;        // this instance's partial sums
     long long n;
     int sblk0, sblocks;  // its share of the batched stencil launches
+    int pblk0, pblocks;  // its share of the paired-march Richardson launches (FP32)
     int ublk0, ublocks;  // its share of the batched point-local launches
     double hre, him;     // scale of the Gram right-hand side (the Jacobi factor)
     double sig_re, sig_im;  // the operator's shift (mixed solves deflate the constant mode when non-zero)
@@ -602,6 +603,7 @@ template <typename T>
 struct BInst {
     Geom g;
     int tx, ty, lz;      // stencil tiles along x and y; z planes per block
+    int ptx, pty, plz;   // the same for the paired march (64-wide tiles; FP32 Richardson passes)
     int vec;             // n is a multiple of the 16-byte vector width
     Weights<T> w;
     Weights<typename WideOf<T>::type> w64;
@@ -638,6 +640,11 @@ struct BatchKernels {
     // vectors, the reference form for FP64 ones).
     static cudaError_t richardson(const BInst<T> *tab, const BArgs &a, int grid, bool generic, int var,
                                   cudaStream_t s);
+    // The same pass in the paired march (FP32, radius 6, every nx even; a.map
+    // is the paired block map); cudaErrorInvalidValue for other types.
+    static cudaError_t richardson_paired(const BInst<T> *tab, const BArgs &a, int grid, cudaStream_t s);
+    // Resident blocks per SM of the paired Richardson pass (0 when T has none).
+    static int paired_blocks_per_sm();
     // r0 = b - A x, ||r0||^2 partials.
     static cudaError_t residual_init(const BInst<T> *tab, const BArgs &a, int grid, bool generic, int var,
                                      cudaStream_t s);

@@ -908,6 +908,26 @@ __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const floa
     block_reduce_store<NV>(acc, red, partials + (long long)blockIdx.x * NV, RING ? perm : nullptr);
 }
 
+// LSG_FAULT_GRAM_TX=<bytes>: failure test of the bulk-copy Gram's bounded
+// waits (every stage armed with that many bytes more than its copies bring),
+// which then give up after LSG_GRAM_WAIT_CYCLES SM clocks (default kWaitCycles).
+static inline unsigned gram_fault_tx() {
+    static const unsigned v = [] {
+        const char *e = getenv("LSG_FAULT_GRAM_TX");
+        const long t = e ? atol(e) : 0;
+        return (unsigned)(t > 0 && t < 65536 ? t : 0);
+    }();
+    return v;
+}
+static inline long long gram_wait_cycles() {
+    static const long long v = [] {
+        const char *e = getenv("LSG_GRAM_WAIT_CYCLES");
+        const long long t = e ? atoll(e) : 0;
+        return t >= 1000000 && t <= kWaitCycles ? t : kWaitCycles;
+    }();
+    return v;
+}
+
 template <int M>
 static size_t gram_bulk_smem() {
     return (size_t)kGramStages * (M + 1) * kGramChunk * sizeof(float);
@@ -1499,18 +1519,8 @@ static cudaError_t gram_dispatch(int m, const T *dx, const T *df, const T *r, lo
         // the bulk-copy form: 16-byte aligned columns and residual, n % 4 == 0
         if (n % 4 == 0 && m >= 1 && m <= 8 && (((uintptr_t)df | (uintptr_t)r) & 15u) == 0) {
             DevCtrl *c = const_cast<DevCtrl *>(ctrl);
-            // LSG_FAULT_GRAM_TX=<bytes>: failure test of the bounded waits, which
-            // then give up after LSG_GRAM_WAIT_CYCLES (default kWaitCycles)
-            static const unsigned extra_tx = [] {
-                const char *e = getenv("LSG_FAULT_GRAM_TX");
-                const long v = e ? atol(e) : 0;
-                return (unsigned)(v > 0 && v < 65536 ? v : 0);
-            }();
-            static const long long wait_cycles = [] {
-                const char *e = getenv("LSG_GRAM_WAIT_CYCLES");
-                const long long v = e ? atoll(e) : 0;
-                return v >= 1000000 && v <= kWaitCycles ? v : kWaitCycles;
-            }();
+            const unsigned extra_tx = gram_fault_tx();
+            const long long wait_cycles = gram_wait_cycles();
             switch (m) {
 #define LSG_GRAM_BULK(MM)                                                                                     \
     case MM: {                                                                                                \
@@ -1639,11 +1649,8 @@ cudaError_t Kernels<T>::ring_gram(int m, const RingWindow &rw, const T *ring, lo
     if constexpr (std::is_same<T, float>::value) {
         if (m < 1 || m > kRingMaxM || n % 4 != 0 || ss % 4 != 0 || !aligned16(ring, df))
             return cudaErrorInvalidValue;
-        static const long long wait_cycles = [] {
-            const char *e = getenv("LSG_GRAM_WAIT_CYCLES");
-            const long long v = e ? atoll(e) : 0;
-            return v >= 1000000 && v <= kWaitCycles ? v : kWaitCycles;
-        }();
+        const unsigned extra_tx = gram_fault_tx();
+        const long long wait_cycles = gram_wait_cycles();
         switch (m) {
 #define LSG_GRAM_RING(MM)                                                                                   \
     case MM: {                                                                                              \
@@ -1652,7 +1659,7 @@ cudaError_t Kernels<T>::ring_gram(int m, const RingWindow &rw, const T *ring, lo
                                                     (int)gram_bulk_smem<MM>());                             \
         if (ea != cudaSuccess) return ea;                                                                   \
         gram_bulk_kernel<MM, true><<<blocks, kReduceThreads, gram_bulk_smem<MM>(), s>>>(                    \
-            df, nullptr, n, partials, ctrl, 0u, wait_cycles, ring, ss, rw, (float)cf);                      \
+            df, nullptr, n, partials, ctrl, extra_tx, wait_cycles, ring, ss, rw, (float)cf);                \
         return cudaGetLastError();                                                                          \
     }
             LSG_GRAM_RING(1) LSG_GRAM_RING(2) LSG_GRAM_RING(3) LSG_GRAM_RING(4)

@@ -320,6 +320,8 @@ struct GmresWs {
 };
 
 static std::mutex g_gws_mu;
+// keyed by (device, element size, doubled for complex, n, m): FP64 and
+// complex64 vectors have the same size but different solver-state layouts
 static std::map<std::tuple<int, size_t, long long, int>, std::unique_ptr<GmresWs>> g_gws;
 
 int release_gmres_workspaces() {
@@ -332,7 +334,8 @@ int release_gmres_workspaces() {
     do {                                                                                     \
         cudaError_t e_ = (call);                                                             \
         if (e_ != cudaSuccess)                                                               \
-            return set_error(e_ == cudaErrorMemoryAllocation ? LSG_NO_MEMORY : LSG_CUDA_ERROR, \
+            return cudaGetLastError(), /* clear it for later launches */                     \
+                   set_error(e_ == cudaErrorMemoryAllocation ? LSG_NO_MEMORY : LSG_CUDA_ERROR, \
                              "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
 
@@ -356,7 +359,7 @@ static int gmres_t(const lsg_operator *op, const lsg_params *prm, T *x, const T 
     GmresWs *ws;
     {
         std::lock_guard<std::mutex> gl(g_gws_mu);
-        auto &slot = g_gws[std::make_tuple(dev, sizeof(T), n, m)];
+        auto &slot = g_gws[std::make_tuple(dev, (size_t)(sizeof(T) * (IsCplx<T>::value ? 2 : 1)), n, m)];
         if (!slot) slot.reset(new GmresWs());
         ws = slot.get();
     }
@@ -614,7 +617,7 @@ static int cocg_t(const lsg_operator *op, const lsg_params *prm, T *x, const T *
     const int mcols = 3;  // r, d ping-pong and q in the basis storage
     {
         std::lock_guard<std::mutex> gl(g_gws_mu);
-        auto &slot = g_gws[std::make_tuple(dev, sizeof(T), n, -mcols)];
+        auto &slot = g_gws[std::make_tuple(dev, (size_t)(sizeof(T) * (IsCplx<T>::value ? 2 : 1)), n, -mcols)];
         if (!slot) slot.reset(new GmresWs());
         ws = slot.get();
     }

@@ -56,7 +56,8 @@ const char *last_error() { return t_last_error; }
     do {                                                                                     \
         cudaError_t e_ = (call);                                                             \
         if (e_ != cudaSuccess)                                                               \
-            return set_error(e_ == cudaErrorMemoryAllocation ? LSG_NO_MEMORY : LSG_CUDA_ERROR, \
+            return cudaGetLastError(), /* clear it for later launches */                     \
+                   set_error(e_ == cudaErrorMemoryAllocation ? LSG_NO_MEMORY : LSG_CUDA_ERROR, \
                              "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
 
@@ -392,7 +393,8 @@ static const char *const kClassNames[LSG_K_CLASSES] = {"richardson", "residual",
         cudaError_t e_ = (call);                                                             \
         R.launches++;                                                                        \
         if (e_ != cudaSuccess)                                                               \
-            return set_error(LSG_CUDA_ERROR, "launch %s: %s", #call, cudaGetErrorString(e_)); \
+            return cudaGetLastError(),                                                       \
+                   set_error(LSG_CUDA_ERROR, "launch %s: %s", #call, cudaGetErrorString(e_)); \
         if (ea_) {                                                                           \
             cudaEvent_t eb_ = R.event();                                                     \
             if (eb_) { cudaEventRecord(eb_, R.s); R.recs.push_back({cls, ea_, eb_}); }       \

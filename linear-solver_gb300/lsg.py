@@ -100,7 +100,7 @@ EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "ls
            "lsg_pinv_solve_noalloc", "lsg_aar_batched", "lsg_aar_mixed_batched", "lsg_autotune",
            "lsg_set_autotune", "lsg_autotune_save", "lsg_autotune_load", "lsg_gmres",
            "lsg_aar_csr", "lsg_apply_csr", "lsg_register_operator_csr", "lsg_bounds_errors",
-           "lsg_set_fp64_arith", "lsg_aar_icc", "lsg_icc_factor", "lsg_cocg", "lsg_set_aar_form", "lsg_dot", "lsg_dot_blocks"]
+           "lsg_set_fp64_arith", "lsg_aar_icc", "lsg_icc_factor", "lsg_cocg", "lsg_set_aar_form", "lsg_dot", "lsg_dot_blocks", "lsg_set_batch_march"]
 
 KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "precond"]
 
@@ -142,6 +142,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
         L.lsg_set_autotune.argtypes = [ip]
         L.lsg_set_fp64_arith.argtypes = [ip]
         L.lsg_set_aar_form.argtypes = [ip]
+        L.lsg_set_batch_march.argtypes = [ip]
         L.lsg_dot_blocks.argtypes = [C.c_longlong]
         L.lsg_dot.argtypes = [ip, ip, C.c_longlong, vp, vp, vp, vp, vp]
         L.lsg_aar_icc.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), C.POINTER(ip), vp, vp,
@@ -467,6 +468,12 @@ def dot(x, y, batched: bool = False, stream=None):
     if w == 2:
         out = torch.view_as_complex(out.view(count, 2))
     return out if batched else out.reshape(())
+
+
+def set_batch_march(paired: bool) -> bool:
+    """FP32 batched Richardson passes: paired march (default) or one column per
+    lane; identical results.  Returns the previous setting."""
+    return bool(lib().lsg_set_batch_march(1 if paired else 0))
 
 
 def set_aar_form(form: int) -> int:

@@ -172,3 +172,28 @@ def test_batched_helmholtz_48(lsg, oracle):
     print(f"48 Helmholtz solves: max error vs FFT {worst:.2e}, "
           f"iterations {min(r['iters'] for r in rs)}..{max(r['iters'] for r in rs)}, "
           f"{rs[0]['seconds']:.3f} s, {rs[0]['launches']} launches")
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_batched_paired_march_bitwise(lsg, mixed):
+    """FP32 batches: the paired march of the Richardson passes (two columns
+    per lane, 64-wide tiles) against the one-column march, bit for bit, on
+    uneven grids (even nx), including a stop between extrapolations and
+    p - 1 > m (the x-carrying pass)."""
+    import torch
+    shapes = [(16, 16, 16), (34, 20, 12), (24, 30, 18), (66, 10, 9)]
+    ops = [lsg.Operator(sh, a=-float(sh[0] ** 2), sigma=s) for sh, s in zip(shapes, [0.0, 3.0, 0.5, 9.0])]
+    dt = torch.float64 if mixed else torch.float32
+    bs = [_cuda(_real_problem(sh, 50 + k), dt) for k, sh in enumerate(shapes)]
+    kws = [dict(tol=1e-9)] if mixed else [dict(tol=1e-5), dict(max_iter=23), dict(tol=1e-5, m=2, p=5)]
+    for kw in kws:
+        prev = lsg.set_batch_march(True)
+        try:
+            xp, rp = lsg.aar_batched(ops, bs, mixed=mixed, **kw)
+            lsg.set_batch_march(False)
+            x1, r1 = lsg.aar_batched(ops, bs, mixed=mixed, **kw)
+        finally:
+            lsg.set_batch_march(prev)
+        for a, b, ra, rb in zip(xp, x1, rp, r1):
+            assert ra["iters"] == rb["iters"] and ra["status"] == rb["status"]
+            assert torch.equal(a, b)

@@ -82,3 +82,22 @@ def test_gpu_cocg_rejects_real(lsg):
     b = torch.zeros((8, 8, 8), dtype=torch.float64, device="cuda")
     with pytest.raises(lsg.CudaLibraryError):
         lsg.cocg(lsg.Operator(8), b)
+
+
+@pytest.mark.gpu
+def test_gpu_gmres_workspaces_per_dtype(lsg):
+    """FP64 and complex64 vectors have the same element size but different
+    GMRES states: solves of both (and complex128) on one grid and restart
+    length, interleaved in one process, each converge."""
+    import torch
+    n = 12
+    rng = np.random.default_rng(4)
+    br = rng.uniform(-0.5, 0.5, (n, n, n))
+    bc = br + 1j * rng.uniform(-0.5, 0.5, (n, n, n))
+    opr = lsg.Operator(n, a=-float(n * n), sigma=2.0)
+    opc = lsg.Operator(n, a=-float(n * n), sigma=2.0 + 3.0j)
+    for dt, b, op in [(torch.float64, br, opr), (torch.complex64, bc, opc), (torch.complex128, bc, opc),
+                      (torch.float64, br, opr), (torch.complex64, bc, opc)]:
+        x, r = lsg.gmres(op, torch.from_numpy(b).to(device="cuda", dtype=dt), restart=20,
+                         tol=1e-5 if dt == torch.complex64 else 1e-8)
+        assert r["status"] == 0, (dt, r)
