@@ -557,8 +557,9 @@ def other_workloads(dev):
         secs, (x, r) = timed(fn)
         cmp[name] = {"seconds": secs, "iters": r["iters"], "relres": r["relres"], "status": r["status_name"]}
     res["krylov_comparison_256_1e-6"] = cmp
-    # the complex comparison (PETSC_COMPLEX/main.c:47-175: AAR against GMRES and
-    # BiCG): one 96^3 shifted Helmholtz instance, sigma = 20 + 10i, complex128, 1e-6
+    # the complex comparison (PETSC_COMPLEX/main.c:47-175: AAR against GMRES,
+    # LGMRES and BiCG): one 96^3 shifted Helmholtz instance, sigma = 20 + 10i,
+    # complex128, 1e-6
     n = 96
     rng = np.random.default_rng(96)
     bc = torch.from_numpy(rng.uniform(-0.5, 0.5, (n, n, n)) + 1j * rng.uniform(-0.5, 0.5, (n, n, n))).to(dev)
@@ -568,6 +569,7 @@ def other_workloads(dev):
     for name, fn in (("aar", lambda: lsg.aar(opc, bc, tol=1e-6)),
                      ("aar_mixed", lambda: lsg.aar_mixed(opc, bc, tol=1e-6)),
                      ("gmres30", lambda: lsg.gmres(opc, bc, restart=30, tol=1e-6, max_iter=20000)),
+                     ("lgmres30_2", lambda: lsg.lgmres(opc, bc, restart=30, aug=2, tol=1e-6, max_iter=20000)),
                      ("cocg", lambda: lsg.cocg(opc, bc, tol=1e-6))):
         secs, (x, r) = timed(fn)
         ccmp[name] = {"seconds": secs, "iters": r["iters"], "relres": r["relres"], "status": r["status_name"],

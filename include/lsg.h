@@ -207,6 +207,16 @@ int lsg_apply_csr(const lsg_csr *A, const double *d_x, double *d_y, void *stream
 int lsg_gmres(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x,
               const void *d_b, lsg_result *res, void *stream);
 
+/* LGMRES(m, aug) (the reference's KSPLGMRES, PETSC_COMPLEX/main.c:123-147;
+ * Baker, Jessup & Manteuffel 2005) with PETSc's convention: prm->m is the
+ * whole approximation space of a cycle, m - aug Krylov vectors plus the error
+ * approximations x_i - x_{i-1} of the last aug cycles (fewer in the first
+ * cycles; PETSc's defaults are m = 30, aug = 2).  Otherwise as lsg_gmres:
+ * left Jacobi, classical Gram-Schmidt, any dtype, res->iters counts operator
+ * applications.  1 <= aug <= min(4, m - 1). */
+int lsg_lgmres(const lsg_operator *op, const lsg_params *prm, int aug, int dtype, void *d_x,
+               const void *d_b, lsg_result *res, void *stream);
+
 /* BiCG on the complex-symmetric shifted operator (the reference's KSPBICG,
  * PETSC_COMPLEX/main.c:150-175), in its conjugate orthogonal CG form: with
  * the shadow residual conj(r0) BiCG's shadow iterates are the conjugates of

@@ -38,7 +38,7 @@ int solve_csr(const lsg_csr *A, const lsg_params *prm, double *x, const double *
               cudaStream_t s);
 // Restarted GMRES (lsg_krylov.cu).
 int gmres(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, const void *d_b, lsg_result *res,
-          cudaStream_t s);
+          cudaStream_t s, int aug = 0);
 int release_gmres_workspaces();
 // Block-Jacobi ICC(0) AAR (lsg_solvers.cu, kernels in lsg_icc.cu).
 int solve_icc(const lsg_operator *op, const lsg_params *prm, const int block[3], double *x, const double *b,

@@ -27,11 +27,19 @@
 #include <memory>
 #include <mutex>
 #include <tuple>
+#include <vector>
 
 #include "lsg_kernels.cuh"
 #include "lsg_host.h"
 
 namespace lsg {
+
+constexpr int kMaxAug = 4;  // LGMRES: error approximations kept (PETSc's default is 2)
+
+// Slots of the error approximations used in one LGMRES cycle, newest first.
+struct AugSlots {
+    int slot[kMaxAug];
+};
 
 // S: double for real vectors, cplx<double> for complex ones (Hermitian
 // inner products, complex Hessenberg matrix and Givens rotations).
@@ -46,6 +54,7 @@ struct GmresState {
     S H[(LSG_MAX_M + 1) * LSG_MAX_M];    // Hessenberg matrix, H[i * LSG_MAX_M + j]
     double cs[LSG_MAX_M];
     S sn[LSG_MAX_M], g[LSG_MAX_M + 1];
+    S zs[kMaxAug + 1];                   // LGMRES: scales of the error approximations z = zs_l Z_l
 };
 
 template <typename S>
@@ -77,8 +86,9 @@ struct ArnoldiOp {
     T scale;
     double *partials;
     const DevCtrl *ctrl;
+    int zslot = -1;  // LGMRES: >= 0 when the input is error approximation zslot (scale zs)
     __device__ bool skip() const { return cycle_over(st, ctrl); }
-    __device__ void init() { scale = (T)st->s[j]; }
+    __device__ void init() { scale = (T)(zslot < 0 ? st->s[j] : st->zs[zslot]); }
     __device__ __forceinline__ Raw fetch(unsigned i) const { return ldg(w + i); }
     __device__ __forceinline__ T value(const Raw &v) const { return v * scale; }
     __device__ __forceinline__ Ctr fetch_center(unsigned) const { return Ctr{}; }
@@ -248,8 +258,10 @@ __global__ void gmres_fin_step_kernel(const double *partials, int nblk, int j, i
 }
 
 // y = R^-1 g (back substitution on the rotated Hessenberg); coef_i = y_i s_i.
+// LGMRES (mk < m): the steps from mk on took error approximation aug.slot[i -
+// mk] as their input, so their coefficient is y_i zs_slot.
 template <typename S>
-__global__ void gmres_solve_y_kernel(GmresState<S> *st, const DevCtrl *ctrl) {
+__global__ void gmres_solve_y_kernel(GmresState<S> *st, const DevCtrl *ctrl, int mk, AugSlots aug) {
     if (solve_done(ctrl) || threadIdx.x != 0) return;
     const int k = st->k;
     S y[LSG_MAX_M];
@@ -259,7 +271,58 @@ __global__ void gmres_solve_y_kernel(GmresState<S> *st, const DevCtrl *ctrl) {
         const S d = st->H[i * LSG_MAX_M + i];
         y[i] = sabs(d) != 0.0 ? sdiv(t, d) : S(0.0);
     }
-    for (int i = 0; i < k; i++) st->coef[i] = y[i] * st->s[i];
+    for (int i = 0; i < k; i++) st->coef[i] = y[i] * (i < mk ? st->s[i] : st->zs[aug.slot[i - mk]]);
+}
+
+// LGMRES cycle end: delta = sum_{i < min(k, mk)} coef_i w_i + sum_{i >= mk}
+// coef_i Z_slot(i - mk) (= W y), written to the free slot zf; x += delta;
+// ||delta||^2 partials.
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) lgmres_delta_kernel(const T *__restrict__ V, long long ld,
+                                                                      T *Z, int mk, AugSlots aug, int zf, T *x,
+                                                                      long long n, double *partials,
+                                                                      const GmresState<typename ScalarOf<T>::type> *st,
+                                                                      const DevCtrl *ctrl) {
+    __shared__ double red[(kReduceThreads / 32) * AccWidth<T>::value];
+    __shared__ T c[LSG_MAX_M + 1];
+    if (solve_done(ctrl)) return;
+    const int k = st->k;
+    const int kv = k < mk ? k : mk;
+    if (threadIdx.x < k) c[threadIdx.x] = (T)st->coef[threadIdx.x];
+    __syncthreads();
+    Acc<T> acc;
+    acc.zero();
+    T *zo = Z + (long long)zf * ld;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+        T a = T(0);
+        for (int i = 0; i < kv; i++) a = fma(c[i], ldg(V + (long long)i * ld + t), a);
+        for (int i = mk; i < k; i++) a = fma(c[i], ldg(Z + (long long)aug.slot[i - mk] * ld + t), a);
+        zo[t] = a;
+        x[t] += a;
+        acc.add_prod(a, a);
+    }
+    Acc<T> a1[1] = {acc};
+    block_reduce_store<1>(a1, red, partials + blockIdx.x * AccWidth<T>::value);
+}
+
+// zs[zf] = 1 / ||delta|| (0 for a zero update).
+template <typename S>
+__global__ void lgmres_znorm_kernel(const double *partials, int nblk, int zf, GmresState<S> *st,
+                                    const DevCtrl *ctrl) {
+    constexpr int W = sizeof(S) / sizeof(double);
+    __shared__ double red[32];
+    if (solve_done(ctrl)) return;
+    double sum = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) sum += partials[(long long)b * W];
+    sum = warp_sum(sum);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += red[w];
+    const double nd = sqrt(tot);
+    st->zs[zf] = S(nd > 0.0 ? 1.0 / nd : 0.0);
 }
 
 // After r = b - A x (the new w_0): convergence on the true residual, else a
@@ -339,9 +402,12 @@ int release_gmres_workspaces() {
                              "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
 
+// aug > 0: LGMRES(m, aug) -- each cycle runs m - aug Krylov steps and then one
+// step on each of the last min(cycles, aug) error approximations (newest
+// first), kept in aug + 1 slots Z after the basis.
 template <typename T>
 static int gmres_t(const lsg_operator *op, const lsg_params *prm, T *x, const T *b, lsg_result *res,
-                   cudaStream_t s) {
+                   cudaStream_t s, int aug = 0) {
     using S = typename ScalarOf<T>::type;
     using State = GmresState<S>;
     const double t0 = std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -359,7 +425,7 @@ static int gmres_t(const lsg_operator *op, const lsg_params *prm, T *x, const T 
     GmresWs *ws;
     {
         std::lock_guard<std::mutex> gl(g_gws_mu);
-        auto &slot = g_gws[std::make_tuple(dev, (size_t)(sizeof(T) * (IsCplx<T>::value ? 2 : 1)), n, m)];
+        auto &slot = g_gws[std::make_tuple(dev, (size_t)(sizeof(T) * (IsCplx<T>::value ? 2 : 1)), n, m | (aug << 8))];
         if (!slot) slot.reset(new GmresWs());
         ws = slot.get();
     }
@@ -367,7 +433,7 @@ static int gmres_t(const lsg_operator *op, const lsg_params *prm, T *x, const T 
     if (!ws->base) {
         const long long ld = (long long)((((size_t)n * sizeof(T) + 255) & ~(size_t)255) / sizeof(T));
         const long long pcap = std::max<long long>((long long)rb * nchunk * kDotChunk, sb) * AccWidth<T>::value;
-        const size_t vbytes = (size_t)ld * sizeof(T) * (size_t)(m + 1);
+        const size_t vbytes = (size_t)ld * sizeof(T) * (size_t)(m + 1 + (aug > 0 ? aug + 1 : 0));
         const size_t pbytes = ((size_t)pcap * 8 + 255) & ~(size_t)255;
         const size_t cbytes = (sizeof(DevCtrl) + 255) & ~(size_t)255;
         cudaError_t e = cudaMalloc(&ws->base, vbytes + pbytes + cbytes + sizeof(State));
@@ -418,10 +484,22 @@ static int gmres_t(const lsg_operator *op, const lsg_params *prm, T *x, const T 
     };
     int rc = restart();
     if (rc) return rc;
+    // LGMRES: the error approximations' slots, newest first
+    T *Z = V + (long long)(m + 1) * ld;
+    const int mk = m - aug;
+    std::vector<int> zorder;
     auto cycle = [&](int) -> int {
-        for (int j = 0; j < m; j++) {
+        const int na = std::min((int)zorder.size(), aug);
+        const int steps = mk + na;
+        AugSlots as{};
+        for (int l = 0; l < na; l++) as.slot[l] = zorder[l];
+        for (int j = 0; j < steps; j++) {
             T *wj = V + (long long)j * ld, *z = V + (long long)(j + 1) * ld;
             ArnoldiOp<T> aop{wj, z, st, j, T(0), nullptr, ctrl};
+            if (j >= mk) {
+                aop.w = Z + (long long)as.slot[j - mk] * ld;
+                aop.zslot = as.slot[j - mk];
+            }
             LSG_GK(launch_stencil<T>(L, wcf, aop));
             const int nc = (j + 1 + kDotChunk - 1) / kDotChunk;
             gmres_dots_kernel<T><<<dim3(rb, nc), kReduceThreads, 0, s>>>(V, ld, j + 1, z, n, part, st, ctrl);
@@ -430,19 +508,31 @@ static int gmres_t(const lsg_operator *op, const lsg_params *prm, T *x, const T 
             LSG_GK(cudaGetLastError());
             gmres_combine_kernel<T><<<rb, kReduceThreads, 0, s>>>(V, ld, j + 1, z, n, part, st, ctrl, 0);
             LSG_GK(cudaGetLastError());
-            gmres_fin_step_kernel<S><<<1, 256, 0, s>>>(part, rb, j, m, acf, prm->max_iter, st, ctrl);
+            gmres_fin_step_kernel<S><<<1, 256, 0, s>>>(part, rb, j, steps, acf, prm->max_iter, st, ctrl);
             LSG_GK(cudaGetLastError());
         }
-        gmres_solve_y_kernel<S><<<1, 32, 0, s>>>(st, ctrl);
+        gmres_solve_y_kernel<S><<<1, 32, 0, s>>>(st, ctrl, aug > 0 ? mk : m + 1, as);
         LSG_GK(cudaGetLastError());
-        gmres_combine_kernel<T><<<rb, kReduceThreads, 0, s>>>(V, ld, m, x, n, part, st, ctrl, 1);
-        LSG_GK(cudaGetLastError());
+        if (aug > 0) {
+            // x += W y, kept (scaled to unit norm) as the newest error approximation
+            int zf = 0;
+            while (std::find(zorder.begin(), zorder.begin() + na, zf) != zorder.begin() + na) zf++;
+            lgmres_delta_kernel<T><<<rb, kReduceThreads, 0, s>>>(V, ld, Z, mk, as, zf, x, n, part, st, ctrl);
+            LSG_GK(cudaGetLastError());
+            lgmres_znorm_kernel<S><<<1, 256, 0, s>>>(part, rb, zf, st, ctrl);
+            LSG_GK(cudaGetLastError());
+            zorder.insert(zorder.begin(), zf);
+            if ((int)zorder.size() > aug) zorder.resize(aug);
+        } else {
+            gmres_combine_kernel<T><<<rb, kReduceThreads, 0, s>>>(V, ld, m, x, n, part, st, ctrl, 1);
+            LSG_GK(cudaGetLastError());
+        }
         return restart();
     };
 #undef LSG_GK
     // one cycle per "iteration" of the pipelined loop, convergence read every cycle
     int c = 0, batch = 0;
-    const int max_cycles = prm->max_iter / std::max(1, m) + 2;
+    const int max_cycles = prm->max_iter / std::max(1, m - aug) + 2;
     bool stop = false;
     while (!stop) {
         rc = cycle(c++);
@@ -729,17 +819,20 @@ int cocg(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, co
 }
 
 int gmres(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, const void *d_b, lsg_result *res,
-          cudaStream_t s) {
+          cudaStream_t s, int aug) {
     int rc = check_operator(op);
     if (rc) return rc;
     rc = check_params(prm, true);
     if (rc) return rc;
     if (!d_x || !d_b) return set_error(LSG_BAD_ARG, "NULL vector");
-    if (dtype == LSG_F64) return gmres_t<double>(op, prm, (double *)d_x, (const double *)d_b, res, s);
-    if (dtype == LSG_F32) return gmres_t<float>(op, prm, (float *)d_x, (const float *)d_b, res, s);
+    if (aug < 0 || aug > kMaxAug || (aug > 0 && aug >= prm->m))
+        return set_error(LSG_BAD_ARG, "LGMRES: augmentation %d outside 1..min(%d, m - 1)", aug, kMaxAug);
+    if (dtype == LSG_F64) return gmres_t<double>(op, prm, (double *)d_x, (const double *)d_b, res, s, aug);
+    if (dtype == LSG_F32) return gmres_t<float>(op, prm, (float *)d_x, (const float *)d_b, res, s, aug);
     if (dtype == LSG_C128)
-        return gmres_t<cplx<double>>(op, prm, (cplx<double> *)d_x, (const cplx<double> *)d_b, res, s);
-    if (dtype == LSG_C64) return gmres_t<cplx<float>>(op, prm, (cplx<float> *)d_x, (const cplx<float> *)d_b, res, s);
+        return gmres_t<cplx<double>>(op, prm, (cplx<double> *)d_x, (const cplx<double> *)d_b, res, s, aug);
+    if (dtype == LSG_C64)
+        return gmres_t<cplx<float>>(op, prm, (cplx<float> *)d_x, (const cplx<float> *)d_b, res, s, aug);
     return set_error(LSG_BAD_ARG, "GMRES: unknown dtype %d", dtype);
 }
 
@@ -747,7 +840,12 @@ int gmres(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, c
 
 extern "C" int lsg_gmres(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, const void *d_b,
                          lsg_result *res, void *stream) {
-    return lsg::gmres(op, prm, dtype, d_x, d_b, res, (cudaStream_t)stream);
+    return lsg::gmres(op, prm, dtype, d_x, d_b, res, (cudaStream_t)stream, 0);
+}
+
+extern "C" int lsg_lgmres(const lsg_operator *op, const lsg_params *prm, int aug, int dtype, void *d_x,
+                          const void *d_b, lsg_result *res, void *stream) {
+    return lsg::gmres(op, prm, dtype, d_x, d_b, res, (cudaStream_t)stream, aug);
 }
 
 extern "C" int lsg_cocg(const lsg_operator *op, const lsg_params *prm, int dtype, void *d_x, const void *d_b,

@@ -100,7 +100,7 @@ EXPORTS = ["lsg_lap_coefficient", "lsg_operator_init", "lsg_params_default", "ls
            "lsg_pinv_solve_noalloc", "lsg_aar_batched", "lsg_aar_mixed_batched", "lsg_autotune",
            "lsg_set_autotune", "lsg_autotune_save", "lsg_autotune_load", "lsg_gmres",
            "lsg_aar_csr", "lsg_apply_csr", "lsg_register_operator_csr", "lsg_bounds_errors",
-           "lsg_set_fp64_arith", "lsg_aar_icc", "lsg_icc_factor", "lsg_cocg", "lsg_set_aar_form", "lsg_dot", "lsg_dot_blocks", "lsg_set_batch_march"]
+           "lsg_set_fp64_arith", "lsg_aar_icc", "lsg_icc_factor", "lsg_cocg", "lsg_set_aar_form", "lsg_dot", "lsg_dot_blocks", "lsg_set_batch_march", "lsg_lgmres"]
 
 KERNEL_CLASSES = ["richardson", "residual", "gram", "update", "small", "cg", "refine", "precond"]
 
@@ -143,6 +143,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
         L.lsg_set_fp64_arith.argtypes = [ip]
         L.lsg_set_aar_form.argtypes = [ip]
         L.lsg_set_batch_march.argtypes = [ip]
+        L.lsg_lgmres.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), ip, ip, vp, vp, C.POINTER(_Result), vp]
         L.lsg_dot_blocks.argtypes = [C.c_longlong]
         L.lsg_dot.argtypes = [ip, ip, C.c_longlong, vp, vp, vp, vp, vp]
         L.lsg_aar_icc.argtypes = [C.POINTER(_Operator), C.POINTER(_Params), C.POINTER(ip), vp, vp,
@@ -355,6 +356,23 @@ def icc_factor(op, block=(8, 8, 8)):
     _check(lib().lsg_icc_factor(C.byref(op._s), blk, L.ctypes.data_as(dp), d.ctypes.data_as(dp), C.byref(sh)),
            "lsg_icc_factor", allow=(0,))
     return L.reshape(nb, 18), d, sh.value
+
+
+def lgmres(op, b, x0=None, restart=30, aug=2, stream=None, **kw):
+    """LGMRES(restart, aug), the reference's KSPLGMRES comparator
+    (PETSC_COMPLEX/main.c:123-147): restart = the whole approximation space,
+    restart - aug Krylov vectors plus the last aug error approximations."""
+    import torch
+    _check_vec(b, op, "b")
+    x = torch.zeros_like(b) if x0 is None else x0.clone()
+    res = _Result()
+    kw = dict(kw)
+    kw["m"] = restart
+    prm = _params(**kw)
+    rc = lib().lsg_lgmres(C.byref(op._s), C.byref(prm), int(aug), _dtype_code(b), C.c_void_p(x.data_ptr()),
+                          C.c_void_p(b.data_ptr()), C.byref(res), _stream_ptr(stream))
+    _check(rc, "lsg_lgmres")
+    return x, _result(res)
 
 
 def gmres(op, b, x0=None, restart=30, **kw):

@@ -347,6 +347,96 @@ def gmres(b: np.ndarray, x0=None, *, restart=30, tol=1e-8, max_iter=2000, radius
         x = x + sum((y[i] * s[i]) * W[i] for i in range(k))
 
 
+def lgmres(b: np.ndarray, x0=None, *, restart=30, aug=2, tol=1e-8, max_iter=2000, radius=6, a=A_REF,
+           sigma=0.0, precond=True):
+    """LGMRES(m, k) of Baker, Jessup & Manteuffel (SIAM J. Matrix Anal. Appl.
+    26, 2005) with the parameters of PETSc's KSPLGMRES defaults, which the
+    reference runs on its complex operator (PETSC_COMPLEX/main.c:123-147):
+    restart = m = the whole approximation space, m - k Krylov vectors plus the
+    error approximations z = x_i - x_{i-1} of the last k cycles (fewer in the
+    first cycles), newest first.  Each cycle runs the Arnoldi process on the
+    augmented set [v_1 .. v_{m-k}, z_1 .. z_na] (classical Gram-Schmidt,
+    Givens rotations, left Jacobi), x += W y, and keeps W y as the newest z.
+    Real or complex (Hermitian inner products, complex Givens rotations as in
+    gmres_c).  PETSc is absent here; this restates the published algorithm
+    with the steps of liblsg's lsg_lgmres.  Returns (x, dict)."""
+    cx = np.iscomplexobj(b) or isinstance(sigma, complex)
+    dt = np.complex128 if cx else np.float64
+    b = np.asarray(b, dtype=dt)
+    x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=dt, copy=True)
+    c = coefficients(radius)
+    if cx:
+        sg = complex(sigma)
+        cf = 1.0 / (a * 3.0 * c[0] + sg) if precond else 1.0 + 0j
+        A = lambda v: apply_c(v, radius, a, sg)
+    else:
+        cf = 1.0 / (a * 3.0 * c[0] + sigma) if precond else 1.0
+        A = lambda v: apply(v, radius, a, sigma)
+    acf = abs(cf)
+    bnorm = np.linalg.norm(b)
+    tol_abs = tol * bnorm
+    m, mk = restart, restart - aug
+    iters = 0
+    Z = []  # (vector, scale), newest first
+    while True:
+        r = b - A(x)
+        nr = np.linalg.norm(r)
+        if not nr > tol_abs or iters >= max_iter:
+            return x, dict(iters=iters, relres=nr / bnorm if bnorm > 0 else nr,
+                           converged=bool(not nr > tol_abs))
+        W = [r]
+        s = [(1.0 / nr) * (cf / acf)]
+        g = np.zeros(m + 1, dtype=dt)
+        g[0] = acf * nr
+        H = np.zeros((m + 1, m), dtype=dt)
+        cs = np.zeros(m)
+        sn = np.zeros(m, dtype=dt)
+        na = min(len(Z), aug)
+        k = 0
+        for j in range(mk + na):
+            u = s[j] * W[j] if j < mk else Z[j - mk][1] * Z[j - mk][0]
+            z = cf * A(u)
+            h = np.array([np.conj(s[i]) * np.vdot(W[i].ravel(), z.ravel()) for i in range(j + 1)])
+            H[:j + 1, j] = h
+            z = z - sum((h[i] * s[i]) * W[i] for i in range(j + 1))
+            eta = np.linalg.norm(z)
+            W.append(z)
+            s.append(1.0 / eta if eta > 0 else 0.0)
+            for i in range(j):
+                hi, hn = H[i, j], H[i + 1, j]
+                H[i, j] = cs[i] * hi + sn[i] * hn
+                H[i + 1, j] = cs[i] * hn - np.conj(sn[i]) * hi
+            hj = H[j, j]
+            if cx:  # c = |h| / rho, s = (h / |h|) eta / rho
+                ah = abs(hj)
+                rr = np.hypot(ah, eta)
+                ph = hj / ah if ah > 0 else 1.0
+                cs[j] = ah / rr if rr > 0 else 1.0
+                sn[j] = (eta / rr) * ph if rr > 0 else 0.0
+                H[j, j] = rr * ph
+            else:  # c = h / rho, s = eta / rho
+                rr = np.hypot(hj, eta)
+                cs[j], sn[j] = (hj / rr, eta / rr) if rr > 0 else (1.0, 0.0)
+                H[j, j] = rr
+            H[j + 1, j] = 0.0
+            g[j + 1] = -np.conj(sn[j]) * g[j]
+            g[j] = cs[j] * g[j]
+            k = j + 1
+            iters += 1
+            if abs(g[j + 1]) <= tol_abs * acf or iters >= max_iter or not eta > 0:
+                break
+        y = np.zeros(k, dtype=dt)
+        for i in range(k - 1, -1, -1):
+            y[i] = (g[i] - H[i, i + 1:k] @ y[i + 1:k]) / H[i, i] if H[i, i] != 0 else 0.0
+        delta = sum((y[i] * s[i]) * W[i] for i in range(min(k, mk)))
+        for i in range(mk, k):
+            delta = delta + (y[i] * Z[i - mk][1]) * Z[i - mk][0]
+        x = x + delta
+        nd = np.linalg.norm(delta)
+        Z.insert(0, (delta, 1.0 / nd if nd > 0 else 0.0))
+        del Z[aug:]
+
+
 def gmres_c(b: np.ndarray, x0=None, *, restart=30, tol=1e-8, max_iter=2000, radius=6, a=A_REF,
             sigma=0.0, precond=True):
     """Complex restarted GMRES(restart) for the complex-shifted operator

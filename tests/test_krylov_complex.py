@@ -1,8 +1,9 @@
 """The reference's complex Krylov comparators (PETSC_COMPLEX/main.c:80-175:
-KSPGMRES and KSPBICG on the complex-shifted Helmholtz operator; PETSc is
-absent, so the oracle restates Saad & Schultz's GMRES with Hermitian inner
-products and complex Givens rotations, and BiCG in its conjugate orthogonal
-CG form for the complex-symmetric operator).  CPU: the restatements against
+KSPGMRES, KSPLGMRES and KSPBICG on the complex-shifted Helmholtz operator;
+PETSc is absent, so the oracle restates Saad & Schultz's GMRES with Hermitian
+inner products and complex Givens rotations, Baker, Jessup & Manteuffel's
+LGMRES, and BiCG in its conjugate orthogonal CG form for the
+complex-symmetric operator).  CPU: the restatements against
 the FFT solve.  GPU (through the C ABI): against the restatements -- Arnoldi /
 COCG step counts within 1, solutions to 1e-6 -- and complex64 runs."""
 import numpy as np
@@ -34,6 +35,61 @@ def test_complex_gmres_on_real_data_is_real_gmres(oracle):
     x2, r2 = oracle.gmres_c(b + 0j, tol=1e-8)
     assert r1["iters"] == r2["iters"]
     assert np.abs(x1 - x2.real).max() <= 1e-12 * np.abs(x1).max()
+
+
+def test_lgmres_restatement(oracle):
+    """LGMRES with no augmentation is GMRES (same steps, same iterate); with
+    PETSc's default augmentation it solves the real and complex problems."""
+    n = 12
+    rng = np.random.default_rng(11)
+    b = rng.uniform(-0.5, 0.5, (n, n, n))
+    b -= b.mean()
+    a = -float(n * n)
+    x1, r1 = oracle.gmres(b, restart=20, tol=1e-9, a=a, sigma=2.0)
+    x0, r0 = oracle.lgmres(b, restart=20, aug=0, tol=1e-9, a=a, sigma=2.0)
+    assert r0["iters"] == r1["iters"] and np.array_equal(x0, x1)
+    for bb, sg in ((b, 2.0), (_problem(n, 4), 20 + 10j), (_problem(n, 5), 3 + 40j)):
+        x, r = oracle.lgmres(bb, restart=30, aug=2, tol=1e-10, a=a, sigma=sg, max_iter=5000)
+        xf = oracle.fft_solve(bb, a=a, sigma=sg)
+        assert r["converged"] and np.linalg.norm(x - xf) <= 1e-7 * np.linalg.norm(xf)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,sigma,restart,aug", [(16, 20 + 10j, 30, 2), (20, 3 + 40j, 12, 3), ((24, 16, 12), 2.0, 30, 2),
+                                                 (16, 0.5, 10, 1)])
+def test_gpu_lgmres_matches_restatement(lsg, oracle, n, sigma, restart, aug):
+    """LGMRES(m, k) (the reference's KSPLGMRES, PETSC_COMPLEX/main.c:123-147)
+    against the restatement: operator applications within 1, solution to 1e-6,
+    real and complex; complex64 / FP32 runs converge."""
+    import torch
+    nx, ny, nz = (n, n, n) if isinstance(n, int) else n
+    rng = np.random.default_rng(nx + 7 * restart)
+    cx = isinstance(sigma, complex)
+    b = rng.uniform(-0.5, 0.5, (nz, ny, nx))
+    if cx:
+        b = b + 1j * rng.uniform(-0.5, 0.5, (nz, ny, nx))
+    else:
+        b -= b.mean()
+    a = -float(nx * nx)
+    xo, ro = oracle.lgmres(b, restart=restart, aug=aug, tol=1e-9, a=a, sigma=sigma, max_iter=4000)
+    op = lsg.Operator((nx, ny, nz), a=a, sigma=sigma)
+    x, r = lsg.lgmres(op, torch.from_numpy(b).cuda(), restart=restart, aug=aug, tol=1e-9, max_iter=4000)
+    assert r["status"] == 0 and ro["converged"]
+    assert abs(r["iters"] - ro["iters"]) <= 1, (r, ro)
+    assert np.linalg.norm(x.cpu().numpy() - xo) <= 1e-6 * np.linalg.norm(xo)
+    lo = torch.complex64 if cx else torch.float32
+    x32, r32 = lsg.lgmres(op, torch.from_numpy(b).to(lo).cuda(), restart=restart, aug=aug, tol=1e-5, max_iter=4000)
+    assert r32["status"] == 0 and r32["relres"] <= 1e-5
+
+
+@pytest.mark.gpu
+def test_gpu_lgmres_rejects_bad_augmentation(lsg):
+    import torch
+    op = lsg.Operator(8, a=-64.0, sigma=1.0)
+    b = torch.ones((8, 8, 8), dtype=torch.float64, device="cuda")
+    for aug, restart in ((5, 30), (10, 10), (-1, 30)):
+        with pytest.raises(lsg.CudaLibraryError):
+            lsg.lgmres(op, b, restart=restart, aug=aug)
 
 
 @pytest.mark.gpu
