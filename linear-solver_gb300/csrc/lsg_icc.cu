@@ -26,11 +26,13 @@
 // previous step x - x_old (AAR.c:96-102 with the preconditioned residual).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <memory>
 #include <mutex>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "lsg_kernels.cuh"
@@ -351,11 +353,161 @@ __global__ void __launch_bounds__(kIccThreads) icc_apply_kernel(IccView F, Geom 
     }
 }
 
+// ---- the same apply with the factor staged in shared memory once per CTA
+// and one warp per box: a CTA loads L (slot-major, so a warp's points hit
+// distinct banks), 1/d, the level order and the coordinates once; each warp
+// then solves boxes on its own, its wavefront levels separated by warp
+// barriers only, with the box's vector in its own shared-memory slice.  The
+// per-point sums are the ones of icc_apply_kernel, in the same order, so the
+// result is the same bit for bit.
+constexpr int kIccWarps = 32;  // warps per CTA (fewer when the box's slices do not fit)
+
+template <typename V>
+__device__ __forceinline__ V icc_fnms(V acc, V l, V y);
+template <>
+__device__ __forceinline__ float2 icc_fnms<float2>(float2 acc, float2 l, float2 y) { return df_fnms(acc, l, y); }
+template <>
+__device__ __forceinline__ double icc_fnms<double>(double acc, double l, double y) { return fma(-l, y, acc); }
+
+// DFM: double-float pairs (V = float2), else FP64 (V = double).
+template <bool DFM>
+__global__ void __launch_bounds__(32 * kIccWarps) icc_apply_smem_kernel(IccView F, Geom g, const double *__restrict__ r,
+                                                                        double *__restrict__ f,
+                                                                        const double *__restrict__ f_old,
+                                                                        double *__restrict__ df,
+                                                                        double *__restrict__ hc, double beta, int hist,
+                                                                        int nboxes, const DevCtrl *ctrl) {
+    using V = typename std::conditional<DFM, float2, double>::type;
+    extern __shared__ __align__(16) unsigned char icc_sm[];
+    if (solve_done(ctrl)) return;
+    const int nb = F.nb, nlev = F.nlev, R = F.radius;
+    const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    V *Ls = reinterpret_cast<V *>(icc_sm);               // 18 x nb, slot-major
+    V *Ds = Ls + (size_t)nb * kIccSlots;                  // nb: 1 / d
+    V *Yall = Ds + nb;                                    // nw x nb
+    int *ord = reinterpret_cast<int *>(Yall + (size_t)nw * nb);
+    int *crd = ord + nb;
+    int *lvl = crd + nb;                                  // nlev + 1
+    const V *Lg = DFM ? reinterpret_cast<const V *>(F.Lf) : reinterpret_cast<const V *>(F.L);
+    const V *Dg = DFM ? reinterpret_cast<const V *>(F.dinvf) : reinterpret_cast<const V *>(F.dinv);
+    for (int k = threadIdx.x; k < nb * kIccSlots; k += blockDim.x) {
+        const int i = k / kIccSlots, sl = k - i * kIccSlots;
+        Ls[(size_t)sl * nb + i] = Lg[k];
+    }
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+        Ds[k] = Dg[k];
+        ord[k] = F.order[k];
+        crd[k] = F.coord[k];
+    }
+    for (int k = threadIdx.x; k <= nlev; k += blockDim.x) lvl[k] = F.lev[k];
+    const int ks = (DFM && ctrl) ? df_shift_for(ctrl->rhs_norm) : 0;
+    bool bad = false;
+    const int nbx = g.nx / F.bx, nby = g.ny / F.by;
+    const int st[3] = {1, F.bx, F.bx * F.by};
+    const int dim[3] = {F.bx, F.by, F.bz};
+    V *y = Yall + (size_t)warp * nb;
+    __syncthreads();
+    for (int box = blockIdx.x * nw + warp; box < nboxes; box += gridDim.x * nw) {
+        const int ox = (box % nbx) * F.bx, oy = ((box / nbx) % nby) * F.by, oz = (box / (nbx * nby)) * F.bz;
+        auto gidx = [&](int cw) -> long long {
+            return (long long)(ox + (cw & 0xff)) +
+                   (long long)g.nx * ((oy + ((cw >> 8) & 0xff)) + (long long)g.ny * (oz + (cw >> 16)));
+        };
+        for (int i = lane; i < nb; i += 32) {
+            const double rv = r[gidx(crd[i])];
+            if constexpr (DFM) y[i] = df_split(rv, ks, bad);
+            else y[i] = rv;
+        }
+        __syncwarp();
+        // forward: y_i = r_i - sum l(i, k) y_k over the lower neighbours k
+        for (int l = 0; l < nlev; l++) {
+            for (int t = lvl[l] + lane; t < lvl[l + 1]; t += 32) {
+                const int i = ord[t];
+                const int cw = crd[i];
+                const int c[3] = {cw & 0xff, (cw >> 8) & 0xff, cw >> 16};
+                V acc = y[i];
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+#pragma unroll
+                    for (int p = 1; p <= 6; p++)
+                        if (p <= R && c[a] >= p)
+                            acc = icc_fnms<V>(acc, Ls[(size_t)(6 * a + p - 1) * nb + i], y[i - p * st[a]]);
+                if constexpr (DFM) y[i] = df_norm(acc);
+                else y[i] = acc;
+            }
+            __syncwarp();
+        }
+        // backward: x_i = y_i / d_i - sum l(j, i) x_j over the upper neighbours j
+        for (int l = nlev - 1; l >= 0; l--) {
+            for (int t = lvl[l] + lane; t < lvl[l + 1]; t += 32) {
+                const int i = ord[t];
+                const int cw = crd[i];
+                const int c[3] = {cw & 0xff, (cw >> 8) & 0xff, cw >> 16};
+                V acc;
+                if constexpr (DFM) acc = df_mul(y[i], Ds[i]);
+                else acc = y[i] * Ds[i];
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+#pragma unroll
+                    for (int p = 1; p <= 6; p++)
+                        if (p <= R && c[a] + p < dim[a]) {
+                            const int j = i + p * st[a];
+                            acc = icc_fnms<V>(acc, Ls[(size_t)(6 * a + p - 1) * nb + j], y[j]);
+                        }
+                if constexpr (DFM) y[i] = df_norm(acc);
+                else y[i] = acc;
+            }
+            __syncwarp();
+        }
+        for (int i = lane; i < nb; i += 32) {
+            const long long gi = gidx(crd[i]);
+            double fv;
+            if constexpr (DFM) fv = df_to_double(y[i], ks);
+            else fv = y[i];
+            f[gi] = fv;
+            if (hist) {
+                const double d = fv - f_old[gi];
+                df[gi] = d;
+                hc[gi] = fma(beta, d, hc[gi]);
+            }
+        }
+        __syncwarp();  // y is reused by the warp's next box
+    }
+    if (DFM && __syncthreads_or(bad ? 1 : 0) && threadIdx.x == 0 && ctrl)
+        atomicOr(&const_cast<DevCtrl *>(ctrl)->df_range, 1);
+}
+
+// Shared memory of icc_apply_smem_kernel with nw warps.
+static size_t icc_smem_bytes(const IccFactor *F, int nw) {
+    return (size_t)F->nb * kIccSlots * 8 + (size_t)F->nb * 8 + (size_t)nw * F->nb * 8 + (size_t)F->nb * 8 +
+           (size_t)(F->nlev + 1) * 4;
+}
+constexpr size_t kIccSmemMax = 220 * 1024;
+
 cudaError_t icc_apply(const IccFactor *F, const Geom &g, const double *r, double *f, const double *f_old,
                       double *df, double *hc, double beta, int hist, const DevCtrl *ctrl, int exact, cudaStream_t s) {
     const IccView v{F->L, F->dinv, F->Lf, F->dinvf, F->order, F->lev, F->coord, F->bx, F->by, F->bz, F->nb,
                     F->nlev, F->radius};
     const long long boxes = (long long)(g.nx / F->bx) * (g.ny / F->by) * (g.nz / F->bz);
+    int nw = kIccWarps;
+    while (nw > 4 && icc_smem_bytes(F, nw) > kIccSmemMax) nw /= 2;
+    const size_t sm2 = icc_smem_bytes(F, nw);
+    if (sm2 <= kIccSmemMax && boxes < (1LL << 30)) {
+        // the factor staged once per CTA, one warp per box
+        auto launch = [&](auto kern) -> cudaError_t {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+            if (e != cudaSuccess) return e;
+            int occ = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32 * nw, sm2);
+            if (e != cudaSuccess) return e;
+            const long long need = (boxes + nw - 1) / nw;
+            const unsigned grid = (unsigned)std::max<long long>(
+                1, std::min<long long>(need, (long long)sm_count() * std::max(1, occ)));
+            kern<<<grid, 32 * nw, sm2, s>>>(v, g, r, f, f_old, df, hc, beta, hist, (int)boxes, ctrl);
+            return cudaGetLastError();
+        };
+        return exact ? launch(icc_apply_smem_kernel<false>) : launch(icc_apply_smem_kernel<true>);
+    }
     const size_t smem = (size_t)F->nb * sizeof(double);
     if (exact)
         icc_apply_kernel<false><<<(unsigned)boxes, kIccThreads, smem, s>>>(v, g, r, f, f_old, df, hc, beta, hist, ctrl);

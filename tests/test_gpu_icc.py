@@ -1,7 +1,10 @@
 """Block-Jacobi ICC(0) AAR on the GPU (lsg_aar_icc, the reference's pc = 1)
 against the oracle's restatement (oracle.aar_general with the block ICC(0)
 preconditioner on the same boxes): identical iteration counts and solutions,
-in FP64 arithmetic and in the default double-float stencil arithmetic."""
+in FP64 arithmetic and in the default double-float stencil arithmetic.
+Boxes whose factor fits in shared memory (up to ~1000 points) take the
+staged kernel that solves four boxes per CTA; 16 x 16 x 8 boxes the
+one-box-per-CTA kernel."""
 import numpy as np
 import pytest
 
@@ -21,7 +24,8 @@ def _oracle_icc(oracle, b, shape, block, radius=6, sigma=0.0, **kw):
 @pytest.mark.parametrize("mode", [1, 0])
 @pytest.mark.parametrize("n,block,radius,sigma", [((16, 16, 16), (8, 8, 8), 6, 0.0),
                                                   ((24, 16, 20), (4, 8, 5), 6, 0.0),
-                                                  ((16, 16, 16), (8, 4, 8), 3, 0.4)])
+                                                  ((16, 16, 16), (8, 4, 8), 3, 0.4),
+                                                  ((32, 32, 16), (16, 16, 8), 6, 0.0)])
 def test_icc_matches_restatement(lsg, oracle, mode, n, block, radius, sigma):
     import torch
     import workloads
