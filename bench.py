@@ -57,6 +57,22 @@ CPU_SAMPLE_ITERS = 24
 RICH32_TRAFFIC_BYTES = {False: 224.2e6, True: 101.0e6}
 
 
+def solve_roofline(n, inner_iters, outer_iters, seconds, fp64_iters, fp64_seconds, peak):
+    """Algorithmic bytes of a whole AAR solve (11 vectors per iteration at
+    m = 7, p = 6: (p - 1) 7-vector Richardson steps and one (3m + 10)-vector
+    extrapolation per cycle; 5 FP64 vectors per mixed outer step) over its
+    wall time, for the mixed and the FP64 solve."""
+    per_it = ((SOLVER_KW["p"] - 1) * 7 + 3 * SOLVER_KW["m"] + 10) / SOLVER_KW["p"]
+    mixed_b = per_it * n * 4 * inner_iters + 5 * 8 * n * outer_iters
+    fp64_b = per_it * n * 8 * fp64_iters
+    return {"vectors_per_iteration": per_it, "unit": "GB/s", "peak": peak,
+            "mixed": {"bytes": mixed_b, "achieved": mixed_b / seconds / 1e9, "frac": mixed_b / seconds / 1e9 / peak},
+            "fp64": {"bytes": fp64_b, "achieved": fp64_b / fp64_seconds / 1e9,
+                     "frac": fp64_b / fp64_seconds / 1e9 / peak},
+            "note": "the reference algorithm's data movement; the residual ring moves ~34 vectors per "
+                    "6-iteration cycle instead of 66, so the mixed figure can exceed the copy peak"}
+
+
 def aar_form_in_use(lsg):
     """The FP32 AAR form the library will run (0 ring, 1 lean, 2 x-carrying)."""
     f = lsg.set_aar_form(0)
@@ -468,6 +484,11 @@ def run_lsg(args):
                      "share_of_kernel_time": rms / total_ms if total_ms else None},
         "kernel_profile_ms": {k: round(v[1], 4) for k, v in prof.items() if v[0]},
         "updates_per_s": {"mixed": N * infos[-1]["inner_iters"] / value, "fp64": N * fp64["aar"]["iters"] / fp64_s},
+        # whole-solve figure: the reference algorithm's data movement (AAR average
+        # 11 N s per iteration at m = 7, p = 6; a mixed solve's outer step adds
+        # 5 N 8 bytes) over the measured solve time
+        "roofline_solve": solve_roofline(N, infos[-1]["inner_iters"], infos[-1]["outer_iters"], value,
+                                         fp64["aar"]["iters"], fp64_s, peak),
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 2 * N * 8,
                 "d2h_bytes_per_step": N * 8, "path": "AAR(POISSON*, ...) drop-in, mixed mode, pinned host buffers",
                 "converged": e2e_ok},
