@@ -73,10 +73,12 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // (FP64) to out[0..NV).  `scratch` is NV * 32 doubles of shared memory.
 // FP32 accumulators are reduced as double-float pairs with FP32 instructions;
 // only the NV final conversions to double touch the (slow) FP64 pipe.
-// perm (optional, shared memory): total k goes to out[perm[k]].
+// perm (optional, shared memory): total k goes to out[perm[k]].  s1, s2:
+// powers of two the (double) totals are multiplied by, one after the other
+// (scaled double-float sums).
 template <int NV, typename T>
 __device__ __forceinline__ void block_reduce_store(Acc<T> (&acc)[NV], double *scratch, double *out,
-                                                   const int *perm = nullptr) {
+                                                   const int *perm = nullptr, double s1 = 1.0, double s2 = 1.0) {
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     const int lane = tid & 31, warp = tid >> 5;
     const int nwarps = (blockDim.x * blockDim.y) >> 5;
@@ -105,7 +107,7 @@ __device__ __forceinline__ void block_reduce_store(Acc<T> (&acc)[NV], double *sc
             float hi = 0.f, lo = 0.f;
             if (lane < nwarps) { const float2 v = sf[k * nwarps + lane]; hi = v.x; lo = v.y; }
             df_warp_sum(hi, lo);
-            if (lane == 0) out[perm ? perm[k] : k] = (double)hi + (double)lo;
+            if (lane == 0) out[perm ? perm[k] : k] = ((double)hi + (double)lo) * s1 * s2;
         }
     }
 }

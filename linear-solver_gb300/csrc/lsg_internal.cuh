@@ -440,8 +440,9 @@ struct Kernels {
     static int gram_grid(int kind, int m, long long n, int sms);
     // Gram partials over the history (point-local, grid-stride).  Complex
     // vectors: G(i,j) = DF_i^H DF_j, h_j = DF_j^H r (PETSC_COMPLEX/AAR_Complex.c:213-216).
+    // exact = 0: FP64 vectors summed in double-float arithmetic (m <= 8).
     static cudaError_t gram(int kind, int m, const T *dx, const T *df, const T *r, long long n,
-                            double *partials, int blocks, const DevCtrl *ctrl, cudaStream_t s);
+                            double *partials, int blocks, const DevCtrl *ctrl, cudaStream_t s, int exact = 1);
     // AAR extrapolation: x += beta*f - sum_j H_j s_j with f = r*cf and
     // H_j = DX_j + beta DF_j; step = x_new - x_old.
     static cudaError_t aar_update(int m, T *x, const T *r, const T *h, T *step, double beta,

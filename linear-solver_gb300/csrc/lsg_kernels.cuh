@@ -711,6 +711,70 @@ __device__ __forceinline__ void gram_block(const T *__restrict__ dx, const T *__
     block_reduce_store<NV>(acc, red, out);
 }
 
+// The FP64 Gram in double-float arithmetic on the FP32 pipe (the solvers'
+// default double-float mode; GB300 runs FP64 at ~1/64 of FP32, which bound
+// the FP64 form at ~6x its DRAM time).  Each double is split once into a float
+// pair scaled by 2^k (df_split, k from ||b||), each product is formed by the
+// FMA two-product with its cross terms (~2^-47 relative, the rounding of a
+// thread's FP64 running sum of ~50 products), sums are double-float pairs,
+// and the block totals are converted to doubles and scaled back by 2^-2k.
+__device__ __forceinline__ void acc_prod_df(Acc<float> &acc, float2 a, float2 b) {
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    float s, t;
+    two_sum(acc.hi, p, s, t);
+    acc.hi = s;
+    acc.lo = __fadd_rn(acc.lo, __fadd_rn(t, e));
+}
+
+template <int KIND, int M>
+__global__ void __launch_bounds__(kReduceThreads) gram_df_kernel(const double *__restrict__ dx,
+                                                                 const double *__restrict__ df,
+                                                                 const double *__restrict__ r, long long n,
+                                                                 double *partials, DevCtrl *ctrl) {
+    constexpr int NP = (KIND == GRAM_SYM) ? (M * (M + 1)) / 2 : M * M;
+    constexpr int NV = NP + M;
+    __shared__ double red[NV * (kReduceThreads / 32)];
+    if (solve_done(ctrl)) return;
+    const int k = ctrl ? df_shift_for(ctrl->rhs_norm) : 0;
+    bool bad = false;
+    Acc<float> acc[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) acc[q].zero();
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        float2 f[M], xv[KIND == GRAM_SYM ? 1 : M];
+#pragma unroll
+        for (int j = 0; j < M; j++) f[j] = df_split(ldg(df + j * n + i), k, bad);
+        if (KIND == GRAM_GALERKIN) {
+#pragma unroll
+            for (int j = 0; j < M; j++) xv[j] = df_split(ldg(dx + j * n + i), k, bad);
+        }
+        const float2 rv = df_split(ldg(r + i), k, bad);
+        int q = 0;
+        if (KIND == GRAM_SYM) {
+#pragma unroll
+            for (int j = 0; j < M; j++)
+#pragma unroll
+                for (int a = 0; a <= j; a++) { acc_prod_df(acc[q], f[a], f[j]); q++; }
+#pragma unroll
+            for (int j = 0; j < M; j++) acc_prod_df(acc[NP + j], f[j], rv);
+        } else {
+#pragma unroll
+            for (int a = 0; a < M; a++)
+#pragma unroll
+                for (int j = 0; j < M; j++) { acc_prod_df(acc[q], xv[a], f[j]); q++; }
+#pragma unroll
+            for (int j = 0; j < M; j++) acc_prod_df(acc[NP + j], xv[j], rv);
+        }
+    }
+    const double us = ldexp(1.0, -k);  // (u 2^k)(v 2^k): scale back by 2^-k twice
+    block_reduce_store<NV>(acc, red, partials + (long long)blockIdx.x * NV, nullptr, us, us);
+    if (__syncthreads_or(bad ? 1 : 0) && threadIdx.x == 0 && ctrl) atomicOr(&ctrl->df_range, 1);
+}
+
 template <typename T, int KIND, int M>
 __global__ void __launch_bounds__(kReduceThreads) gram_kernel(const T *__restrict__ dx,
                                                               const T *__restrict__ df,
@@ -1587,7 +1651,25 @@ int Kernels<T>::gram_grid(int kind, int m, long long n, int sms) {
 
 template <typename T>
 cudaError_t Kernels<T>::gram(int kind, int m, const T *dx, const T *df, const T *r, long long n,
-                             double *partials, int blocks, const DevCtrl *ctrl, cudaStream_t s) {
+                             double *partials, int blocks, const DevCtrl *ctrl, cudaStream_t s, int exact) {
+    if constexpr (std::is_same<T, double>::value) {
+        if (!exact && m >= 1 && m <= 8) {
+            DevCtrl *c = const_cast<DevCtrl *>(ctrl);
+            switch (m) {
+#define LSG_GRAM_DF(MM)                                                                                        \
+    case MM:                                                                                                   \
+        if (kind == GRAM_SYM)                                                                                  \
+            gram_df_kernel<GRAM_SYM, MM><<<blocks, kReduceThreads, 0, s>>>(dx, df, r, n, partials, c);         \
+        else                                                                                                   \
+            gram_df_kernel<GRAM_GALERKIN, MM><<<blocks, kReduceThreads, 0, s>>>(dx, df, r, n, partials, c);    \
+        return cudaGetLastError();
+                LSG_GRAM_DF(1) LSG_GRAM_DF(2) LSG_GRAM_DF(3) LSG_GRAM_DF(4)
+                LSG_GRAM_DF(5) LSG_GRAM_DF(6) LSG_GRAM_DF(7) LSG_GRAM_DF(8)
+#undef LSG_GRAM_DF
+            default: break;
+            }
+        }
+    }
     if constexpr (IsCplx<T>::value) {
         using R = typename RealOf<T>::type;
         (void)kind;

@@ -687,7 +687,7 @@ struct AarLoop {
           }
         }
         if (is_anderson(it)) {
-            LSG_KC(LSG_K_GRAM, Kernels<T>::gram(GRAM_SYM, m, DX, DF, Rv[rc], n, part, gb, ctrl, R.s));
+            LSG_KC(LSG_K_GRAM, Kernels<T>::gram(GRAM_SYM, m, DX, DF, Rv[rc], n, part, gb, ctrl, R.s, L.exact));
             if constexpr (IsCplx<T>::value)
                 LSG_KC(LSG_K_SMALL, finalize_gram_solve_c(part, gb, m, cf, ctrl, R.s));
             else
@@ -806,7 +806,7 @@ int prich_core(Run &R, bool galerkin, const lsg_operator *op, const lsg_params *
                                       cf, 0.0, ctrl));
         cur ^= 1;
         if (is_proj(it)) {
-            LSG_KC(LSG_K_GRAM, Kernels<T>::gram(kind, m, DX, DF, Rv[cur], n, part, gb, ctrl, R.s));
+            LSG_KC(LSG_K_GRAM, Kernels<T>::gram(kind, m, DX, DF, Rv[cur], n, part, gb, ctrl, R.s, L.exact));
             LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, gb, kind, m, 1.0, ctrl, R.s));
             LSG_KC(LSG_K_UPDATE, Kernels<T>::proj_update(m, col, X[cur], Rv[cur], DX, DF, n, part, rb, ctrl, R.s));
             LSG_KC(LSG_K_SMALL, finalize_norm(part, rb, ctrl, NF_CHECK, prm->tol, it, R.s));
@@ -1149,7 +1149,7 @@ int solve_icc(const lsg_operator *op, const lsg_params *prm, const int block[3],
         const double *f = Fv[fc];
         double *hcol = H + (size_t)((it - 1) % m) * n;
         if (is_anderson(it)) {
-            LSG_KC(LSG_K_GRAM, Kernels<double>::gram(GRAM_SYM, m, H, DF, f, n, part, gb, ctrl, s));
+            LSG_KC(LSG_K_GRAM, Kernels<double>::gram(GRAM_SYM, m, H, DF, f, n, part, gb, ctrl, s, L.exact));
             LSG_KC(LSG_K_SMALL, finalize_gram_solve(part, gb, GRAM_SYM, m, 1.0, ctrl, s));
             LSG_KC(LSG_K_UPDATE, Kernels<double>::aar_update(m, X[xc], f, H, hcol, prm->beta, 1.0, n, ctrl, s));
             LSG_KC(LSG_K_RESIDUAL, Kernels<double>::residual(L, w, RES_INIT, X[xc], b, r, nullptr, nullptr, 1.0, 0.0,
