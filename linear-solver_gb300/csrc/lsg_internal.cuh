@@ -300,7 +300,10 @@ constexpr int kPair2BY = 4, kPair2NY = 2, kPair2MINB = 4;
 template <typename T, int V> struct TileVar;
 template <> struct TileVar<double, 0> { static constexpr int BY = 8, NY = 1, MINB = 2; };
 template <> struct TileVar<double, 1> { static constexpr int BY = 16, NY = 1, MINB = 1; };
-template <> struct TileVar<double, 2> { static constexpr int BY = 8, NY = 1, MINB = 3; };
+// two rows per thread (32 x 16 tile, one 256-thread block per SM at ~200
+// registers): the double-float march is issue-bound and a taller tile stages
+// ~26% fewer halo values per point (the tuner's choice at 256^3: 557 vs 631 us)
+template <> struct TileVar<double, 2> { static constexpr int BY = 8, NY = 2, MINB = 1; };
 template <> struct TileVar<float, 0> { static constexpr int BY = 4, NY = 4, MINB = 4; };
 template <> struct TileVar<float, 1> { static constexpr int BY = 8, NY = 2, MINB = 2; };
 template <> struct TileVar<float, 2> { static constexpr int BY = 4, NY = 2, MINB = 4; };

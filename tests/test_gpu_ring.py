@@ -44,6 +44,8 @@ CASES = [
     ((16, 16, 16), dict(max_iter=23, m=5, p=4)),
     ((16, 16, 16), dict(max_iter=17)),
     ((15, 13, 11), dict(tol=1e-5)),  # n % 4 != 0: the lean form runs
+    ((15, 16, 12), dict(tol=1e-5)),  # odd nx: the ring passes in the one-column march
+    ((16, 12, 20), dict(tol=1e-5, radius=4)),  # generic radius
 ]
 
 
@@ -51,7 +53,8 @@ CASES = [
 def test_ring_equals_x_carrying_fp32(lsg, shape, kw):
     import torch
     nx = shape[0]
-    op = lsg.Operator(shape, a=-float(nx * nx), sigma=0.5)
+    kw = dict(kw)
+    op = lsg.Operator(shape, radius=kw.pop("radius", 6), a=-float(nx * nx), sigma=0.5)
     b = torch.from_numpy(_problem(shape, sum(shape))).to(device="cuda", dtype=torch.float32)
     res = _solve_forms(lsg, lambda: lsg.aar(op, b, **kw))
     (x0, r0), (x2, r2), (x1, r1) = res[0], res[2], res[1]
