@@ -272,7 +272,7 @@ struct StencilLaunch {
     cudaStream_t stream;
     int tile = 0;     // tile variant (passes without partial sums only)
     int paired = -1;  // 1: the two-columns-per-lane march (planned by Kernels<T>::paired_plan);
-                      // 2: its 64 x 8 shape (passes without partial sums only);
+                      // 2: its 64 x 8 shape, 3: its 64 x 32 shape (passes without partial sums only);
                       // -1: the solver may choose it; 0: not
     int exact = 0;    // FP64 passes: 1 = FP64-arithmetic march, 0 = the double-float one
 };
@@ -297,6 +297,11 @@ constexpr int kPairBY = 8, kPairNY = 2, kPairMINB = 2;  // its block: 32 x 8 thr
 // keep the first shape (in the second they spill: 4 halo slots per thread).
 constexpr int kTilePaired2 = 4;
 constexpr int kPair2BY = 4, kPair2NY = 2, kPair2MINB = 4;
+// A third, taller shape for passes without a reduction (tuner code 5): 32 x 8
+// threads, 4 rows x 2 columns each (64 x 32 tile), one block per SM at ~210
+// registers: ~0.56 staged halo values per point instead of 1.7 in 64 x 8.
+constexpr int kTilePaired3 = 5;
+constexpr int kPair3BY = 8, kPair3NY = 4, kPair3MINB = 1;
 template <typename T, int V> struct TileVar;
 template <> struct TileVar<double, 0> { static constexpr int BY = 8, NY = 1, MINB = 2; };
 template <> struct TileVar<double, 1> { static constexpr int BY = 16, NY = 1, MINB = 1; };

@@ -529,7 +529,9 @@ int Kernels<T>::paired_blocks_per_sm(int shape) {
     if constexpr (std::is_same<T, float>::value) {
         int occ = 0;
         const cudaError_t e =
-            shape == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            shape == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                             &occ, stencil_x2_kernel<T, kPair3BY, kPair3NY, kPair3MINB, RichRingOp<T>>, 32 * kPair3BY, 0)
+            : shape == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                              &occ, stencil_x2_kernel<T, kPair2BY, kPair2NY, kPair2MINB, RichLeanOp<T>>, 32 * kPair2BY, 0)
                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                              &occ, stencil_x2_kernel<T, kPairBY, kPairNY, kPairMINB, RichLeanOp<T>>, 32 * kPairBY, 0);
@@ -577,8 +579,10 @@ cudaError_t launch_stencil(const StencilLaunch &L, const Weights<T> &w, const Op
         if constexpr (IsPaired<Op>::value && std::is_same<T, float>::value) {
             if (!paired_ok<T>(L, w, op)) return cudaErrorInvalidValue;
             if (L.paired == 1) return launch_x2<T, kPairBY, kPairNY, kPairMINB>(L, w, op);
-            if constexpr (Op::NACC == 0)
+            if constexpr (Op::NACC == 0) {
                 if (L.paired == 2) return launch_x2<T, kPair2BY, kPair2NY, kPair2MINB>(L, w, op);
+                if (L.paired == 3) return launch_x2<T, kPair3BY, kPair3NY, kPair3MINB>(L, w, op);
+            }
             return cudaErrorInvalidValue;
         } else {
             return cudaErrorInvalidValue;

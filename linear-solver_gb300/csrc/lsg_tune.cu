@@ -176,8 +176,8 @@ static int tune_t(const lsg_operator *op, cudaStream_t s, TuneEntry *out, int *n
     int plz = 0;
     if (rc == LSG_OK && Kernels<T>::paired_plan(g, &plz) > 0 && std::is_same<T, float>::value &&
         g.nx % 2 == 0) {
-        for (int shape = 1; shape <= 2 && rc == LSG_OK; shape++) {
-            const int rows = shape == 1 ? kPairBY * kPairNY : kPair2BY * kPair2NY;
+        for (int shape = 1; shape <= 3 && rc == LSG_OK; shape++) {
+            const int rows = shape == 1 ? kPairBY * kPairNY : shape == 2 ? kPair2BY * kPair2NY : kPair3BY * kPair3NY;
             const int slots = sms * Kernels<T>::paired_blocks_per_sm(shape);
             const long long bxy = (long long)((g.nx + 63) / 64) * ((g.ny + rows - 1) / rows);
             const long long chunks = std::max<long long>(1, bxy >= slots ? 1 : slots / bxy);
@@ -199,7 +199,7 @@ static int tune_t(const lsg_operator *op, cudaStream_t s, TuneEntry *out, int *n
                 if (shape == 1 && lz == plz) best.us_default = us;  // the untuned solve runs this one
                 if (us < best.us) {
                     best.us = us;
-                    best.tile = shape == 1 ? kTilePaired : kTilePaired2;
+                    best.tile = shape == 1 ? kTilePaired : shape == 2 ? kTilePaired2 : kTilePaired3;
                     best.lz = lz;
                 }
             }
@@ -246,9 +246,9 @@ StencilLaunch rich_launch(const lsg_operator *op, const StencilLaunch &L) {
         }
     }
     StencilLaunch r = L;
-    if (e.tile == kTilePaired || e.tile == kTilePaired2) {
+    if (e.tile == kTilePaired || e.tile == kTilePaired2 || e.tile == kTilePaired3) {
         r.tile = 0;
-        r.paired = e.tile == kTilePaired ? 1 : 2;
+        r.paired = e.tile == kTilePaired ? 1 : e.tile == kTilePaired2 ? 2 : 3;
     } else {
         r.tile = e.tile;
         r.paired = 0;  // a tuned classic shape
@@ -290,7 +290,8 @@ int tune_load(const char *path, int *count) {
         double us, usd;
         if (sscanf(line, "%d %d %d %d %d %d %d %lf %lf", &dev, &dt, &nx, &ny, &nz, &tile, &lz, &us, &usd) != 9)
             continue;
-        if (tile < 0 || (tile >= kTileVariants && tile != kTilePaired && tile != kTilePaired2) || lz < 1 ||
+        if (tile < 0 || (tile >= kTileVariants && tile != kTilePaired && tile != kTilePaired2 && tile != kTilePaired3) ||
+            lz < 1 ||
             lz > nz)
             continue;
         g_tune[TuneKey{dev, dt, nx, ny, nz}] = TuneEntry{tile, lz, us, usd};
@@ -322,6 +323,11 @@ int lsg_autotune(const lsg_operator *op, int dtype, lsg_tune_info *info, void *s
             if (e.tile == lsg::kTilePaired2) {  // 32 x 4 threads, 2 rows x 2 columns each
                 by = lsg::kPair2BY;
                 ny = lsg::kPair2NY;
+                return;
+            }
+            if (e.tile == lsg::kTilePaired3) {  // 32 x 8 threads, 4 rows x 2 columns each
+                by = lsg::kPair3BY;
+                ny = lsg::kPair3NY;
                 return;
             }
             switch (e.tile) {
