@@ -551,12 +551,10 @@ struct RichPrecOp {
         return df_add2(df_split(v.a, k, bad), df_mul(df_split(v.b, k, bad), cp));
     }
     static constexpr bool STORE_DF = true;
+    // A u rounded to a double once, then the FP64 epilogue of store().
     __device__ __forceinline__ void store_df(unsigned i, float2, float2 au, const Ctr &cc, int k,
-                                             Acc<double> *) const {
-        bool nb = false;
-        x2[i] = fma(c, cc.c, cc.b);
-        r2[i] = df_to_double(df_sub(df_split(cc.a, k, nb), au), k);
-        hn[i] = c * cc.c;
+                                             Acc<double> *acc) const {
+        store(i, fma(c, cc.c, cc.b), df_to_double(au, k), cc, acc);
     }
 };
 

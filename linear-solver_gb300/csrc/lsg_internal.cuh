@@ -281,7 +281,7 @@ struct StencilLaunch {
 // registers); FP32 is bandwidth-bound (taller tile, less halo per point).
 // A block is 32 x BY threads covering 32 x (BY*NY) columns.
 template <typename T> struct TileOf;
-template <> struct TileOf<double> { static constexpr int BY = 8, NY = 2, MINB = 1; };
+template <> struct TileOf<double> { static constexpr int BY = 8, NY = 1, MINB = 2; };
 template <> struct TileOf<float> { static constexpr int BY = 4, NY = 4, MINB = 4; };
 template <> struct TileOf<cplx<double>> { static constexpr int BY = 8, NY = 1, MINB = 1; };
 template <> struct TileOf<cplx<float>> { static constexpr int BY = 8, NY = 2, MINB = 2; };
@@ -303,13 +303,12 @@ constexpr int kPair2BY = 4, kPair2NY = 2, kPair2MINB = 4;
 constexpr int kTilePaired3 = 5;
 constexpr int kPair3BY = 8, kPair3NY = 4, kPair3MINB = 1;
 template <typename T, int V> struct TileVar;
-// The default: two rows per thread (32 x 16 tile, one 256-thread block per SM
-// at ~200 registers): the double-float march is issue-bound and a taller tile
-// stages ~26% fewer halo values per point (557 vs 631 us per FP64 Richardson
-// pass at 256^3 against one row per thread).
-template <> struct TileVar<double, 0> { static constexpr int BY = 8, NY = 2, MINB = 1; };
+template <> struct TileVar<double, 0> { static constexpr int BY = 8, NY = 1, MINB = 2; };
 template <> struct TileVar<double, 1> { static constexpr int BY = 16, NY = 1, MINB = 1; };
-template <> struct TileVar<double, 2> { static constexpr int BY = 8, NY = 1, MINB = 2; };
+// two rows per thread (32 x 16 tile, one 256-thread block per SM at ~200
+// registers): ~26% fewer staged halo values per point, but half the warps to
+// cover the FP64 epilogue's latency
+template <> struct TileVar<double, 2> { static constexpr int BY = 8, NY = 2, MINB = 1; };
 template <> struct TileVar<float, 0> { static constexpr int BY = 4, NY = 4, MINB = 4; };
 template <> struct TileVar<float, 1> { static constexpr int BY = 8, NY = 2, MINB = 2; };
 template <> struct TileVar<float, 2> { static constexpr int BY = 4, NY = 2, MINB = 4; };

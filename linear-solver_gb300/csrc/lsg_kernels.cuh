@@ -74,25 +74,12 @@ struct ResidualOp {
         else if constexpr (MODE == RES_INIT) return ldg(b + i);
         else return Ctr{};
     }
-    // Double-float epilogue: r_new = b - Au and DF formed from pairs, each
-    // rounded to a double once.
+    // Double-float epilogue: A u rounded to a double once, then the FP64
+    // epilogue of store() (a few FP64 operations instead of double-float ones).
     static constexpr bool STORE_DF = DF;
     __device__ __forceinline__ void store_df(unsigned i, float2, float2 au, const Ctr &c, int k,
                                              Acc<T> *acc) const {
-        bool nb = false;
-        if constexpr (MODE == RES_INIT) {
-            const double rn = df_to_double(df_sub(df_split(c, k, nb), au), k);
-            r[i] = rn;
-            acc[0].add_prod(rn, rn);
-        } else if constexpr (MODE == RES_ANDERSON) {
-            const float2 rn = df_sub(df_split(c.a, k, nb), au);
-            const double dfv = df_to_double(df_mul(df_sub(rn, df_split(c.b, k, nb)), cfp), k);
-            const double rnd = df_to_double(rn, k);
-            df[i] = dfv;
-            hc[i] = fma(hb, dfv, c.c);
-            r[i] = rnd;
-            acc[0].add_prod(rnd, rnd);
-        }
+        store(i, T(0), (T)df_to_double(au, k), c, acc);
     }
     __device__ __forceinline__ void store(unsigned i, T u, T au, const Ctr &c, Acc<T> *acc) const {
         if constexpr (MODE == RES_APPLY) {
@@ -163,21 +150,15 @@ struct RichOp {
         dx[i] = fma(hb, dfv, u - cc.b);
         df[i] = dfv;
     }
-    // Double-float epilogue: x2 = x + c r in FP64 (the reference's update);
-    // r2 = b - Au, DF and the history column c r + hb DF (x2 - x + hb DF in
-    // exact arithmetic) from double-float pairs, each rounded to a double once.
+    // Double-float epilogue: A u rounded to a double once, then the FP64
+    // epilogue above with x2 = x + c r in FP64 (the reference's update) -- six
+    // FP64 operations on the otherwise idle FP64 pipe in place of ~150
+    // double-float instructions; rounding Au first adds 2^-53 |Au| to the
+    // sums' own ~2^-48 sum_p |w_p| |u|.
     static constexpr bool STORE_DF = DF;
     __device__ __forceinline__ void store_df(unsigned i, float2, float2 au, const Ctr &cc, int k,
-                                             Acc<T> *) const {
-        bool nb = false;
-        const float2 rd = df_split(cc.c, k, nb);
-        const float2 rn = df_sub(df_split(cc.a, k, nb), au);
-        const float2 dfv = (MODE == RICH_AAR) ? df_mul(df_sub(rn, rd), cfp) : df_sub(rd, rn);
-        const float2 dxv = df_add(df_mul(rd, cp), df_mul(dfv, hbp));
-        x2[i] = fma(c, cc.c, cc.b);
-        r2[i] = df_to_double(rn, k);
-        dx[i] = df_to_double(dxv, k);
-        df[i] = df_to_double(dfv, k);
+                                             Acc<T> *acc) const {
+        store(i, fma(c, cc.c, cc.b), (T)df_to_double(au, k), cc, acc);
     }
 };
 
@@ -392,15 +373,11 @@ struct IrResidualOp {
         r32[i] = (T32)rn;
         acc[0].add_prod(rn, rn);
     }
+    // A u rounded to a double once, then the FP64 epilogue of store().
     static constexpr bool STORE_DF = DF;
     __device__ __forceinline__ void store_df(unsigned i, float2, float2 au, const Ctr &bb, int k,
                                              Acc<T64> *acc) const {
-        if constexpr (DF) {
-            bool nb = false;
-            const double rn = df_to_double(df_sub(df_split(bb, k, nb), au), k);
-            r32[i] = (T32)rn;
-            acc[0].add_prod(rn, rn);
-        }
+        if constexpr (DF) store(i, T64(0), (T64)df_to_double(au, k), bb, acc);
     }
 };
 
