@@ -548,7 +548,7 @@ struct RichPrecOp {
     }
     static constexpr bool VALUE_DF = true;
     __device__ __forceinline__ float2 value_df(const Raw &v, int k, bool &bad) const {
-        return df_add2(df_split(v.a, k, bad), df_mul(df_split(v.b, k, bad), cp));
+        return df_split(fma(c, v.b, v.a), k, bad);  // u = x + omega f in FP64, split once
     }
     static constexpr bool STORE_DF = true;
     // A u rounded to a double once, then the FP64 epilogue of store().

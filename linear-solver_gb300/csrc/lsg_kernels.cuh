@@ -134,10 +134,11 @@ struct RichOp {
     }
     __device__ __forceinline__ Raw fetch(unsigned i) const { return Raw{ldg(x + i), ldg(r + i)}; }
     __device__ __forceinline__ T value(const Raw &v) const { return fma(c, v.b, v.a); }
-    // u = x + c r from the split operands (double-float march; no FP64 operation)
+    // u = x + c r formed in FP64 (as the reference updates x, on the FP64 pipe
+    // the double-float sums leave idle) and split once into a float pair
     static constexpr bool VALUE_DF = DF;
     __device__ __forceinline__ float2 value_df(const Raw &v, int k, bool &bad) const {
-        return df_add2(df_split(v.a, k, bad), df_mul(df_split(v.b, k, bad), cp));
+        return df_split(fma(c, v.b, v.a), k, bad);
     }
     __device__ __forceinline__ Ctr fetch_center(unsigned i) const {
         return Ctr{ldg(b + i), ldg(x + i), ldg(r + i)};
@@ -335,11 +336,12 @@ struct CgDirOp {
     }
     __device__ __forceinline__ Raw fetch(unsigned i) const { return Raw{ldg(r + i), ldg(d_old + i)}; }
     __device__ __forceinline__ T value(const Raw &v) const { return fma(beta, v.b, cf * v.a); }
-    // d = cf r + beta d_old from the split operands (double-float march); the
-    // stored direction is the pair the sums used, rounded once
+    // d = cf r + beta d_old formed in FP64 (on the FP64 pipe the double-float
+    // sums leave idle) and split once into the pair the sums use; the stored
+    // direction is that pair, rounded once
     static constexpr bool VALUE_DF = DF;
     __device__ __forceinline__ float2 value_df(const Raw &v, int k, bool &bad) const {
-        return df_add2(df_mul(df_split(v.a, k, bad), cfp), df_mul(df_split(v.b, k, bad), betap));
+        return df_split(value(v), k, bad);
     }
     __device__ __forceinline__ Ctr fetch_center(unsigned) const { return Ctr{}; }
     __device__ __forceinline__ void store(unsigned i, T u, T au, const Ctr &, Acc<T> *acc) const {
