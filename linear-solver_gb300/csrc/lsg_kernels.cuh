@@ -617,7 +617,7 @@ int Kernels<T>::stencil_blocks_per_sm(int var) {
 // double-float accumulator (lsg_accum.cuh); FP64 vectors: FP64 FMAs.
 // True when every pointer is 16-byte aligned (nullptr counts as aligned).
 template <typename... P>
-inline bool aligned16(const P *...p) {
+__host__ __device__ inline bool aligned16(const P *...p) {
     return ((((uintptr_t)p) | ... | (uintptr_t)0) & 15u) == 0;
 }
 
@@ -1494,6 +1494,38 @@ __device__ __forceinline__ void gram_c_block(const cplx<R> *__restrict__ df,
 #pragma unroll
     for (int k = 0; k < NV; k++) acc[k].zero();
     const long long stride = nblk * blockDim.x;
+    if constexpr (std::is_same<R, float>::value) {
+        // complex64: two points per 16-byte load; the real and imaginary parts
+        // of conj(a) b over both points are summed in FP32 (four products each)
+        // and then folded into the double-float accumulators, as the real Gram
+        // folds its four-point dot products
+        if (n % 2 == 0 && aligned16(df, r)) {
+            const long long nv = n / 2;
+            const float4 *dv = reinterpret_cast<const float4 *>(df);
+            const float4 *rvv = reinterpret_cast<const float4 *>(r);
+            for (long long i = blk * blockDim.x + threadIdx.x; i < nv; i += stride) {
+                float4 f[M];
+#pragma unroll
+                for (int j = 0; j < M; j++) f[j] = ldg(dv + j * nv + i);
+                const float4 rv = ldg(rvv + i);
+                auto cdot = [](const float4 &a, const float4 &b, Acc<cplx<float>> &c) {
+                    const float re = fmaf(a.w, b.w, fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)));
+                    const float im = fmaf(-a.w, b.z, fmaf(a.z, b.w, fmaf(-a.y, b.x, a.x * b.y)));
+                    c.re.add(re);
+                    c.im.add(im);
+                };
+                int k = 0;
+#pragma unroll
+                for (int j = 0; j < M; j++)
+#pragma unroll
+                    for (int a = 0; a <= j; a++) { cdot(f[a], f[j], acc[k]); k++; }
+#pragma unroll
+                for (int j = 0; j < M; j++) cdot(f[j], rv, acc[NP + j]);
+            }
+            block_reduce_store<NV>(acc, red, out);
+            return;
+        }
+    }
     for (long long i = blk * blockDim.x + threadIdx.x; i < n; i += stride) {
         cplx<R> f[M];
 #pragma unroll
