@@ -244,3 +244,35 @@ def test_zero_iterations(lsg):
     assert r["iters"] == 0 and r["status"] == 1
     x, r = lsg.cg(lsg.Operator(8), b - b.mean(), max_iter=0)
     assert r["iters"] == 0
+
+
+@pytest.mark.parametrize("dtype_name", ["float64", "float32"])
+def test_unaligned_views(lsg, dtype_name):
+    """x and b as views at a one-element offset (not 16-byte aligned): the
+    16-byte load paths stand aside (the scalar paths compute the same sums),
+    so the solve matches the one on aligned copies."""
+    import torch
+    dt = getattr(torch, dtype_name)
+    n = 24
+    rng = np.random.default_rng(12)
+    b = rng.uniform(-0.5, 0.5, (n, n, n))
+    b -= b.mean()
+    op = lsg.Operator(n, a=-float(n * n), sigma=1.0)
+    tol = 1e-9 if dt == torch.float64 else 1e-5
+    bb = torch.from_numpy(b).to(device="cuda", dtype=dt)
+    x_ref, r_ref = lsg.aar(op, bb, tol=tol)
+    store_b = torch.empty(n ** 3 + 1, dtype=dt, device="cuda")
+    store_x = torch.zeros(n ** 3 + 1, dtype=dt, device="cuda")
+    bv = store_b[1:].view(n, n, n)
+    bv.copy_(bb)
+    xv = store_x[1:].view(n, n, n)
+    assert bv.data_ptr() % 16 != 0 and xv.data_ptr() % 16 != 0
+    import ctypes as C
+    res = lsg._Result()
+    prm = lsg._params(tol=tol)
+    rc = lsg.lib().lsg_aar(C.byref(op._s), C.byref(prm), lsg._dtype_code(bv), C.c_void_p(xv.data_ptr()),
+                           C.c_void_p(bv.data_ptr()), C.byref(res), lsg._stream_ptr())
+    torch.cuda.synchronize()
+    r = lsg._result(res)
+    assert rc == 0 and r["iters"] == r_ref["iters"]
+    assert ((xv - x_ref).norm() / x_ref.norm()).item() <= (1e-12 if dt == torch.float64 else 1e-6)
