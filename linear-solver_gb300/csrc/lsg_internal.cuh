@@ -44,6 +44,7 @@ struct DevCtrl {
     int df_range;     // FP64 double-float stencil: a value beyond the float range was split
     double bmean[2];  // mixed solves (outer block): mean of b (re, im)
     double shift[2];  // mixed solves (outer block): constant added to x64 by the last deflation
+    unsigned fin_ticket;  // Gram finalize: blocks done summing (0 between launches)
     double s[LSG_MAX_M];  // m x m solve output
 };
 
@@ -185,8 +186,8 @@ DevCtrl ctrl_init(double tol, int stall_limit);
 
 // ----------------------------------------------------------------------------
 // Reductions.  Every reducing kernel writes one partial per block (FP64) to a
-// partials array; a single-block finalize kernel sums them in a fixed order,
-// so results are run-to-run deterministic.
+// partials array; a finalize kernel sums them in a fixed order, so results
+// are run-to-run deterministic.
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -527,14 +528,15 @@ enum NormFinal {
 cudaError_t finalize_norm(const double *partials, int nparts, DevCtrl *ctrl, int mode,
                           double tol, int iter, cudaStream_t s, int width = 1);
 // Sums Gram partials, assembles G (m x m) and h (m), solves s = pinv(G) h with
-// the reference semantics into ctrl->s.  hscale multiplies h.
-cudaError_t finalize_gram_solve(const double *partials, int nparts, int kind, int m,
-                                double hscale, DevCtrl *ctrl, cudaStream_t s);
+// the reference semantics into ctrl->s.  hscale multiplies h.  Row 0 of the
+// partials is overwritten with the totals.
+cudaError_t finalize_gram_solve(double *partials, int nparts, int kind, int m, double hscale, DevCtrl *ctrl,
+                                cudaStream_t s);
 // Complex Hermitian variant: G(i,j) = DF_i^H DF_j, h = hscale * DF^H r; solved
 // as its real 2m x 2m representation with zgelsd's cutoff (eps * sigma_max,
 // PETSC_COMPLEX/AAR_Complex.c:239); ctrl->s holds (re, im) pairs, m <= 16.
-cudaError_t finalize_gram_solve_c(const double *partials, int nparts, int m, cplx<double> hscale,
-                                  DevCtrl *ctrl, cudaStream_t s);
+cudaError_t finalize_gram_solve_c(double *partials, int nparts, int m, cplx<double> hscale, DevCtrl *ctrl,
+                                  cudaStream_t s);
 // CG scalars: mode 0: alpha = delta / sum(d.q).  mode 1: delta_new = cf*sum(r.r),
 // relres = sqrt(sum r.r), beta = delta_new/delta_old, convergence test.
 cudaError_t finalize_cg(const double *partials, int nparts, DevCtrl *ctrl, int mode, double cf,

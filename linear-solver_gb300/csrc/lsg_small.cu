@@ -1,5 +1,5 @@
-// lsg_small.cu — single-block kernels that turn per-block partial sums into
-// the scalars a solve needs, and the m x m pseudo-inverse solve.
+// lsg_small.cu — the kernels that turn per-block partial sums into the
+// scalars a solve needs, and the m x m pseudo-inverse solve.
 //
 //   finalize_norm        ||v|| from partials; convergence test     tools.c:18-28, AAR.c:91,123
 //   finalize_gram_solve  Gram assembly + s = pinv(G) h             AAR.c:212-223; PGR.c:206-217;
@@ -24,6 +24,7 @@
 namespace lsg {
 
 constexpr int kFinThreads = 256;
+constexpr int kFinWarps = kFinThreads / 32;
 constexpr int kMaxSweeps = 60;
 constexpr double kPinvEps = 2.22044605e-16;
 
@@ -304,21 +305,26 @@ __device__ bool warp_ldl_solve(const double *G, const double *h, double *x, int 
     trg *= sc;
     for (int k = lane; k < m * m; k += 32) Ls[k] = 0.0;
     __syncwarp();
-    // LDL^T over the active indices: lane r holds row r of L.
+    // LDL^T over the active indices: lane r holds row r of L, and Wi (free
+    // until the bound below) row r of -L(r, t) d_t, formed once per entry.
     double rinv = 0.0;  // lane j: 1 / d_j
     for (int j = 0; j < m; j++) {
         if (!((amask >> j) & 1u)) continue;
         double acc = 0.0;
-        if (lane < m) {
+        if (lane < m && act) {
             acc = G[lane * m + j] * sc;
             for (int t = 0; t < j; t++)
-                if ((amask >> t) & 1u) acc = fma(-Ls[lane * m + t] * dd[t], Ls[j * m + t], acc);
+                if ((amask >> t) & 1u) acc = fma(Wi[lane * m + t], Ls[j * m + t], acc);
         }
         const double dj = __shfl_sync(full, acc, j);
         if (!(dj > 0.0)) return false;
         const double inv = rcp_newton(dj);
         if (lane == j) { dd[j] = dj; Ls[j * m + j] = 1.0; rinv = inv; }
-        if (lane < m && lane > j && act) Ls[lane * m + j] = acc * inv;
+        if (lane < m && lane > j && act) {
+            const double l = acc * inv;
+            Ls[lane * m + j] = l;
+            Wi[lane * m + j] = -l * dj;
+        }
         __syncwarp();
     }
     // kappa bound: trace(G^-1) = sum_k (1/d_k) ||row k of L^-1||^2.  Lane c
@@ -423,19 +429,14 @@ __device__ __forceinline__ void sum_gram_partials(const double *__restrict__ par
     }
 }
 
-__device__ void gram_solve_body(const double *partials, int nparts, int kind, int m, double hscale,
-                                DevCtrl *ctrl) {
-    __shared__ double vals[LSG_MAX_M * LSG_MAX_M + LSG_MAX_M];
+// Assembles G (m x m) and h from the summed values and solves s = pinv(G) h
+// into ctrl->s (one warp); bad: a value was not finite.
+__device__ void gram_solve_tail(const double *vals, int bad, int kind, int m, double hscale, DevCtrl *ctrl) {
     __shared__ double G[LSG_MAX_M * LSG_MAX_M], V[LSG_MAX_M * LSG_MAX_M];
     __shared__ double Gs[LSG_MAX_M * LSG_MAX_M], Vs[64];
     __shared__ double h[LSG_MAX_M], s[LSG_MAX_M], dd[LSG_MAX_M];
-    __shared__ int bad;
     const int nv = gram_values(kind, m);
     const int np = nv - m;
-    if (threadIdx.x == 0) bad = 0;
-    __syncthreads();
-    sum_gram_partials(partials, nparts, nv, vals, &bad);
-    __syncthreads();
     if (threadIdx.x < 32) {
         // Assemble G (row-major) and h.
         if (kind == GRAM_SYM) {
@@ -470,31 +471,91 @@ __device__ void gram_solve_body(const double *partials, int nparts, int kind, in
     }
 }
 
-__global__ void finalize_gram_solve_kernel(const double *partials, int nparts, int kind, int m,
-                                           double hscale, DevCtrl *ctrl) {
+__device__ void gram_solve_body(const double *partials, int nparts, int kind, int m, double hscale,
+                                DevCtrl *ctrl) {
+    __shared__ double vals[LSG_MAX_M * LSG_MAX_M + LSG_MAX_M];
+    __shared__ int bad;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    sum_gram_partials(partials, nparts, gram_values(kind, m), vals, &bad);
+    __syncthreads();
+    gram_solve_tail(vals, bad, kind, m, hscale, ctrl);
+}
+
+// The Gram sums of a single solve spread over ceil(nv / 8) blocks: the FP64
+// pipe issues one warp instruction per ~64 cycles on each SM partition, so
+// one block summing all nv values over the block partials is slower than the
+// small solve after it.  Warp w of block b sums value v = 8 b + w over rows
+// lane, lane + 32, ... (four loads in flight) and then across the warp, the
+// order of sum_gram_partials, so the totals equal the one-block totals bit for
+// bit.  Lane 0 stores the total in row 0 of its column, which no other warp
+// reads.  Returns true in the last block to finish: a ticket in the control
+// block, which that block resets to 0 for the next launch.
+__device__ bool sum_gram_spread(double *partials, int nparts, int nv, DevCtrl *ctrl) {
+    __shared__ int last;
+    const int lane = threadIdx.x & 31;
+    const int v = blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
+    if (v < nv) {
+        const double *col = partials + v;
+        double t = 0.0;
+        int k = lane;
+        for (; k + 96 < nparts; k += 128) {
+            const double a0 = __ldcg(col + (long long)k * nv), a1 = __ldcg(col + (long long)(k + 32) * nv);
+            const double a2 = __ldcg(col + (long long)(k + 64) * nv), a3 = __ldcg(col + (long long)(k + 96) * nv);
+            t += a0;
+            t += a1;
+            t += a2;
+            t += a3;
+        }
+        for (; k < nparts; k += 32) t += __ldcg(col + (long long)k * nv);
+        t = warp_sum(t);
+        if (lane == 0) __stcg(partials + v, t);
+    }
+    __threadfence();  // the totals are visible device-wide before the ticket
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned ticket = atomicAdd(&ctrl->fin_ticket, 1u);
+        last = ticket == gridDim.x - 1;
+        if (last) ctrl->fin_ticket = 0;
+    }
+    __syncthreads();
+    return last != 0;
+}
+
+// The last block's read of the totals (through L2: other blocks stored them).
+__device__ void load_gram_totals(const double *partials, int nv, double *vals, int *bad) {
+    if (threadIdx.x == 0) *bad = 0;
+    __syncthreads();
+    for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+        const double t = __ldcg(partials + v);
+        vals[v] = t;
+        if (!isfinite(t)) *bad = 1;
+    }
+    __syncthreads();
+}
+
+__global__ void finalize_gram_solve_kernel(double *partials, int nparts, int kind, int m, double hscale,
+                                           DevCtrl *ctrl) {
+    __shared__ double vals[LSG_MAX_M * LSG_MAX_M + LSG_MAX_M];
+    __shared__ int bad;
     if (ctrl_done(ctrl)) return;
-    gram_solve_body(partials, nparts, kind, m, hscale, ctrl);
+    const int nv = gram_values(kind, m);
+    if (!sum_gram_spread(partials, nparts, nv, ctrl)) return;
+    load_gram_totals(partials, nv, vals, &bad);
+    gram_solve_tail(vals, bad, kind, m, hscale, ctrl);
 }
 
 // Complex Hermitian Gram: sums the (re, im) partials, builds the real 2m x 2m
 // representation [[A, -B], [B, A]] of G = A + iB (same singular values, each
 // twice) and right-hand side [Re h; Im h], and solves it with zgelsd's cutoff
 // sigma < eps * sigma_max (PETSC_COMPLEX/AAR_Complex.c:239, rcond = -1).
-__device__ void gram_solve_c_body(const double *partials, int nparts, int m, double hre, double him,
-                                  DevCtrl *ctrl) {
+__device__ void gram_solve_c_tail(const double *vals, int bad, int m, double hre, double him, DevCtrl *ctrl) {
     constexpr int M2MAX = LSG_MAX_M;
-    __shared__ double vals[2 * (LSG_MAX_M * LSG_MAX_M + LSG_MAX_M)];
     __shared__ double G[M2MAX * M2MAX], V[M2MAX * M2MAX], W[M2MAX * M2MAX];
     __shared__ double Gs[64], Vs[64];
     __shared__ double h[M2MAX], s[M2MAX], dd[M2MAX];
-    __shared__ int bad;
     const int np = (m * (m + 1)) / 2;
-    const int nvr = 2 * (np + m);  // reals per block partial
     const int m2 = 2 * m;
-    if (threadIdx.x == 0) bad = 0;
-    __syncthreads();
-    sum_gram_partials(partials, nparts, nvr, vals, &bad);
-    __syncthreads();
     if (threadIdx.x < 32) {
         for (int k = threadIdx.x; k < np; k += 32) {
             int j = 0;
@@ -534,10 +595,28 @@ __device__ void gram_solve_c_body(const double *partials, int nparts, int m, dou
     }
 }
 
-__global__ void finalize_gram_solve_c_kernel(const double *partials, int nparts, int m, double hre,
-                                             double him, DevCtrl *ctrl) {
+__device__ void gram_solve_c_body(const double *partials, int nparts, int m, double hre, double him,
+                                  DevCtrl *ctrl) {
+    __shared__ double vals[2 * (LSG_MAX_M * LSG_MAX_M + LSG_MAX_M)];
+    __shared__ int bad;
+    const int nvr = m * (m + 1) + 2 * m;  // reals per block partial: 2 (m (m + 1) / 2 + m)
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    sum_gram_partials(partials, nparts, nvr, vals, &bad);
+    __syncthreads();
+    gram_solve_c_tail(vals, bad, m, hre, him, ctrl);
+}
+
+// One solve's complex Gram, its sums spread as in finalize_gram_solve_kernel.
+__global__ void finalize_gram_solve_c_kernel(double *partials, int nparts, int m, double hre, double him,
+                                             DevCtrl *ctrl) {
+    __shared__ double vals[2 * (LSG_MAX_M * LSG_MAX_M + LSG_MAX_M)];
+    __shared__ int bad;
     if (ctrl_done(ctrl)) return;
-    gram_solve_c_body(partials, nparts, m, hre, him, ctrl);
+    const int nvr = m * (m + 1) + 2 * m;
+    if (!sum_gram_spread(partials, nparts, nvr, ctrl)) return;
+    load_gram_totals(partials, nvr, vals, &bad);
+    gram_solve_c_tail(vals, bad, m, hre, him, ctrl);
 }
 
 // ---------------------------------------------------------------- batched finalize
@@ -681,16 +760,18 @@ cudaError_t finalize_norm(const double *partials, int nparts, DevCtrl *ctrl, int
     return cudaGetLastError();
 }
 
-cudaError_t finalize_gram_solve(const double *partials, int nparts, int kind, int m, double hscale,
-                                DevCtrl *ctrl, cudaStream_t s) {
-    finalize_gram_solve_kernel<<<1, kFinThreads, 0, s>>>(partials, nparts, kind, m, hscale, ctrl);
+cudaError_t finalize_gram_solve(double *partials, int nparts, int kind, int m, double hscale, DevCtrl *ctrl,
+                                cudaStream_t s) {
+    const int blocks = (gram_values(kind, m) + kFinWarps - 1) / kFinWarps;
+    finalize_gram_solve_kernel<<<blocks, kFinThreads, 0, s>>>(partials, nparts, kind, m, hscale, ctrl);
     return cudaGetLastError();
 }
 
-cudaError_t finalize_gram_solve_c(const double *partials, int nparts, int m, cplx<double> hscale,
-                                  DevCtrl *ctrl, cudaStream_t s) {
+cudaError_t finalize_gram_solve_c(double *partials, int nparts, int m, cplx<double> hscale, DevCtrl *ctrl,
+                                  cudaStream_t s) {
     if (2 * m > LSG_MAX_M) return cudaErrorInvalidValue;
-    finalize_gram_solve_c_kernel<<<1, kFinThreads, 0, s>>>(partials, nparts, m, hscale.x, hscale.y, ctrl);
+    const int blocks = (m * (m + 1) + 2 * m + kFinWarps - 1) / kFinWarps;
+    finalize_gram_solve_c_kernel<<<blocks, kFinThreads, 0, s>>>(partials, nparts, m, hscale.x, hscale.y, ctrl);
     return cudaGetLastError();
 }
 
