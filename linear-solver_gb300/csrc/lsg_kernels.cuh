@@ -827,7 +827,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *b, unsigne
 // block rebuilds DF_t = (r_t+1 - r_t) cf (stored columns, rw.dfmem, straight
 // from df), accumulates in time order and writes each sum at its column-order
 // place, so the partials equal gram()'s over the same columns bit for bit.
-template <int M, bool RING = false>
+// FULL (RING): every column valid and none stored (rw.valid all ones,
+// rw.dfmem 0, the steady state): the per-column tests, which cost ~10% of
+// the pass at 256^3, are compiled out.
+template <int M, bool RING = false, bool FULL = false>
 __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const float *__restrict__ df,
                                                                      const float *__restrict__ r, long long n,
                                                                      double *partials, DevCtrl *ctrl,
@@ -908,7 +911,7 @@ __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const floa
 #pragma unroll
                     for (int t = 0; t < M; t++) {
                         float4 d;
-                        if ((rw.dfmem >> t) & 1u) {
+                        if (!FULL && ((rw.dfmem >> t) & 1u)) {
                             d = ldg(reinterpret_cast<const float4 *>(df + (long long)((rw.s0 + t) % M) * n + off) + tid);
                         } else {
                             d.x = (u[t + 1].x - u[t].x) * cf;
@@ -916,7 +919,7 @@ __global__ void __launch_bounds__(kReduceThreads, 2) gram_bulk_kernel(const floa
                             d.z = (u[t + 1].z - u[t].z) * cf;
                             d.w = (u[t + 1].w - u[t].w) * cf;
                         }
-                        if (!((rw.valid >> t) & 1u)) d = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (!FULL && !((rw.valid >> t) & 1u)) d = make_float4(0.f, 0.f, 0.f, 0.f);
                         f[t] = d;
                     }
                     rv = u[M];
@@ -1748,15 +1751,16 @@ cudaError_t Kernels<T>::ring_gram(int m, const RingWindow &rw, const T *ring, lo
             return cudaErrorInvalidValue;
         const unsigned extra_tx = gram_fault_tx();
         const long long wait_cycles = gram_wait_cycles();
+        const bool full = rw.valid == (1u << m) - 1u && rw.dfmem == 0u;
         switch (m) {
 #define LSG_GRAM_RING(MM)                                                                                   \
     case MM: {                                                                                              \
-        const cudaError_t ea = cudaFuncSetAttribute(gram_bulk_kernel<MM, true>,                             \
-                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,            \
+        auto *kern = full ? gram_bulk_kernel<MM, true, true> : gram_bulk_kernel<MM, true, false>;           \
+        const cudaError_t ea = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
                                                     (int)gram_bulk_smem<MM>());                             \
         if (ea != cudaSuccess) return ea;                                                                   \
-        gram_bulk_kernel<MM, true><<<blocks, kReduceThreads, gram_bulk_smem<MM>(), s>>>(                    \
-            df, nullptr, n, partials, ctrl, extra_tx, wait_cycles, ring, ss, rw, (float)cf);                \
+        kern<<<blocks, kReduceThreads, gram_bulk_smem<MM>(), s>>>(df, nullptr, n, partials, ctrl, extra_tx, \
+                                                                  wait_cycles, ring, ss, rw, (float)cf);    \
         return cudaGetLastError();                                                                          \
     }
             LSG_GRAM_RING(1) LSG_GRAM_RING(2) LSG_GRAM_RING(3) LSG_GRAM_RING(4)
