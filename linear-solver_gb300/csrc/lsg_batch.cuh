@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(32 * BY, MINB) batch_stencil_kernel(const BIns
     const int lb = blockIdx.x - C.sblk0;
     const int t = lb / I.tx;
     const Weights<TS> w = Pass::weights(I);
-    if constexpr (DFM && std::is_same<TS, double>::value) {
+    if constexpr (DFM && IsDfMarch<TS>::value) {
         stencil_march_df<RQ, BY, NY, GENERIC>(I.g, w, I.lz, op, smem[0], smem[1], lb - t * I.tx, t % I.ty,
                                               t / I.ty, lb);
     } else {

@@ -102,8 +102,10 @@ struct Weights {
     T w[LSG_MAX_RADIUS + 1];
     int radius;
     // FP64 weights as three floats w = w1 + w2 + w3 (exactly: 72 >= 53 bits)
-    // for the double-float march (zero for the other vector types)
+    // for the double-float march (complex128: the real parts; zero for the
+    // other vector types)
     float wf[3 * (LSG_MAX_RADIUS + 1)];
+    float wfi[3];  // complex128: the imaginary part of w[0] (the shift's), three floats
 };
 
 // Three floats whose sum is exactly the double w (each the float nearest the
@@ -126,6 +128,10 @@ inline Weights<T> make_weights(const lsg_operator *op) {
     if constexpr (IsCplx<T>::value) {
         w.w[0] = T(op->a * 3.0 * op->coeff[0] + op->sigma, op->sigma_im);
         for (int p = 1; p <= op->radius; p++) w.w[p] = T(op->a * op->coeff[p], 0.0);
+        if constexpr (std::is_same<T, cplx<double>>::value) {
+            for (int p = 0; p <= op->radius; p++) split3(w.w[p].x, w.wf + 3 * p);
+            split3(w.w[0].y, w.wfi);
+        }
     } else {
         w.w[0] = (T)(op->a * 3.0 * op->coeff[0] + op->sigma);
         for (int p = 1; p <= op->radius; p++) w.w[p] = (T)(op->a * op->coeff[p]);
@@ -138,8 +144,12 @@ inline Weights<T> make_weights(const lsg_operator *op) {
 // Re-derives the three-float weights after w.w changed.
 template <typename T>
 inline void refresh_df_weights(Weights<T> &w) {
-    if constexpr (std::is_same<T, double>::value)
+    if constexpr (std::is_same<T, double>::value) {
         for (int p = 0; p <= LSG_MAX_RADIUS; p++) split3(w.w[p], w.wf + 3 * p);
+    } else if constexpr (std::is_same<T, cplx<double>>::value) {
+        for (int p = 0; p <= LSG_MAX_RADIUS; p++) split3(w.w[p].x, w.wf + 3 * p);
+        split3(w.w[0].y, w.wfi);
+    }
 }
 
 // Jacobi factor cf = 1 / diag (or 1 without preconditioning), in the

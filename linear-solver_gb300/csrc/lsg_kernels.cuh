@@ -356,7 +356,7 @@ struct CgDirOp {
 template <typename T64, typename T32>
 struct IrResidualOp {
     static constexpr int NACC = 1;
-    static constexpr bool DF = std::is_same<T64, double>::value;
+    static constexpr bool DF = IsDfMarch<T64>::value;  // FP64 and complex128
     using Raw = T64;
     using Ctr = T64;  // b
     const T64 *x;
@@ -375,11 +375,11 @@ struct IrResidualOp {
         r32[i] = (T32)rn;
         acc[0].add_prod(rn, rn);
     }
-    // A u rounded to a double once, then the FP64 epilogue of store().
+    // A u rounded to a double (each part) once, then the FP64 epilogue of store().
     static constexpr bool STORE_DF = DF;
-    __device__ __forceinline__ void store_df(unsigned i, float2, float2 au, const Ctr &bb, int k,
-                                             Acc<T64> *acc) const {
-        if constexpr (DF) store(i, T64(0), (T64)df_to_double(au, k), bb, acc);
+    template <class V>
+    __device__ __forceinline__ void store_df(unsigned i, V, V au, const Ctr &bb, int k, Acc<T64> *acc) const {
+        if constexpr (DF) store(i, T64(0), DfMarch<T64>::to_double(au, k), bb, acc);
     }
 };
 

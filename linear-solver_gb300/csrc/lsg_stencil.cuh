@@ -282,10 +282,62 @@ template <class Op, class = void> struct HasValueDf { static constexpr bool valu
 template <class Op>
 struct HasValueDf<Op, std::void_t<decltype(Op::VALUE_DF)>> { static constexpr bool value = Op::VALUE_DF; };
 
-template <class Op, class Raw>
-__device__ __forceinline__ float2 df_value(const Op &op, const Raw &v, int k, bool &bad) {
+// The value the march carries: a (hi, lo) pair for FP64 vectors, a pair per
+// part for complex128.  The weights are real but for the centre's, which
+// carries the complex shift (w.wfi).  The FP64 steps are the float operations
+// of the real march; the complex ones apply them to each part.
+__device__ __forceinline__ float2 df_mul3(float2 c, const float *w) {  // c (w[0] + w[1] + w[2])
+    float2 au;
+    au.x = __fmul_rn(c.x, w[0]);
+    au.y = __fmaf_rn(c.x, w[0], -au.x);
+    au.y = __fmaf_rn(c.x, w[1], au.y);
+    au.y = __fmaf_rn(c.y, w[0], au.y);
+    au.y = __fmaf_rn(c.x, w[2], au.y);
+    return au;
+}
+
+struct DfCplx { float2 re, im; };
+
+template <typename TS> struct DfMarch;
+template <> struct DfMarch<double> {
+    using V = float2;
+    __device__ static __forceinline__ V split(double u, int k, bool &bad) { return df_split(u, k, bad); }
+    __device__ static __forceinline__ V add(V a, V b) { return df_add2(a, b); }
+    __device__ static __forceinline__ V centre(V c, const Weights<double> &w) { return df_mul3(c, w.wf); }
+    __device__ static __forceinline__ void fma_acc(V &au, V s, const float *w3) {
+        df_fma_acc(au, s.x, s.y, w3[0], w3[1], w3[2]);
+    }
+    __device__ static __forceinline__ double to_double(V v, int k) { return df_to_double(v, k); }
+};
+template <> struct DfMarch<cplx<double>> {
+    using V = DfCplx;
+    __device__ static __forceinline__ V split(cplx<double> u, int k, bool &bad) {
+        return V{df_split(u.x, k, bad), df_split(u.y, k, bad)};
+    }
+    __device__ static __forceinline__ V add(V a, V b) { return V{df_add2(a.re, b.re), df_add2(a.im, b.im)}; }
+    // (c.re + i c.im)(w0 + i w0i): Re = c.re w0 - c.im w0i, Im = c.im w0 + c.re w0i
+    __device__ static __forceinline__ V centre(V c, const Weights<cplx<double>> &w) {
+        V au{df_mul3(c.re, w.wf), df_mul3(c.im, w.wf)};
+        df_fma_acc(au.re, -c.im.x, -c.im.y, w.wfi[0], w.wfi[1], w.wfi[2]);
+        df_fma_acc(au.im, c.re.x, c.re.y, w.wfi[0], w.wfi[1], w.wfi[2]);
+        return au;
+    }
+    __device__ static __forceinline__ void fma_acc(V &au, V s, const float *w3) {
+        df_fma_acc(au.re, s.re.x, s.re.y, w3[0], w3[1], w3[2]);
+        df_fma_acc(au.im, s.im.x, s.im.y, w3[0], w3[1], w3[2]);
+    }
+    __device__ static __forceinline__ cplx<double> to_double(V v, int k) {
+        return cplx<double>(df_to_double(v.re, k), df_to_double(v.im, k));
+    }
+};
+template <typename TS> struct IsDfMarch { static constexpr bool value = false; };
+template <> struct IsDfMarch<double> { static constexpr bool value = true; };
+template <> struct IsDfMarch<cplx<double>> { static constexpr bool value = true; };
+
+template <typename TS, class Op, class Raw>
+__device__ __forceinline__ typename DfMarch<TS>::V df_value(const Op &op, const Raw &v, int k, bool &bad) {
     if constexpr (HasValueDf<Op>::value) return op.value_df(v, k, bad);
-    else return df_split(op.value(v), k, bad);
+    else return DfMarch<TS>::split(op.value(v), k, bad);
 }
 
 // STORE_DF: the functor's epilogue takes the centre u and Au as pairs scaled
@@ -312,12 +364,15 @@ __device__ __forceinline__ V from_bits(const Bits<V> &b) {
     return v;
 }
 
-template <int RQ, int BY, int NY, bool GENERIC, class Op>
-__device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<double> &w, int lz, Op &op,
-                                                 double *smem0d, double *smem1d, int bx, int by, int bz,
+template <int RQ, int BY, int NY, bool GENERIC, class Op, typename TS>
+__device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<TS> &w, int lz, Op &op,
+                                                 TS *smem0d, TS *smem1d, int bx, int by, int bz,
                                                  long long blk) {
     using Raw = typename Op::Raw;
     using Ctr = typename Op::Ctr;
+    using DM = DfMarch<TS>;
+    using V = typename DM::V;
+    static_assert(sizeof(V) == sizeof(TS), "a staged value keeps the vector type's size");
     constexpr int TX = 32;
     constexpr int TY = BY * NY;
     constexpr int FX = TX + 2 * RQ;
@@ -328,8 +383,8 @@ __device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<do
     constexpr int FY = TY + 2 * RQ;
     const unsigned long long gn = (unsigned long long)g.n;
     (void)gn;
-    float2 *const smem0 = reinterpret_cast<float2 *>(smem0d);
-    float2 *const smem1 = reinterpret_cast<float2 *>(smem1d);
+    V *const smem0 = reinterpret_cast<V *>(smem0d);
+    V *const smem1 = reinterpret_cast<V *>(smem1d);
 
     const int radius = GENERIC ? w.radius : RQ;
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -373,19 +428,19 @@ __device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<do
         }
     }
 
-    Acc<double> acc[Op::NACC > 0 ? Op::NACC : 1];
+    Acc<TS> acc[Op::NACC > 0 ? Op::NACC : 1];
 #pragma unroll
     for (int a = 0; a < (Op::NACC > 0 ? Op::NACC : 1); a++) acc[a].zero();
 
     // ring: q[k][j] holds plane z - RQ + j at the step of plane z
-    float2 q[NY][Q];
+    V q[NY][Q];
     unsigned zl = (unsigned)wrap_index(z0 - RQ, g.nz);
     const unsigned nxy = (unsigned)g.nxy, nz = (unsigned)g.nz;
 #pragma unroll
     for (int s = 0; s < 2 * RQ; s++) {
         const unsigned base = zl * nxy;
 #pragma unroll
-        for (int k = 0; k < NY; k++) q[k][s] = df_value(op, op.fetch(LSG_IX(base + col[k], gn)), ks, bad);
+        for (int k = 0; k < NY; k++) q[k][s] = df_value<TS>(op, op.fetch(LSG_IX(base + col[k], gn)), ks, bad);
         zl = (zl + 1 == nz) ? 0u : zl + 1;
     }
     Bits<Raw> qn[NY], hn[NH];
@@ -403,7 +458,7 @@ __device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<do
         zl = (zl + 1 == nz) ? 0u : zl + 1;
     }
 
-    float2 *sm = smem0;
+    V *sm = smem0;
 #pragma unroll 1
     for (int z = z0; z < z1; z++) {
         constexpr int HEAD = Q - 1;
@@ -411,12 +466,12 @@ __device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<do
         const unsigned zbase = (unsigned)z * nxy;
 #pragma unroll
         for (int k = 0; k < NY; k++) {
-            q[k][HEAD] = df_value(op, from_bits(qn[k]), ks, bad);
+            q[k][HEAD] = df_value<TS>(op, from_bits(qn[k]), ks, bad);
             sm[LSG_IX((RQ + ty * NY + k) * FX + RQ + tx, FX * FY)] = q[k][CEN];
         }
 #pragma unroll
         for (int s = 0; s < NH; s++)
-            if (hs[s] >= 0) sm[LSG_IX(hs[s], FX * FY)] = df_value(op, from_bits(hn[s]), ks, bad);
+            if (hs[s] >= 0) sm[LSG_IX(hs[s], FX * FY)] = df_value<TS>(op, from_bits(hn[s]), ks, bad);
         Bits<Ctr> cc[NY];
 #pragma unroll
         for (int k = 0; k < NY; k++) cc[k] = cn[k];
@@ -433,8 +488,8 @@ __device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<do
             zl = (zl + 1 == nz) ? 0u : zl + 1;
         }
         __syncthreads();
-        const float2 *col0 = sm + (RQ + ty * NY) * FX + RQ + tx;
-        float2 yv[NY + 2 * RQ];
+        const V *col0 = sm + (RQ + ty * NY) * FX + RQ + tx;
+        V yv[NY + 2 * RQ];
 #pragma unroll
         for (int j = 0; j < RQ; j++) {
             yv[j] = col0[(j - RQ) * FX];
@@ -444,29 +499,24 @@ __device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<do
         for (int k = 0; k < NY; k++) yv[RQ + k] = q[k][CEN];
 #pragma unroll
         for (int k = 0; k < NY; k++) {
-            const float2 *row = col0 + k * FX;
-            const float2 c = q[k][CEN];
-            float2 au;
-            au.x = __fmul_rn(c.x, w.wf[0]);
-            au.y = __fmaf_rn(c.x, w.wf[0], -au.x);
-            au.y = __fmaf_rn(c.x, w.wf[1], au.y);
-            au.y = __fmaf_rn(c.y, w.wf[0], au.y);
-            au.y = __fmaf_rn(c.x, w.wf[2], au.y);
+            const V *row = col0 + k * FX;
+            const V c = q[k][CEN];
+            V au = DM::centre(c, w);
 #pragma unroll
             for (int p = 1; p <= RQ; p++) {
                 if (GENERIC && p > radius) break;
                 // the six neighbours at distance p, summed as a tree (depth 3)
-                const float2 sx = df_add2(row[-p], row[p]);
-                const float2 sy = df_add2(yv[RQ + k - p], yv[RQ + k + p]);
-                const float2 sz = df_add2(q[k][CEN - p], q[k][CEN + p]);
-                const float2 sp = df_add2(df_add2(sx, sy), sz);
-                df_fma_acc(au, sp.x, sp.y, w.wf[3 * p], w.wf[3 * p + 1], w.wf[3 * p + 2]);
+                const V sx = DM::add(row[-p], row[p]);
+                const V sy = DM::add(yv[RQ + k - p], yv[RQ + k + p]);
+                const V sz = DM::add(q[k][CEN - p], q[k][CEN + p]);
+                const V sp = DM::add(DM::add(sx, sy), sz);
+                DM::fma_acc(au, sp, w.wf + 3 * p);
             }
             if (valid[k] && LSG_IX_OK(zbase + col[k], gn)) {
                 if constexpr (HasStoreDf<Op>::value)
                     op.store_df(zbase + col[k], c, au, from_bits(cc[k]), ks, acc);
                 else
-                    op.store(zbase + col[k], df_to_double(c, ks), df_to_double(au, ks), from_bits(cc[k]), acc);
+                    op.store(zbase + col[k], DM::to_double(c, ks), DM::to_double(au, ks), from_bits(cc[k]), acc);
             }
         }
         sm = (sm == smem0) ? smem1 : smem0;
@@ -481,8 +531,9 @@ __device__ __forceinline__ void stencil_march_df(const Geom &g, const Weights<do
         atomicOr(&const_cast<DevCtrl *>(op.ctrl)->df_range, 1);
     if (Op::NACC > 0) {
         constexpr int NA = Op::NACC > 0 ? Op::NACC : 1;
-        __shared__ double red[NA * 32];
-        block_reduce_store<NA>(acc, red, op.partials + blk * Op::NACC);
+        constexpr int W = AccWidth<TS>::value;
+        __shared__ double red[NA * W * 32];
+        block_reduce_store<NA>(acc, red, op.partials + blk * Op::NACC * W);
     }
 }
 
@@ -495,7 +546,7 @@ __global__ void __launch_bounds__(32 * BY, MINB) stencil_kernel(Geom g, Weights<
     if (op.skip()) return;
     op.init();
     const long long blk = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
-    if constexpr (DFM && std::is_same<T, double>::value) {
+    if constexpr (DFM && IsDfMarch<T>::value) {
         stencil_march_df<RQ, BY, NY, GENERIC>(g, w, lz, op, smem[0], smem[1], blockIdx.x, blockIdx.y, blockIdx.z,
                                               blk);
     } else {

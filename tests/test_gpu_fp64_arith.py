@@ -102,3 +102,50 @@ def test_tight_tolerance_uses_fp64_arithmetic(lsg, fp64_mode):
     assert r["status"] == 0 and r["relres"] <= 1e-13
     true = ((b - lsg.apply(op, x)).norm() / b.norm()).item()
     assert true <= 1.5e-13
+
+
+@pytest.mark.parametrize("n", [16, 37])
+def test_double_float_complex_residual_matches_fp64_operator(lsg, fp64_mode, n):
+    """The complex128 residual replacement of a mixed complex solve in both
+    arithmetics: a mixed solve with max_iter = 0 and a nonzero x0 reports
+    ||b - A x0|| / ||b|| from its first replacement pass (double-float march by
+    default, the shift's imaginary part in the centre weight); the complex128
+    FP64 operator (lsg_apply) gives the reference value."""
+    import torch
+    g = torch.Generator().manual_seed(7)
+
+    def crand(scale):
+        re = torch.rand((n, n, n), generator=g, dtype=torch.float64) - 0.5
+        im = torch.rand((n, n, n), generator=g, dtype=torch.float64) - 0.5
+        return (scale * torch.complex(re, im)).cuda()
+
+    x0 = crand(1.0)
+    b = crand(1e-3)
+    op = lsg.Operator(n, a=-float(n * n), sigma=complex(3.0, 7.5))
+    for mode in (0, 1):
+        fp64_mode(mode)
+        # with a shift the solve first moves x0's constant mode to mean(b) / sigma
+        # and then forms the residual: the returned x is that x0
+        x, r = lsg.aar_mixed(op, b, x0.clone(), max_iter=0)
+        ref = ((b - lsg.apply(op, x)).norm() / b.norm()).item()
+        assert r["relres"] == pytest.approx(ref, rel=1e-12), (mode, r["relres"], ref)
+
+
+def test_complex_mixed_solve_both_arithmetics(lsg, fp64_mode):
+    """A complex mixed solve reaches the same true (complex128) residual with
+    the double-float and the FP64-arithmetic residual replacements."""
+    import torch
+    n = 24
+    g = torch.Generator().manual_seed(11)
+    b = torch.complex(torch.rand((n, n, n), generator=g, dtype=torch.float64) - 0.5,
+                      torch.rand((n, n, n), generator=g, dtype=torch.float64) - 0.5).cuda()
+    op = lsg.Operator(n, a=-float(n * n), sigma=complex(2.0, 4.0))
+    iters = []
+    for mode in (0, 1):
+        fp64_mode(mode)
+        x, r = lsg.aar_mixed(op, b, tol=1e-9)
+        assert r["status"] == 0 and r["relres"] <= 1e-9, (mode, r)
+        true = ((b - lsg.apply(op, x)).norm() / b.norm()).item()
+        assert true <= 1e-9 * 1.01, (mode, true)
+        iters.append(r["iters"])
+    assert abs(iters[0] - iters[1]) <= 12, iters
