@@ -608,14 +608,20 @@ def other_workloads(dev):
     return res
 
 
-def run_case(case: str):
+def run_case(case: str, tune_file=None):
     """Short fixed invocations for profilers (ncu): one launch pattern each.
 
     rich32 / rich64: 6 AAR iterations (FP32 / FP64 vectors) of the 256^3
     workload -- the initial residual, five fused Richardson steps and one
     Anderson step (Gram, m x m solve, update, residual).
     mixed / fp64: one complete solve of the benchmark workload.
-    Launch shapes are autotuned first, as in the benchmark run.
+    helmholtz: the 48-instance complex shifted-Helmholtz batch (mixed, tol
+    1e-8) twice, a warm-up and the one in the "solve" range.
+    Launch shapes are autotuned first, as in the benchmark run.  tune_file:
+    when it exists, the shapes are read from it instead (a profiler slows
+    every launch, the tuner's timings too); otherwise they are tuned and
+    saved there, so a plain run followed by the profiled run of the same
+    command profiles the plain run's shapes.
     """
     import torch
 
@@ -623,9 +629,28 @@ def run_case(case: str):
     import workloads
 
     torch.cuda.set_device(0)
+    if case == "helmholtz":
+        batch = workloads.helmholtz_batch(2024)
+        ops = [lsg.Operator(m, a=-float(m * m), sigma=s) for m, s, _ in batch]
+        bs = [torch.from_numpy(v).cuda() for _, _, v in batch]
+        lsg.aar_batched(ops, bs, mixed=True, tol=1e-8)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("solve")
+        xs, rs = lsg.aar_batched(ops, bs, mixed=True, tol=1e-8)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        print(json.dumps({"case": case, "instances": len(rs), "iters_max": max(r["iters"] for r in rs),
+                          "seconds": rs[0]["seconds"], "launches": rs[0]["launches"],
+                          "converged": sum(r["status"] == 0 for r in rs)}))
+        return 0
     op = lsg.Operator(N_GRID)
     b = torch.from_numpy(workloads.uniform_rhs(N_GRID, SEED)).cuda()
-    lsg.autotune(op, torch.float32 if case in ("rich32", "mixed") else torch.float64)
+    if tune_file and os.path.exists(tune_file):
+        lsg.autotune_load(tune_file)
+    else:
+        lsg.autotune(op, torch.float32 if case in ("rich32", "mixed") else torch.float64)
+        if tune_file:
+            lsg.autotune_save(tune_file)
     torch.cuda.synchronize()
     # the solve's launches sit in an NVTX range "solve" (ncu --nvtx
     # --nvtx-include "solve/" leaves out the tuner's launches)
@@ -655,11 +680,12 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the other measured workloads")
     ap.add_argument("--cpu-full", action="store_true",
                     help="time one complete CPU solve for the baseline instead of a bounded sample")
-    ap.add_argument("--case", choices=["rich32", "rich64", "mixed", "fp64"],
+    ap.add_argument("--case", choices=["rich32", "rich64", "mixed", "fp64", "helmholtz"],
                     help="run one short fixed invocation for a profiler and exit")
+    ap.add_argument("--tune-file", help="--case: launch shapes read from this file if it exists, else saved there")
     args = ap.parse_args()
     if args.case:
-        return run_case(args.case)
+        return run_case(args.case, args.tune_file)
     if args.impl == "reference":
         return run_reference(args)
     return run_lsg(args)
