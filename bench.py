@@ -617,6 +617,8 @@ def run_case(case: str, tune_file=None):
     mixed / fp64: one complete solve of the benchmark workload.
     helmholtz: the 48-instance complex shifted-Helmholtz batch (mixed, tol
     1e-8) twice, a warm-up and the one in the "solve" range.
+    icc: the first three iterations of the block-Jacobi ICC(0) AAR (8^3
+    boxes) at 128^3 (FP64, default launch shapes).
     Launch shapes are autotuned first, as in the benchmark run.  tune_file:
     when it exists, the shapes are read from it instead (a profiler slows
     every launch, the tuner's timings too); otherwise they are tuned and
@@ -642,6 +644,13 @@ def run_case(case: str, tune_file=None):
         print(json.dumps({"case": case, "instances": len(rs), "iters_max": max(r["iters"] for r in rs),
                           "seconds": rs[0]["seconds"], "launches": rs[0]["launches"],
                           "converged": sum(r["status"] == 0 for r in rs)}))
+        return 0
+    if case == "icc":
+        op = lsg.Operator(128)
+        b = torch.from_numpy(workloads.uniform_rhs(128, 1)).cuda()
+        x, info = lsg.aar_icc(op, b, block=(8, 8, 8), max_iter=3, tol=1e-8)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": case, "iters": info["iters"], "status": info["status_name"]}))
         return 0
     op = lsg.Operator(N_GRID)
     b = torch.from_numpy(workloads.uniform_rhs(N_GRID, SEED)).cuda()
@@ -680,7 +689,7 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the other measured workloads")
     ap.add_argument("--cpu-full", action="store_true",
                     help="time one complete CPU solve for the baseline instead of a bounded sample")
-    ap.add_argument("--case", choices=["rich32", "rich64", "mixed", "fp64", "helmholtz"],
+    ap.add_argument("--case", choices=["rich32", "rich64", "mixed", "fp64", "helmholtz", "icc"],
                     help="run one short fixed invocation for a profiler and exit")
     ap.add_argument("--tune-file", help="--case: launch shapes read from this file if it exists, else saved there")
     args = ap.parse_args()
