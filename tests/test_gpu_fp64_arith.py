@@ -104,13 +104,14 @@ def test_tight_tolerance_uses_fp64_arithmetic(lsg, fp64_mode):
     assert true <= 1.5e-13
 
 
-@pytest.mark.parametrize("n", [16, 37])
-def test_double_float_complex_residual_matches_fp64_operator(lsg, fp64_mode, n):
+@pytest.mark.parametrize("n, radius", [(16, 6), (37, 6), (20, 4)])
+def test_double_float_complex_residual_matches_fp64_operator(lsg, fp64_mode, n, radius):
     """The complex128 residual replacement of a mixed complex solve in both
     arithmetics: a mixed solve with max_iter = 0 and a nonzero x0 reports
     ||b - A x0|| / ||b|| from its first replacement pass (double-float march by
-    default, the shift's imaginary part in the centre weight); the complex128
-    FP64 operator (lsg_apply) gives the reference value."""
+    default, the shift's imaginary part in the centre weight; radius 4 takes
+    the generic-radius march); the complex128 FP64 operator (lsg_apply) gives
+    the reference value."""
     import torch
     g = torch.Generator().manual_seed(7)
 
@@ -121,7 +122,7 @@ def test_double_float_complex_residual_matches_fp64_operator(lsg, fp64_mode, n):
 
     x0 = crand(1.0)
     b = crand(1e-3)
-    op = lsg.Operator(n, a=-float(n * n), sigma=complex(3.0, 7.5))
+    op = lsg.Operator(n, radius=radius, a=-float(n * n), sigma=complex(3.0, 7.5))
     for mode in (0, 1):
         fp64_mode(mode)
         # with a shift the solve first moves x0's constant mode to mean(b) / sigma
