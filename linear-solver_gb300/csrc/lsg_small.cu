@@ -545,10 +545,11 @@ __global__ void finalize_gram_solve_kernel(double *partials, int nparts, int kin
     gram_solve_tail(vals, bad, kind, m, hscale, ctrl);
 }
 
-// Complex Hermitian Gram: sums the (re, im) partials, builds the real 2m x 2m
-// representation [[A, -B], [B, A]] of G = A + iB (same singular values, each
-// twice) and right-hand side [Re h; Im h], and solves it with zgelsd's cutoff
-// sigma < eps * sigma_max (PETSC_COMPLEX/AAR_Complex.c:239, rcond = -1).
+// Complex Hermitian Gram: from the summed (re, im) values, builds the real
+// 2m x 2m representation [[A, -B], [B, A]] of G = A + iB (same singular
+// values, each twice) and right-hand side [Re h; Im h], and solves it with
+// zgelsd's cutoff sigma < eps * sigma_max (PETSC_COMPLEX/AAR_Complex.c:239,
+// rcond = -1).
 __device__ void gram_solve_c_tail(const double *vals, int bad, int m, double hre, double him, DevCtrl *ctrl) {
     constexpr int M2MAX = LSG_MAX_M;
     __shared__ double G[M2MAX * M2MAX], V[M2MAX * M2MAX], W[M2MAX * M2MAX];
