@@ -259,8 +259,9 @@ __device__ __forceinline__ void stencil_march(const Geom &g, const Weights<T> &w
 // double-float arithmetic on the FP32 pipe (lsg_df.cuh): the register ring and
 // the staged plane hold (hi, lo) float pairs (one per part for complex128,
 // DfMarch below), formed once per value with integer and FP32 operations; Au
-// is formed with error-free TwoSum / FMA two-product steps.  Each point's sum is evaluated in the same order in every tile
-// shape, so results do not depend on the launch shape.  Functors opt in with
+// is formed with error-free TwoSum / FMA two-product steps.  Each point's sum
+// is evaluated in the same order in every tile shape, so results do not
+// depend on the launch shape.  Functors opt in with
 // DF = true and carry the solve's control block (the split's scale 2^k comes
 // from its ||b||; a value beyond the float range sets its df_range flag).
 // The ring advances by register moves instead of a Q-fold unrolled march:
