@@ -301,9 +301,8 @@ int lsg_pinv_solve(const double *d_A, const double *d_b, double *d_x, int m, voi
  * allocation per call -- the kernel's status word lives in a 256-byte static
  * device array that every GPU loading the library holds until exit.  m above
  * LSG_MAX_M is rejected with LSG_BAD_ARG.  The first call on a device looks up
- * that array's address and must come before any stream capture; the address
- * is cached for the life of the process, so the call must not be used after
- * cudaDeviceReset on that device.  Calls share the array: calls that overlap
+ * that array's address; the address is cached for the life of the process,
+ * so the call must not be used after cudaDeviceReset on that device.  Calls share the array: calls that overlap
  * on the GPU race.  Each call waits for `stream` (it reads the status word
  * back before returning). */
 int lsg_pinv_solve_noalloc(const double *d_A, const double *d_b, double *d_x, int m,

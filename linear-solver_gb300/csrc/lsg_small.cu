@@ -835,8 +835,7 @@ cudaError_t pinv_solve_dev(const double *A, const double *b, double *x, int m, i
 // cleared on the call's stream before each launch; calls that overlap on the
 // GPU (different streams, or threads) race on it.  The device address of the
 // array is looked up once per device by the first call made with that device
-// current, which therefore must come before any stream capture.  The address
-// is cached for the life of the process: after cudaDeviceReset (a new
+// current.  The address is cached for the life of the process: after cudaDeviceReset (a new
 // primary context) it would be stale, so the call is not to be used after a
 // device reset.  Each call waits for its stream: the status word is read back
 // before the call returns.
